@@ -1,0 +1,345 @@
+// emp_device.cuh -- device code of the EMPEROR RV log-posterior hot path.
+//
+// One kernel template evaluates the log-posterior of a batch of walkers:
+//   * a CTA holds G walker groups of L lanes (G*L = NT threads);
+//   * the CTA stages the dataset into shared memory one epoch tile at a
+//     time (coalesced global reads, a lane-chunk layout in shared memory);
+//   * each lane of a group walks a contiguous chunk of the tile's epochs
+//     sequentially, so the moving-average recurrence of the reference
+//     (support/models/moav01.model:7-15) is a per-lane loop; the chunks are
+//     joined by an affine-map scan across the group's lanes;
+//   * group sums are reduced with warp shuffles (+ shared memory across warps).
+// The same kernel also runs one half-step of the affine-invariant stretch
+// move (propose -> evaluate -> Metropolis accept) for parallel tempering.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+#include "emp_gpu.h"
+
+namespace emp {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+constexpr double kPi = 3.1415926535897932384626433832795;
+constexpr int kMaxQ = EMP_MAX_MA;
+
+// ----------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11).
+// ----------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
+#endif
+}
+
+__host__ __device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+    const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+    const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = mulhi32(M0, c.x), lo0 = M0 * c.x;
+        uint32_t hi1 = mulhi32(M1, c.z), lo1 = M1 * c.z;
+        U4 n;
+        n.x = hi1 ^ c.y ^ k0;
+        n.y = lo1;
+        n.z = hi0 ^ c.w ^ k1;
+        n.w = lo0;
+        c = n;
+        k0 += W0;
+        k1 += W1;
+    }
+    return c;
+}
+
+// purposes (third counter word)
+constexpr uint32_t kRngStretch0 = 1u;   // + half
+constexpr uint32_t kRngSwapPerm = 3u;
+constexpr uint32_t kRngSwapAcc = 4u;
+
+__host__ __device__ __forceinline__ U4 rng_draw(uint64_t seed, uint32_t index,
+                                                 uint64_t iter, uint32_t purpose) {
+    U4 c{index, (uint32_t)iter, purpose, (uint32_t)(iter >> 32)};
+    return philox(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// uniform in [0,1) with 53 random bits from two words (numpy's rand())
+__host__ __device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    uint64_t k = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+    return (double)k * (1.0 / 9007199254740992.0);
+}
+// uniform in (0,1) from one word
+__host__ __device__ __forceinline__ double u32u(uint32_t a) {
+    return ((double)a + 0.5) * (1.0 / 4294967296.0);
+}
+
+// ----------------------------------------------------------------------------
+// dataset as laid out in device memory (one system)
+// ----------------------------------------------------------------------------
+struct DevData {
+    int n;                 // epochs
+    int q;                 // MA order stored in dt arrays
+    double t0;             // acceleration origin (first epoch in time order)
+    const double* t;       // [n]
+    const double* y;       // [n]
+    const double* s2;      // [n] yerr^2
+    const double* dt;      // [q][n] lag-(c+1) time gaps, +inf where no predecessor
+    const float* t_hi;     // float-float split of t
+    const float* t_lo;
+    const float* y32;
+    const float* s2_32;
+    const float* dt32;     // [q][n]
+    const int* inst;       // [n] 0-based instrument
+};
+
+enum Mode : int { kModeLogpost = 0, kModeStretch = 1, kModeSlots = 2 };
+
+struct KArgs {
+    const emp_model_desc* md;
+    DevData d;
+    int mode;
+    int nwalk;             // walkers handled by this launch
+    int tile;              // epochs per shared-memory tile
+    // kModeLogpost
+    const double* theta;   // [nwalk][n_free]
+    const double* beta;    // [nwalk] or null
+    double* logl;
+    double* logprior;
+    double* logp;          // or null
+    // PT (kModeStretch / kModeSlots)
+    double* st_theta;      // [slots][n_free]
+    double* st_logl;
+    double* st_logprior;
+    const int* members;    // [T][W]
+    const double* betas;   // [T]
+    const int64_t* counters;
+    int* accepted;         // [T][W]
+    int W;
+    int half;
+    int step_in_sweep;
+    uint64_t seed;
+    double a;
+};
+
+// ----------------------------------------------------------------------------
+// shared memory layout (bytes), computed identically on host and device
+// ----------------------------------------------------------------------------
+struct Smem {
+    int tile_bytes;        // staged epochs
+    int group_bytes;       // per walker group
+    int off_full, off_thp, off_pc, off_ins, off_acc, off_red, off_scan, off_misc;
+    int total;
+
+    __host__ __device__ static int align16(int x) { return (x + 15) & ~15; }
+
+    __host__ __device__ void build(int prec, int q, int L, int G, int tile, int n_full,
+                                   int n_free, int n_planets, int n_ins, int acc_order) {
+        int rs = prec == EMP_PREC_FP64 ? 8 : 4;          // real size
+        int per_epoch = (prec == EMP_PREC_FP64) ? (8 * 3 + 4 + 8 * q)
+                                                : (4 * 4 + 4 + 4 * q);
+        tile_bytes = align16(per_epoch * tile + 64);
+        int o = 0;
+        off_full = o; o += align16(8 * n_full);
+        off_thp = o;  o += align16(8 * (n_free > 0 ? n_free : 1));
+        off_pc = o;   o += align16(rs * 8 * (n_planets > 0 ? n_planets : 1));
+        off_ins = o;  o += align16(rs * (2 + 2 * kMaxQ) * (n_ins > 0 ? n_ins : 1));
+        off_acc = o;  o += align16(8 * (acc_order > 0 ? acc_order : 1));
+        off_red = o;  o += align16(8 * 4 * ((L + 31) / 32));
+        off_scan = o; o += align16(rs * 2 * (kMaxQ + kMaxQ * kMaxQ) * L);
+        off_misc = o; o += 64;
+        group_bytes = align16(o);
+        total = tile_bytes + G * group_bytes;
+    }
+};
+
+// ----------------------------------------------------------------------------
+// priors (support/priors/*.prior), FP64
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ double prior_term(const emp_prior& p, double x) {
+    if (!(x >= p.lo && x <= p.hi)) return -INFINITY;    // NaN -> -inf
+    switch (p.kind) {
+        case EMP_PRIOR_UNIFORM:
+        case EMP_PRIOR_JEFFREYS:
+            return p.a0;
+        case EMP_PRIOR_NORMAL: {
+            double z = (x - p.a0) / p.a1;
+            return -0.5 * z * z - p.a2;
+        }
+        case EMP_PRIOR_BETA:
+            // ln pdf = (a-1) ln x + (b-1) ln(1-x) - ln B(a,b)
+            return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
+        default:
+            return 0.0;
+    }
+}
+
+// whole my_prior of one full theta (emp.py:190-251): free parameters in
+// block order, each Keplerian block followed by its derived priors.
+static __device__ double log_prior(const emp_model_desc* md, const double* full) {
+    double lp = 0.0;
+    int nf = md->n_free;
+    int np = md->n_planets;
+    int planet = 0;
+    for (int i = 0; i < nf; ++i) {
+        int slot = md->prior_slot[i];
+        // close finished Keplerian blocks
+        while (planet < np && slot >= md->kep_slot[planet] + 5) {
+            for (int k = 0; k < 2; ++k) {
+                const emp_prior& dp = md->derived[planet][k];
+                if (dp.kind == EMP_PRIOR_NONE) continue;
+                const double* th = full + md->kep_slot[planet];
+                double x = k == 0 ? th[3] * th[3] + th[4] * th[4] : th[1] * th[1] + th[2] * th[2];
+                lp += prior_term(dp, x);
+            }
+            ++planet;
+        }
+        emp_prior p = md->prior[i];
+        lp += prior_term(p, full[slot]);
+    }
+    while (planet < np) {
+        for (int k = 0; k < 2; ++k) {
+            const emp_prior& dp = md->derived[planet][k];
+            if (dp.kind == EMP_PRIOR_NONE) continue;
+            const double* th = full + md->kep_slot[planet];
+            double x = k == 0 ? th[3] * th[3] + th[4] * th[4] : th[1] * th[1] + th[2] * th[2];
+            lp += prior_term(dp, x);
+        }
+        ++planet;
+    }
+    return lp;
+}
+
+// ----------------------------------------------------------------------------
+// per-planet elements (FP64): per, K, phase (rad, or NAN with tp), tp, e, w
+// support/models/kep00..kep07.model prologues
+// ----------------------------------------------------------------------------
+struct Elements { double per, K, phase, tp, e, cw, sw; int use_tp; };
+
+__device__ __forceinline__ void omega_from_sc(double S, double C, double ecc, double thr,
+                                              double& cw, double& sw) {
+    if (ecc < thr) { cw = 1.0; sw = 0.0; return; }
+    double w = acos(C / sqrt(ecc));
+    if (S < 0) w = kTwoPi - w;
+    sincos(w, &sw, &cw);
+}
+
+static __device__ Elements planet_elements(int par, const double* v) {
+    Elements el;
+    el.use_tp = 0; el.tp = 0.0;
+    switch (par) {
+        case 0: case 6: {
+            el.per = par == 6 ? exp(v[0]) : v[0];
+            el.K = v[1]; el.phase = v[2]; el.e = v[3];
+            sincos(v[4], &el.sw, &el.cw);
+        } break;
+        case 1: case 7: {
+            el.per = par == 7 ? exp(v[0]) : v[0];
+            el.K = v[1]; el.phase = v[2];
+            el.e = v[3] * v[3] + v[4] * v[4];
+            omega_from_sc(v[3], v[4], el.e, 1e-6, el.cw, el.sw);
+        } break;
+        case 2: {
+            el.per = exp(v[0]);
+            double As = v[1], Ac = v[2];
+            el.K = As * As + Ac * Ac;
+            el.e = v[3] * v[3] + v[4] * v[4];
+            omega_from_sc(v[3], v[4], el.e, 1e-5, el.cw, el.sw);
+            double ph = acos(Ac / sqrt(el.K));
+            if (As < 0) ph = kTwoPi - ph;
+            el.phase = ph;
+        } break;
+        case 3: {
+            el.per = v[0]; el.K = v[1]; el.tp = v[2]; el.use_tp = 1; el.phase = 0.0;
+            el.e = v[3];
+            sincos(v[4], &el.sw, &el.cw);
+        } break;
+        case 4: default: {
+            el.per = v[0]; el.K = v[1]; el.tp = v[2]; el.use_tp = 1; el.phase = 0.0;
+            el.e = v[3] * v[3] + v[4] * v[4];
+            omega_from_sc(v[3], v[4], el.e, 1e-5, el.cw, el.sw);
+        } break;
+    }
+    return el;
+}
+
+// ----------------------------------------------------------------------------
+// Kepler solvers
+// ----------------------------------------------------------------------------
+// FP64: Danby start + Halley to |dE| <= 1e-15 (same iteration as the oracle)
+__device__ __forceinline__ void kepler_f64(double Mr, double e, double& s, double& c) {
+    double sM = sin(Mr);
+    double E = Mr + 0.85 * e * (sM > 0.0 ? 1.0 : (sM < 0.0 ? -1.0 : 0.0));
+#pragma unroll 1
+    for (int it = 0; it < 60; ++it) {
+        sincos(E, &s, &c);
+        double f = E - e * s - Mr;
+        double f1 = 1.0 - e * c;
+        double f2 = e * s;
+        double d1 = -f / f1;
+        double d = -f / (f1 + 0.5 * d1 * f2);
+        E = E + d;
+        if (fabs(d) <= 1e-15) break;
+    }
+    sincos(E, &s, &c);
+}
+
+// FP32: second-order series start, Halley until |dE| < 1e-3 (cubic
+// convergence leaves ~1e-9), final (sin E, cos E) rotated by the last step.
+__device__ __forceinline__ void kepler_f32(float M, float e, float& s, float& c) {
+    float sM, cM;
+    __sincosf(M, &sM, &cM);
+    float E = M + e * sM * (1.f + e * cM);
+    float d = 0.f;
+#pragma unroll 1
+    for (int it = 0; it < 16; ++it) {
+        __sincosf(E, &s, &c);
+        float f = E - e * s - M;
+        float f1 = 1.f - e * c;
+        float f2 = e * s;
+        d = __fdividef(f * f1, f1 * f1 - 0.5f * f * f2);
+        E -= d;
+        if (fabsf(d) < 1e-3f) break;
+    }
+    float d2 = d * d;
+    float cd = 1.f - 0.5f * d2;
+    float sd = d * (1.f - d2 * (1.f / 6.f));
+    float sn = s * cd - c * sd;
+    float cn = c * cd + s * sd;
+    s = sn; c = cn;
+}
+
+// ----------------------------------------------------------------------------
+// precision traits
+// ----------------------------------------------------------------------------
+template <int PREC> struct P;
+
+template <> struct P<EMP_PREC_FP64> {
+    using R = double;
+    // planet constants: [0]=freq [1]=phase [2]=e [3]=Kcw [4]=K sqrt(1-e^2) sw [5]=K e cw [6]=tp/use
+    static constexpr int kPC = 8;
+};
+template <> struct P<EMP_PREC_MIXED> {
+    using R = float;
+    // [0]=f_hi [1]=f_lo (cycles/day) [2]=ph_hi [3]=ph_lo (cycles) [4]=e [5]=A [6]=B [7]=C
+    static constexpr int kPC = 8;
+};
+
+// ----------------------------------------------------------------------------
+// compensated (Kahan) accumulator
+// ----------------------------------------------------------------------------
+template <typename R> struct KSum {
+    R s, c;
+    __device__ __forceinline__ void init() { s = R(0); c = R(0); }
+    __device__ __forceinline__ void add(R x) {
+        R y = x - c;
+        R t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+};
+
+}  // namespace emp

@@ -1,0 +1,676 @@
+// emp_runtime.cu -- host runtime behind the C ABI of include/emp_gpu.h.
+//
+// Owns: descriptor validation, the device dataset layout, launch-shape
+// selection, kernel dispatch, the PT sweep sequence and its CUDA-graph
+// cache.  No exception crosses the ABI; every entry returns a status.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <mutex>
+#include <numeric>
+#include <vector>
+
+#include "emp_device.cuh"
+#include "emp_pt.cuh"
+#include "emp_model_eval.cuh"
+
+namespace emp {
+using KFn = void (*)(KArgs);
+KFn get_kernel_fp64(int q, int lidx);
+KFn get_kernel_mixed(int q, int lidx);
+}  // namespace emp
+
+using namespace emp;
+
+namespace {
+
+thread_local char g_err[512] = "";
+std::atomic<int64_t> g_launches{0};
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                          \
+    do {                                                                        \
+        cudaError_t _e = (expr);                                                \
+        if (_e != cudaSuccess)                                                  \
+            return fail(EMP_E_CUDA, "%s failed: %s", #expr, cudaGetErrorString(_e)); \
+    } while (0)
+
+const int kLanes[6] = {8, 16, 32, 64, 128, 256};
+
+int lanes_index(int L) {
+    for (int i = 0; i < 6; ++i)
+        if (kLanes[i] == L) return i;
+    return -1;
+}
+
+struct GraphCache {
+    bool valid = false;
+    emp_pt_state st{};
+    emp_pt_record rec{};
+    bool has_rec = false;
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int kernels_per_launch = 0;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        valid = false;
+    }
+};
+
+}  // namespace
+
+struct emp_handle {
+    emp_model_desc md{};
+    emp_model_desc* md_dev = nullptr;
+    int n = 0;
+    int q = 0;                 // MA order evaluated on device
+    void* dbuf = nullptr;
+    DevData dd{};
+    int L[2] = {0, 0};
+    int tile[2] = {0, 0};
+    double* scratch = nullptr; // betas_used [kMaxTemps] + chain_row
+    int64_t* chain_row = nullptr;
+    int* dev2orig = nullptr;
+    cudaStream_t own = nullptr;
+    GraphCache gc;
+    bool attr_done[2][4][6] = {};
+};
+
+namespace {
+
+int validate_prior(const emp_prior& p, const char* what, int i) {
+    if (p.kind < EMP_PRIOR_UNIFORM || p.kind > EMP_PRIOR_NONE)
+        return fail(EMP_E_INVALID, "%s %d: unknown prior kind %d", what, i, p.kind);
+    if (p.kind == EMP_PRIOR_NONE) return EMP_OK;
+    if (!(p.lo <= p.hi)) return fail(EMP_E_INVALID, "%s %d: limits not ordered", what, i);
+    if (p.kind == EMP_PRIOR_NORMAL && !(p.a1 > 0))
+        return fail(EMP_E_INVALID, "%s %d: Normal scale must be > 0", what, i);
+    return EMP_OK;
+}
+
+int validate_model(const emp_model_desc* m) {
+    if (!m) return fail(EMP_E_INVALID, "model descriptor is NULL");
+    if (m->abi_version != EMP_ABI_VERSION)
+        return fail(EMP_E_INVALID, "descriptor ABI %d, library ABI %d", m->abi_version, EMP_ABI_VERSION);
+    if (m->n_full < 0 || m->n_full > EMP_MAX_PARAMS)
+        return fail(EMP_E_SIZE, "n_full=%d outside [0, %d]", m->n_full, EMP_MAX_PARAMS);
+    if (m->n_free < 1 || m->n_free > m->n_full)
+        return fail(EMP_E_INVALID, "n_free=%d outside [1, n_full=%d]", m->n_free, m->n_full);
+    if (m->n_planets < 0 || m->n_planets > EMP_MAX_PLANETS)
+        return fail(EMP_E_SIZE, "n_planets=%d outside [0, %d]", m->n_planets, EMP_MAX_PLANETS);
+    if (m->n_ins < 1 || m->n_ins > EMP_MAX_INS)
+        return fail(EMP_E_SIZE, "n_ins=%d outside [1, %d]", m->n_ins, EMP_MAX_INS);
+    if (m->ma_order < 0 || m->ma_order > EMP_MAX_MA)
+        return fail(EMP_E_SIZE, "MA order %d outside [0, %d]", m->ma_order, EMP_MAX_MA);
+    if (m->acc_order < 0 || m->acc_order > 8)
+        return fail(EMP_E_SIZE, "acceleration order %d outside [0, 8]", m->acc_order);
+    for (int p = 0; p < m->n_planets; ++p) {
+        int par = m->kep_param[p];
+        if (!(par == 0 || par == 1 || par == 2 || par == 3 || par == 4 || par == 6 || par == 7))
+            return fail(EMP_E_UNSUPPORTED, "planet %d: parameterisation %d not built", p, par);
+        if (m->kep_slot[p] < 0 || m->kep_slot[p] + 5 > m->n_full)
+            return fail(EMP_E_INVALID, "planet %d: slot %d out of range", p, m->kep_slot[p]);
+        if (p > 0 && m->kep_slot[p] < m->kep_slot[p - 1] + 5)
+            return fail(EMP_E_INVALID, "planet %d: slots overlap", p);
+        for (int k = 0; k < 2; ++k) {
+            int rc = validate_prior(m->derived[p][k], "derived prior of planet", p);
+            if (rc) return rc;
+        }
+    }
+    auto chk = [&](int slot, int count, const char* nm) -> int {
+        if (slot < 0) return EMP_OK;
+        if (slot + count > m->n_full) return fail(EMP_E_INVALID, "%s slot %d + %d > n_full", nm, slot, count);
+        return EMP_OK;
+    };
+    int rc;
+    if ((rc = chk(m->offset_slot, m->n_ins, "offset"))) return rc;
+    if ((rc = chk(m->jitter_slot, m->n_ins, "jitter"))) return rc;
+    if ((rc = chk(m->acc_slot, m->acc_order, "acceleration"))) return rc;
+    if (m->ma_order > 0) {
+        if (m->ma_slot < 0) return fail(EMP_E_INVALID, "MA order > 0 without MA slot");
+        int cnt = m->ma_global ? 2 * m->ma_order : 2 * m->ma_order * m->n_ins;
+        if ((rc = chk(m->ma_slot, cnt, "MA"))) return rc;
+    }
+    if (m->acc_order > 0 && m->acc_slot < 0) return fail(EMP_E_INVALID, "acceleration without slot");
+    std::vector<int> seen(m->n_free, 0);
+    for (int s = 0; s < m->n_full; ++s) {
+        int src = m->full_src[s];
+        if (src >= m->n_free) return fail(EMP_E_INVALID, "full_src[%d]=%d >= n_free", s, src);
+        if (src >= 0) seen[src]++;
+        else if (!isfinite(m->full_fixed[s])) return fail(EMP_E_INVALID, "fixed value of slot %d not finite", s);
+    }
+    for (int i = 0; i < m->n_free; ++i) {
+        if (seen[i] != 1) return fail(EMP_E_INVALID, "free parameter %d mapped %d times", i, seen[i]);
+        int sl = m->prior_slot[i];
+        if (sl < 0 || sl >= m->n_full || m->full_src[sl] != i)
+            return fail(EMP_E_INVALID, "prior_slot[%d]=%d inconsistent with full_src", i, sl);
+        if (i > 0 && sl <= m->prior_slot[i - 1]) return fail(EMP_E_INVALID, "prior_slot not increasing");
+        if ((rc = validate_prior(m->prior[i], "prior of free parameter", i))) return rc;
+        if (m->prior[i].kind == EMP_PRIOR_NONE)
+            return fail(EMP_E_INVALID, "free parameter %d has no prior", i);
+    }
+    return EMP_OK;
+}
+
+int pick_default_L(int prec, int n) {
+    (void)prec;
+    if (n >= 4096) return 64;
+    return 32;
+}
+
+int pick_tile(const emp_handle* h, int prec, int L, int G, Smem& lay) {
+    int want = h->tile[prec];
+    if (want <= 0) want = prec == EMP_PREC_FP64 ? 1024 : 2048;
+    // the lane-chunk layout of a tile of nt epochs occupies ceil(nt/L)*L
+    // slots, so the tile is a multiple of L
+    auto round_L = [L](int x) { return ((x + L - 1) / L) * L; };
+    int t = round_L(std::min(want, h->n));
+    t = std::max(t, L);
+    for (;;) {
+        lay.build(prec, h->q, L, G, t, h->md.n_full, h->md.n_free, h->md.n_planets, h->md.n_ins,
+                  h->md.acc_order);
+        if (lay.total <= 200 * 1024 || t <= L) break;
+        t = std::max(L, round_L(t / 2));
+    }
+    return t;
+}
+
+int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s) {
+    if (prec != EMP_PREC_FP64 && prec != EMP_PREC_MIXED)
+        return fail(EMP_E_INVALID, "precision %d unknown", prec);
+    int L = h->L[prec] > 0 ? h->L[prec] : pick_default_L(prec, h->n);
+    int li = lanes_index(L);
+    if (li < 0) return fail(EMP_E_INVALID, "lanes per walker %d not built", L);
+    int NT = L > 128 ? L : 128;
+    int G = NT / L;
+    Smem lay;
+    int tile = pick_tile(h, prec, L, G, lay);
+    if (lay.total > 227 * 1024)
+        return fail(EMP_E_SIZE, "shared memory %d B exceeds 227 KB", lay.total);
+    KFn fn = prec == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
+    if (!fn) return fail(EMP_E_UNSUPPORTED, "no kernel for q=%d L=%d", h->q, L);
+    if (!h->attr_done[prec][h->q][li]) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      227 * 1024));
+        h->attr_done[prec][h->q][li] = true;
+    }
+    a.md = h->md_dev;
+    a.d = h->dd;
+    a.tile = tile;
+    if (a.nwalk <= 0) return EMP_OK;
+    int grid = (a.nwalk + G - 1) / G;
+    fn<<<grid, NT, lay.total, s>>>(a);
+    g_launches.fetch_add(1);
+    CUDA_TRY(cudaGetLastError());
+    return EMP_OK;
+}
+
+int check_state(const emp_handle* h, const emp_pt_state* st) {
+    if (!st) return fail(EMP_E_INVALID, "state is NULL");
+    if (st->ntemps < 1 || st->ntemps > kMaxTemps)
+        return fail(EMP_E_SIZE, "ntemps=%d outside [1, %d]", st->ntemps, kMaxTemps);
+    if (st->nwalkers < 2 || (st->nwalkers & 1))
+        return fail(EMP_E_INVALID, "nwalkers=%d must be even and >= 2", st->nwalkers);
+    if (st->ndim != h->md.n_free)
+        return fail(EMP_E_INVALID, "state ndim=%d but model has %d free parameters", st->ndim, h->md.n_free);
+    if (st->nsteps < 1) return fail(EMP_E_INVALID, "nsteps=%d < 1", st->nsteps);
+    if (!st->theta || !st->logl || !st->logprior || !st->members || !st->betas || !st->counters ||
+        !st->accepted || !st->swaps_accepted || !st->perm_units)
+        return fail(EMP_E_INVALID, "a state buffer is NULL");
+    if (st->n_perm_units < 1) return fail(EMP_E_INVALID, "no permutation units");
+    if (st->precision != EMP_PREC_FP64 && st->precision != EMP_PREC_MIXED)
+        return fail(EMP_E_INVALID, "precision %d unknown", st->precision);
+    if (st->adapt && st->adapt_mode != 0)
+        return fail(EMP_E_UNSUPPORTED, "adapt_mode %d not built (0 is)", st->adapt_mode);
+    if (!(st->a > 1.0)) return fail(EMP_E_INVALID, "stretch scale a=%g must be > 1", st->a);
+    if (st->adapt && !(st->adapt_tau > 0 && st->adapt_nu > 0))
+        return fail(EMP_E_INVALID, "adapt_tau and adapt_nu must be > 0");
+    return EMP_OK;
+}
+
+int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec,
+                  cudaStream_t s, int* nkern) {
+    int rc;
+    int kcount = 0;
+    for (int step = 0; step < st->nsteps; ++step) {
+        for (int half = 0; half < 2; ++half) {
+            KArgs a{};
+            a.mode = kModeStretch;
+            a.nwalk = st->ntemps * (st->nwalkers / 2);
+            a.st_theta = st->theta;
+            a.st_logl = st->logl;
+            a.st_logprior = st->logprior;
+            a.members = st->members;
+            a.betas = st->betas;
+            a.counters = st->counters;
+            a.accepted = st->accepted;
+            a.W = st->nwalkers;
+            a.half = half;
+            a.step_in_sweep = step;
+            a.seed = st->seed;
+            a.a = st->a;
+            if ((rc = launch_eval(h, st->precision, a, s))) return rc;
+            ++kcount;
+        }
+    }
+    SwapArgs S{};
+    S.T = st->ntemps; S.W = st->nwalkers; S.D = st->ndim; S.nsteps = st->nsteps;
+    S.theta = st->theta; S.logl = st->logl; S.members = st->members; S.betas = st->betas;
+    S.counters = st->counters; S.swaps_accepted = st->swaps_accepted;
+    S.units = st->perm_units; S.nunits = st->n_perm_units;
+    S.adapt = st->adapt; S.adapt_mode = st->adapt_mode;
+    S.adapt_tau = st->adapt_tau; S.adapt_nu = st->adapt_nu; S.seed = st->seed;
+    S.betas_used = h->scratch;
+    S.chain_row = h->chain_row;
+    bool have_rec = rec && rec->n_recorded;
+    S.beta_hist = have_rec ? rec->beta_history : nullptr;
+    S.tsw_hist = have_rec ? rec->tsw_history : nullptr;
+    S.smd_hist = have_rec ? rec->smd_history : nullptr;
+    S.n_rec = have_rec ? rec->n_recorded : h->chain_row + 1;   // dummy pair when not recording
+    S.cap = have_rec ? rec->capacity : 0;
+    S.thin = have_rec ? std::max(1, rec->thin) : 1;
+    S.record_chain = have_rec && (rec->chain || rec->log_like || rec->log_prob);
+    int nth = std::min(1024, std::max(32, ((st->nwalkers + 31) / 32) * 32));
+    k_swap<<<1, nth, 0, s>>>(S);
+    g_launches.fetch_add(1);
+    ++kcount;
+    CUDA_TRY(cudaGetLastError());
+    if (S.record_chain) {
+        RecArgs R{};
+        R.T = st->ntemps; R.W = st->nwalkers; R.D = st->ndim;
+        R.theta = st->theta; R.logl = st->logl; R.logprior = st->logprior;
+        R.members = st->members; R.betas_used = h->scratch; R.chain_row = h->chain_row;
+        R.chain = rec->chain; R.log_like = rec->log_like; R.log_prob = rec->log_prob;
+        int64_t tot = (int64_t)st->ntemps * st->nwalkers * (rec->chain ? st->ndim : 1);
+        int grid = (int)std::min<int64_t>(std::max<int64_t>(1, (tot + 255) / 256), 152 * 8);
+        k_record<<<grid, 256, 0, s>>>(R);
+        g_launches.fetch_add(1);
+        ++kcount;
+        CUDA_TRY(cudaGetLastError());
+    }
+    if (nkern) *nkern = kcount;
+    return EMP_OK;
+}
+
+bool same_state(const emp_pt_state& a, const emp_pt_state& b) {
+    return memcmp(&a, &b, sizeof(a)) == 0;
+}
+bool same_rec(const emp_pt_record& a, const emp_pt_record& b) {
+    return memcmp(&a, &b, sizeof(a)) == 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int emp_abi_version(void) { return EMP_ABI_VERSION; }
+
+const char* emp_last_error_string(void) { return g_err; }
+
+int64_t emp_launch_count(void) { return g_launches.load(); }
+
+int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_handle** out) {
+    if (!out) return fail(EMP_E_INVALID, "out is NULL");
+    *out = nullptr;
+    int rc = validate_model(model);
+    if (rc) return rc;
+    if (!data) return fail(EMP_E_INVALID, "dataset descriptor is NULL");
+    if (data->n_systems != 1)
+        return fail(EMP_E_UNSUPPORTED, "n_systems=%d: this entry takes one system", data->n_systems);
+    if (!data->offsets || !data->t || !data->y || !data->yerr || !data->inst)
+        return fail(EMP_E_INVALID, "a dataset array is NULL");
+    const int64_t n64 = data->offsets[1] - data->offsets[0];
+    if (n64 <= 0) return fail(EMP_E_INVALID, "system has %lld epochs", (long long)n64);
+    if (n64 > (1 << 26)) return fail(EMP_E_SIZE, "%lld epochs exceed 2^26", (long long)n64);
+    const int n = (int)n64;
+    const int64_t o = data->offsets[0];
+    const double* t = data->t + o;
+    const double* y = data->y + o;
+    const double* ye = data->yerr + o;
+    const int32_t* in = data->inst + o;
+    for (int i = 0; i < n; ++i) {
+        if (!isfinite(t[i]) || !isfinite(y[i]) || !isfinite(ye[i]))
+            return fail(EMP_E_INVALID, "epoch %d has a non-finite value", i);
+        if (in[i] < 1 || in[i] > model->n_ins)
+            return fail(EMP_E_INVALID, "epoch %d: instrument %d outside 1..%d", i, in[i], model->n_ins);
+        if (i > 0 && t[i] < t[i - 1]) return fail(EMP_E_INVALID, "times not sorted at epoch %d", i);
+    }
+
+    emp_handle* h = new (std::nothrow) emp_handle();
+    if (!h) return fail(EMP_E_INVALID, "out of host memory");
+    h->md = *model;
+    h->n = n;
+    const bool ma_on = model->ma_order > 0 && (model->ma_global || !model->ma_quirk);
+    h->q = ma_on ? model->ma_order : 0;
+    const bool group_by_ins = ma_on && !model->ma_global;
+
+    // epoch order: per-instrument MA needs each instrument's subsequence
+    // contiguous (time order kept inside); otherwise time order.
+    std::vector<int> order(n);
+    std::iota(order.begin(), order.end(), 0);
+    if (group_by_ins)
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return in[a] < in[b]; });
+    const int q = h->q;
+    std::vector<double> ht(n), hy(n), hs2(n), hdt((size_t)std::max(q, 1) * n);
+    std::vector<float> tf_hi(n), tf_lo(n), yf(n), s2f(n), dtf((size_t)std::max(q, 1) * n);
+    std::vector<int> hin(n);
+    for (int i = 0; i < n; ++i) {
+        int k = order[i];
+        ht[i] = t[k];
+        hy[i] = y[k];
+        hs2[i] = ye[k] * ye[k];
+        hin[i] = in[k] - 1;
+        tf_hi[i] = (float)t[k];
+        tf_lo[i] = (float)(t[k] - (double)tf_hi[i]);
+        yf[i] = (float)y[k];
+        s2f[i] = (float)hs2[i];
+    }
+    for (int c = 0; c < q; ++c) {
+        for (int i = 0; i < n; ++i) {
+            // predecessor at lag c+1 inside the same sequence (instrument or global)
+            int lag = c + 1;
+            double v = INFINITY;
+            if (i - lag >= 0 && (!group_by_ins || hin[i - lag] == hin[i])) v = fabs(ht[i] - ht[i - lag]);
+            hdt[(size_t)c * n + i] = v;
+            dtf[(size_t)c * n + i] = (float)v;
+        }
+    }
+    // one device allocation for the dataset + descriptor + scratch
+    size_t qn = (size_t)std::max(q, 1) * n;
+    size_t bytes = 0;
+    auto take = [&](size_t b) { size_t off = bytes; bytes += (b + 255) & ~(size_t)255; return off; };
+    size_t o_t = take(8 * (size_t)n), o_y = take(8 * (size_t)n), o_s2 = take(8 * (size_t)n);
+    size_t o_dt = take(8 * qn);
+    size_t o_th = take(4 * (size_t)n), o_tl = take(4 * (size_t)n), o_yf = take(4 * (size_t)n);
+    size_t o_sf = take(4 * (size_t)n), o_dtf = take(4 * qn), o_in = take(4 * (size_t)n);
+    size_t o_perm = take(4 * (size_t)n);
+    size_t o_md = take(sizeof(emp_model_desc));
+    size_t o_sc = take(8 * (kMaxTemps + 4));
+    cudaError_t e = cudaMalloc(&h->dbuf, bytes);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(EMP_E_CUDA, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    char* b = (char*)h->dbuf;
+    struct Cp { size_t off; const void* src; size_t n; } cps[] = {
+        {o_t, ht.data(), 8 * (size_t)n}, {o_y, hy.data(), 8 * (size_t)n}, {o_s2, hs2.data(), 8 * (size_t)n},
+        {o_dt, hdt.data(), 8 * qn}, {o_th, tf_hi.data(), 4 * (size_t)n}, {o_tl, tf_lo.data(), 4 * (size_t)n},
+        {o_yf, yf.data(), 4 * (size_t)n}, {o_sf, s2f.data(), 4 * (size_t)n}, {o_dtf, dtf.data(), 4 * qn},
+        {o_in, hin.data(), 4 * (size_t)n}, {o_perm, order.data(), 4 * (size_t)n},
+        {o_md, model, sizeof(emp_model_desc)}};
+    for (auto& c : cps) {
+        e = cudaMemcpy(b + c.off, c.src, c.n, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(h->dbuf);
+            delete h;
+            return fail(EMP_E_CUDA, "cudaMemcpy failed: %s", cudaGetErrorString(e));
+        }
+    }
+    h->md_dev = (emp_model_desc*)(b + o_md);
+    h->dev2orig = (int*)(b + o_perm);
+    h->scratch = (double*)(b + o_sc);
+    h->chain_row = (int64_t*)(h->scratch + kMaxTemps);
+    h->dd.n = n;
+    h->dd.q = q;
+    h->dd.t0 = t[0];
+    h->dd.t = (const double*)(b + o_t);
+    h->dd.y = (const double*)(b + o_y);
+    h->dd.s2 = (const double*)(b + o_s2);
+    h->dd.dt = (const double*)(b + o_dt);
+    h->dd.t_hi = (const float*)(b + o_th);
+    h->dd.t_lo = (const float*)(b + o_tl);
+    h->dd.y32 = (const float*)(b + o_yf);
+    h->dd.s2_32 = (const float*)(b + o_sf);
+    h->dd.dt32 = (const float*)(b + o_dtf);
+    h->dd.inst = (const int*)(b + o_in);
+    e = cudaMemset(h->scratch, 0, 8 * (kMaxTemps + 4));
+    if (e != cudaSuccess) {
+        cudaFree(h->dbuf);
+        delete h;
+        return fail(EMP_E_CUDA, "cudaMemset failed: %s", cudaGetErrorString(e));
+    }
+    *out = h;
+    return EMP_OK;
+}
+
+int emp_destroy(emp_handle* h) {
+    if (!h) return EMP_OK;
+    h->gc.reset();
+    if (h->own) cudaStreamDestroy(h->own);
+    if (h->dbuf) cudaFree(h->dbuf);
+    delete h;
+    return EMP_OK;
+}
+
+int emp_set_launch(emp_handle* h, int precision, int lanes_per_walker, int tile_epochs) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (precision != EMP_PREC_FP64 && precision != EMP_PREC_MIXED)
+        return fail(EMP_E_INVALID, "precision %d unknown", precision);
+    if (lanes_per_walker != 0 && lanes_index(lanes_per_walker) < 0)
+        return fail(EMP_E_INVALID, "lanes per walker %d not in {8,16,32,64,128,256}", lanes_per_walker);
+    if (tile_epochs < 0 || tile_epochs > 16384)
+        return fail(EMP_E_INVALID, "tile %d outside [0, 16384]", tile_epochs);
+    h->L[precision] = lanes_per_walker;
+    h->tile[precision] = tile_epochs;
+    h->gc.reset();
+    return EMP_OK;
+}
+
+int emp_get_launch(emp_handle* h, int precision, int* lanes_per_walker, int* tile_epochs) {
+    if (!h || !lanes_per_walker || !tile_epochs) return fail(EMP_E_INVALID, "NULL argument");
+    if (precision != EMP_PREC_FP64 && precision != EMP_PREC_MIXED)
+        return fail(EMP_E_INVALID, "precision %d unknown", precision);
+    int L = h->L[precision] > 0 ? h->L[precision] : pick_default_L(precision, h->n);
+    int NT = L > 128 ? L : 128;
+    Smem lay;
+    *lanes_per_walker = L;
+    *tile_epochs = pick_tile(h, precision, L, NT / L, lay);
+    return EMP_OK;
+}
+
+int emp_logpost(emp_handle* h, const double* theta, int B, const int32_t* system_of,
+                const double* beta, double* logl, double* logprior, double* logp, int precision,
+                void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (B < 0) return fail(EMP_E_INVALID, "B=%d < 0", B);
+    if (B == 0) return EMP_OK;
+    if (!theta || !logl || !logprior) return fail(EMP_E_INVALID, "theta/logl/logprior NULL");
+    if (system_of != nullptr)
+        return fail(EMP_E_UNSUPPORTED, "system_of is for ragged datasets (one system loaded)");
+    KArgs a{};
+    a.mode = kModeLogpost;
+    a.nwalk = B;
+    a.theta = theta;
+    a.beta = beta;
+    a.logl = logl;
+    a.logprior = logprior;
+    a.logp = logp;
+    return launch_eval(h, precision, a, (cudaStream_t)stream);
+}
+
+int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, double* err2,
+                   void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (B < 0) return fail(EMP_E_INVALID, "B=%d < 0", B);
+    if (B == 0) return EMP_OK;
+    if (B > 65535) return fail(EMP_E_SIZE, "B=%d > 65535", B);
+    if (!theta || !model || !err2) return fail(EMP_E_INVALID, "NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    const emp_model_desc& m = h->md;
+    size_t sm = 8 * ((size_t)m.n_full + 8 * std::max(m.n_planets, 1) + 2 * m.n_ins + std::max(m.acc_order, 1));
+    dim3 grid((unsigned)std::min(64, (h->n + 255) / 256), (unsigned)B);
+    k_model_mean<<<grid, 256, sm, s>>>(h->md_dev, h->dd, h->dev2orig, theta, model, err2);
+    g_launches.fetch_add(1);
+    CUDA_TRY(cudaGetLastError());
+    if (h->q > 0) {
+        k_model_ma<<<(B + 127) / 128, 128, 0, s>>>(h->md_dev, h->dd, h->dev2orig, theta, B, model);
+        g_launches.fetch_add(1);
+        CUDA_TRY(cudaGetLastError());
+    }
+    return EMP_OK;
+}
+
+int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    int rc = check_state(h, st);
+    if (rc) return rc;
+    KArgs a{};
+    a.mode = kModeSlots;
+    a.nwalk = st->ntemps * st->nwalkers;
+    a.st_theta = st->theta;
+    a.st_logl = st->logl;
+    a.st_logprior = st->logprior;
+    return launch_eval(h, st->precision, a, (cudaStream_t)stream);
+}
+
+int emp_pt_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    int rc = check_state(h, st);
+    if (rc) return rc;
+    return enqueue_sweep(h, st, rec, (cudaStream_t)stream, nullptr);
+}
+
+int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, int nsweeps,
+               int use_graph, void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    int rc = check_state(h, st);
+    if (rc) return rc;
+    if (nsweeps < 0) return fail(EMP_E_INVALID, "nsweeps=%d < 0", nsweeps);
+    if (nsweeps == 0) return EMP_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!use_graph) {
+        for (int i = 0; i < nsweeps; ++i)
+            if ((rc = enqueue_sweep(h, st, rec, s, nullptr))) return rc;
+        return EMP_OK;
+    }
+    // graphs are captured and launched on a non-legacy stream
+    cudaStream_t ls = s;
+    if (s == nullptr || s == cudaStreamLegacy) {
+        if (!h->own) CUDA_TRY(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
+        ls = h->own;
+    }
+    emp_pt_record rcopy{};
+    bool has_rec = rec != nullptr;
+    if (has_rec) rcopy = *rec;
+    GraphCache& gc = h->gc;
+    if (!(gc.valid && gc.stream == ls && same_state(gc.st, *st) && gc.has_rec == has_rec &&
+          (!has_rec || same_rec(gc.rec, rcopy)))) {
+        gc.reset();
+        // first eager sweep sets kernel attributes outside capture
+        // (capture forbids cudaFuncSetAttribute side effects on some drivers)
+        int L = h->L[st->precision] > 0 ? h->L[st->precision] : pick_default_L(st->precision, h->n);
+        int li = lanes_index(L);
+        KFn fn = st->precision == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
+        if (fn && !h->attr_done[st->precision][h->q][li]) {
+            CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          227 * 1024));
+            h->attr_done[st->precision][h->q][li] = true;
+        }
+        CUDA_TRY(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
+        int nk = 0;
+        int64_t before = g_launches.load();
+        rc = enqueue_sweep(h, st, has_rec ? &rcopy : nullptr, ls, &nk);
+        g_launches.store(before);   // captured, not launched
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ls, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess) return fail(EMP_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec = nullptr;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return fail(EMP_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        }
+        gc.graph = graph;
+        gc.exec = exec;
+        gc.st = *st;
+        gc.rec = rcopy;
+        gc.has_rec = has_rec;
+        gc.stream = ls;
+        gc.kernels_per_launch = nk;
+        gc.valid = true;
+    }
+    cudaEvent_t ev = nullptr;
+    if (ls != s) {
+        CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventRecord(ev, s));
+        CUDA_TRY(cudaStreamWaitEvent(ls, ev, 0));
+    }
+    for (int i = 0; i < nsweeps; ++i) {
+        cudaError_t e = cudaGraphLaunch(gc.exec, ls);
+        if (e != cudaSuccess) {
+            if (ev) cudaEventDestroy(ev);
+            return fail(EMP_E_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+        }
+        g_launches.fetch_add(gc.kernels_per_launch);
+    }
+    if (ls != s) {
+        CUDA_TRY(cudaEventRecord(ev, ls));
+        CUDA_TRY(cudaStreamWaitEvent(s, ev, 0));
+        cudaEventDestroy(ev);
+    }
+    return EMP_OK;
+}
+
+int emp_probe_peaks(double* fp32_flops, double* fp64_flops, void* stream) {
+    if (!fp32_flops || !fp64_flops) return fail(EMP_E_INVALID, "NULL output");
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    cudaStream_t s = (cudaStream_t)stream;
+    void* out = nullptr;
+    CUDA_TRY(cudaMalloc(&out, 8 * 4096));
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    const int blocks = sms * 8, threads = 256;
+    double res[2] = {0, 0};
+    for (int which = 0; which < 2; ++which) {
+        int iters = which == 0 ? 4096 : 64;
+        float best = 1e30f;
+        for (int rep = 0; rep < 4; ++rep) {
+            cudaEventRecord(e0, s);
+            if (which == 0) k_fma_probe<float><<<blocks, threads, 0, s>>>((float*)out, iters, 1.0f);
+            else k_fma_probe<double><<<blocks, threads, 0, s>>>((double*)out, iters, 1.0);
+            cudaEventRecord(e1, s);
+            g_launches.fetch_add(1);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e != cudaSuccess) {
+                cudaFree(out);
+                return fail(EMP_E_CUDA, "probe: %s", cudaGetErrorString(e));
+            }
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0) best = std::min(best, ms);
+        }
+        double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+        res[which] = flops / (best * 1e-3);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    *fp32_flops = res[0];
+    *fp64_flops = res[1];
+    return EMP_OK;
+}
+
+}  // extern "C"

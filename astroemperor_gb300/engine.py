@@ -1,0 +1,477 @@
+"""GPU parallel-tempering engine with reddemcee's ``PTSampler`` surface.
+
+EMPEROR constructs ``reddemcee.PTSampler(nwalkers, ndim, my_likelihood,
+my_prior, ntemps=..., pool=..., backend=..., betas=..., tsw_history=...,
+smd_history=..., adapt_tau=..., adapt_nu=..., adapt_mode=...)``
+(``src/astroemperor/emp.py:576-593``), runs ``sampler.run_mcmc(p, nsweeps,
+nsteps, progress)`` (``support/endit_reddemcee.scr:3``,
+``endit_freeze1.scr:9-12``) and reads ``get_chain/get_log_like/
+get_log_prob/get_betas/get_tsw/get_smd/get_autocorr_time/
+get_evidence_ti``, ``betas`` and ``backend[t]`` (``emp.py:961-967,
+1375-1447``).  This class keeps that surface, but the two callables are
+replaced by a compiled :class:`~astroemperor_gb300.model.ReddModel`, and the
+walker state, the sweep loop and every history live in device memory.
+
+Per sweep the device runs ``nsteps`` affine-invariant stretch moves
+(Goodman & Weare 2010; emcee 3 ``StretchMove``, a = 2) on every
+temperature, adjacent-temperature swaps from the hottest pair down, and
+(while adaptation is on) the Vousden et al. 2016 ladder update.  Random
+numbers come from Philox4x32-10 keyed by ``seed``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .model import ReddModel
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+def default_betas(ntemps: int) -> np.ndarray:
+    """Geometric ladder beta_t = 7**-t.
+
+    The reference's recorded runs with the default ladder end at
+    beta_9 = 2.478e-08 = 7**-9 (10 temperatures, ``tests/01_51peg_basic.ipynb``)
+    and beta_11 = 5.057e-10 = 7**-11 (12 temperatures,
+    ``tests/00_mini_test.ipynb``).
+    """
+    return 7.0 ** -np.arange(ntemps, dtype=np.float64)
+
+
+def perm_units(W: int) -> np.ndarray:
+    """Multipliers m with gcd(m, W) = 1: j -> (m j + b) mod W is a bijection."""
+    return np.array([m for m in range(1, max(W, 2)) if math.gcd(m, W) == 1] or [1], dtype=np.int32)
+
+
+class Context:
+    """Native handle: compiled model + dataset resident on one GPU."""
+
+    def __init__(self, model: ReddModel, device='cuda:0'):
+        self.lib = N.load()
+        self.device = torch.device(device)
+        if self.device.type != 'cuda':
+            raise ValueError('the EMPEROR GPU engine runs on a CUDA device')
+        torch.cuda.set_device(self.device)
+        torch.cuda.init()
+        self.model = model
+        self.md = model.descriptor()
+        d = model.data
+        self._t = np.ascontiguousarray(d.BJD, dtype=np.float64)
+        self._y = np.ascontiguousarray(d.RV, dtype=np.float64)
+        self._e = np.ascontiguousarray(d.eRV, dtype=np.float64)
+        self._i = np.ascontiguousarray(d.Flag, dtype=np.int32)
+        self._o = np.array([0, len(self._t)], dtype=np.int64)
+        ds = N.EmpDatasetDesc()
+        ds.n_systems = 1
+        ds.offsets = self._o.ctypes.data_as(C.POINTER(C.c_int64))
+        ds.t = self._t.ctypes.data_as(C.POINTER(C.c_double))
+        ds.y = self._y.ctypes.data_as(C.POINTER(C.c_double))
+        ds.yerr = self._e.ctypes.data_as(C.POINTER(C.c_double))
+        ds.inst = self._i.ctypes.data_as(C.POINTER(C.c_int32))
+        h = C.c_void_p()
+        N.call('emp_create', C.byref(self.md), C.byref(ds), C.byref(h))
+        self.h = h
+
+    def close(self):
+        if getattr(self, 'h', None):
+            self.lib.emp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_launch(self, precision: int, lanes: int, tile: int):
+        N.call('emp_set_launch', self.h, int(precision), int(lanes), int(tile))
+
+    def get_launch(self, precision: int):
+        L, T = C.c_int(), C.c_int()
+        N.call('emp_get_launch', self.h, int(precision), C.byref(L), C.byref(T))
+        return L.value, T.value
+
+    def logpost(self, theta: torch.Tensor, precision: int = N.EMP_PREC_MIXED,
+                beta: Optional[torch.Tensor] = None, stream=None):
+        """(logL, logprior) of theta [B, ndim] (device FP64)."""
+        theta = theta.contiguous()
+        B = theta.shape[0]
+        logl = torch.empty(B, dtype=torch.float64, device=theta.device)
+        logprior = torch.empty_like(logl)
+        logp = torch.empty_like(logl) if beta is not None else None
+        s = stream if stream is not None else torch.cuda.current_stream(theta.device)
+        N.call('emp_logpost', self.h, _ptr(theta), B, None,
+               _ptr(beta) if beta is not None else None, _ptr(logl), _ptr(logprior),
+               _ptr(logp) if logp is not None else None, int(precision), s.cuda_stream)
+        if beta is not None:
+            return logl, logprior, logp
+        return logl, logprior
+
+
+    def model_eval(self, theta: torch.Tensor, stream=None):
+        """my_model(theta) on the device: (model0, err20), each [B, ndata], FP64."""
+        theta = theta.contiguous()
+        B = theta.shape[0]
+        n = len(self._t)
+        model = torch.empty(B, n, dtype=torch.float64, device=theta.device)
+        err2 = torch.empty_like(model)
+        s = stream if stream is not None else torch.cuda.current_stream(theta.device)
+        N.call('emp_model_eval', self.h, _ptr(theta), B, _ptr(model), _ptr(err2), s.cuda_stream)
+        return model, err2
+
+
+PRECISIONS = {'fp64': N.EMP_PREC_FP64, 'mixed': N.EMP_PREC_MIXED,
+              N.EMP_PREC_FP64: N.EMP_PREC_FP64, N.EMP_PREC_MIXED: N.EMP_PREC_MIXED}
+
+
+class PTState:
+    """What ``run_mcmc`` returns; pass it back to continue on the device."""
+
+    def __init__(self, sampler):
+        self.sampler = sampler
+
+    @property
+    def coords(self):
+        return self.sampler._coords_host()
+
+    @property
+    def log_like(self):
+        return self.sampler._logl_host()
+
+    @property
+    def log_prob(self):
+        return self.sampler._logp_host()
+
+    @property
+    def betas(self):
+        return self.sampler.betas
+
+
+class _TempBackend:
+    """``sampler.backend[t]`` view (emcee-style backend of one temperature)."""
+
+    def __init__(self, sampler, t):
+        self.s, self.t = sampler, t
+
+    @property
+    def iteration(self):
+        return self.s.iteration
+
+    def get_chain(self, **kw):
+        return self.s.get_chain(**kw)[self.t]
+
+    def get_log_like(self, **kw):
+        return self.s.get_log_like(**kw)[self.t]
+
+    def get_log_prob(self, **kw):
+        return self.s.get_log_prob(**kw)[self.t]
+
+    def get_betas(self, **kw):
+        return self.s.get_betas(**kw)[:, self.t]
+
+    @property
+    def accepted(self):
+        return self.s.accepted[self.t]
+
+
+class _Backend:
+    def __init__(self, sampler):
+        self.s = sampler
+
+    def __getitem__(self, t):
+        return _TempBackend(self.s, t)
+
+    def __len__(self):
+        return self.s.ntemps
+
+    @property
+    def iteration(self):
+        return self.s.iteration
+
+    @property
+    def tsw_history_bool(self):
+        return self.s.tsw_history_bool
+
+    @property
+    def smd_history_bool(self):
+        return self.s.smd_history_bool
+
+    @property
+    def tsw_history(self):
+        return self.s.get_tsw()
+
+    @property
+    def smd_history(self):
+        return self.s.get_smd()
+
+
+class PTSampler:
+    """reddemcee-compatible parallel-tempering sampler on one GPU.
+
+    ``log_likelihood``/``log_prior`` positional arguments of reddemcee are
+    replaced by ``model`` (a compiled :class:`ReddModel`).  Extra keywords:
+    ``precision`` ('mixed' or 'fp64'), ``seed``, ``a`` (stretch scale),
+    ``device``, ``use_graph``.
+    """
+
+    def __init__(self, nwalkers, ndim, model: ReddModel, ntemps=5, pool=None, backend=None,
+                 betas=None, tsw_history=True, smd_history=True, adapt_tau=1000, adapt_nu=1,
+                 adapt_mode=0, precision='mixed', seed=None, a=2.0, device='cuda:0',
+                 use_graph=True, moves=None, context: Optional[Context] = None):
+        if model.ndim__ != ndim:
+            raise ValueError(f'ndim={ndim} but the model has {model.ndim__} free parameters')
+        if nwalkers % 2:
+            raise ValueError('nwalkers must be even (the stretch move splits the ensemble in two)')
+        if adapt_mode != 0:
+            raise NotImplementedError('adapt_mode 0 (swap-rate equalisation) is the built ladder rule')
+        self.model = model
+        self.nwalkers, self.ndim = int(nwalkers), int(ndim)
+        if betas is not None:
+            betas = np.asarray(betas, dtype=np.float64)
+            ntemps = len(betas)
+        else:
+            betas = default_betas(int(ntemps))
+        self.ntemps = int(ntemps)
+        self.tsw_history_bool = bool(tsw_history)
+        self.smd_history_bool = bool(smd_history)
+        self.adapt_tau, self.adapt_nu, self.adapt_mode = float(adapt_tau), float(adapt_nu), int(adapt_mode)
+        self.adaptive = True
+        self.precision = PRECISIONS[precision]
+        self.a = float(a)
+        self.use_graph = bool(use_graph)
+        if seed is None:
+            seed = int(np.random.randint(0, 2 ** 62))
+        self.seed = int(seed)
+        self.ctx = context if context is not None else Context(model, device)
+        self.device = self.ctx.device
+        self.stream = torch.cuda.Stream(device=self.device)
+        self.D_ = None
+        self.pool = pool
+        T, W, D = self.ntemps, self.nwalkers, self.ndim
+        dev = self.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.theta = torch.zeros(T * W, D, **f64)
+        self.logl = torch.full((T * W,), -math.inf, **f64)
+        self.logprior = torch.full((T * W,), -math.inf, **f64)
+        self.members = torch.arange(T * W, **i32)
+        self.betas_d = torch.tensor(betas, **f64)
+        self.counters = torch.zeros(4, dtype=torch.int64, device=dev)
+        self.accepted_d = torch.zeros(T * W, **i32)
+        self.swaps_d = torch.zeros(T, **i32)
+        self.units = torch.tensor(perm_units(W), **i32)
+        self.n_rec = torch.zeros(2, dtype=torch.int64, device=dev)
+        self.cap = 0
+        self.chain = self.log_like_h = self.log_prob_h = None
+        self.beta_h = self.tsw_h = self.smd_h = None
+        self._initialised = False
+        self.backend = _Backend(self)
+
+    # ------------------------------------------------------------------
+    def _state_struct(self, nsteps: int) -> N.EmpPtState:
+        st = N.EmpPtState()
+        st.ntemps, st.nwalkers, st.ndim, st.nsteps = self.ntemps, self.nwalkers, self.ndim, int(nsteps)
+        st.theta, st.logl, st.logprior = _ptr(self.theta), _ptr(self.logl), _ptr(self.logprior)
+        st.members, st.betas, st.counters = _ptr(self.members), _ptr(self.betas_d), _ptr(self.counters)
+        st.accepted, st.swaps_accepted = _ptr(self.accepted_d), _ptr(self.swaps_d)
+        st.perm_units, st.n_perm_units = _ptr(self.units), int(self.units.numel())
+        st.adapt = 1 if self.adaptive else 0
+        st.seed = self.seed & ((1 << 64) - 1)
+        st.a = self.a
+        st.adapt_tau, st.adapt_nu, st.adapt_mode = self.adapt_tau, self.adapt_nu, self.adapt_mode
+        st.precision = self.precision
+        return st
+
+    def _record_struct(self) -> N.EmpPtRecord:
+        r = N.EmpPtRecord()
+        r.capacity = self.cap
+        r.thin = 1
+        r.chain, r.log_like, r.log_prob = _ptr(self.chain), _ptr(self.log_like_h), _ptr(self.log_prob_h)
+        r.beta_history = _ptr(self.beta_h)
+        r.tsw_history = _ptr(self.tsw_h) if self.tsw_history_bool else None
+        r.smd_history = _ptr(self.smd_h) if self.smd_history_bool else None
+        r.n_recorded = _ptr(self.n_rec)
+        return r
+
+    def _grow(self, extra: int):
+        T, W, D = self.ntemps, self.nwalkers, self.ndim
+        used = int(self.n_rec[0].item()) if self.cap else 0
+        newcap = used + int(extra)
+        f64 = dict(dtype=torch.float64, device=self.device)
+
+        def grow(old, shape):
+            new = torch.zeros((newcap,) + shape, **f64)
+            if old is not None and used:
+                new[:used] = old[:used]
+            return new
+        self.chain = grow(self.chain, (T, W, D))
+        self.log_like_h = grow(self.log_like_h, (T, W))
+        self.log_prob_h = grow(self.log_prob_h, (T, W))
+        self.beta_h = grow(self.beta_h, (T,))
+        self.tsw_h = grow(self.tsw_h, (max(T - 1, 1),))
+        self.smd_h = grow(self.smd_h, (max(T - 1, 1),))
+        self.cap = newcap
+
+    def set_positions(self, p0):
+        """Load walker positions [ntemps, nwalkers, ndim] and evaluate them."""
+        p0 = np.asarray(p0, dtype=np.float64)
+        if p0.shape != (self.ntemps, self.nwalkers, self.ndim):
+            raise ValueError(f'p0 shape {p0.shape} != {(self.ntemps, self.nwalkers, self.ndim)}')
+        with torch.cuda.stream(self.stream):
+            self.theta.copy_(torch.from_numpy(p0.reshape(-1, self.ndim)).pin_memory(), non_blocking=True)
+            self.members.copy_(torch.arange(self.ntemps * self.nwalkers, dtype=torch.int32, device=self.device))
+        st = self._state_struct(1)
+        N.call('emp_pt_evaluate', self.ctx.h, C.byref(st), self.stream.cuda_stream)
+        self._initialised = True
+
+    def run_mcmc(self, initial_state, nsweeps, nsteps=1, progress=False, use_graph=None):
+        """``nsweeps`` sweeps of ``nsteps`` stretch steps + swaps (+ adaptation)."""
+        if isinstance(initial_state, PTState) and initial_state.sampler is self and self._initialised:
+            pass
+        else:
+            p0 = initial_state.coords if isinstance(initial_state, PTState) else initial_state
+            self.set_positions(p0)
+        nsweeps = int(nsweeps)
+        self._grow(nsweeps)
+        st = self._state_struct(nsteps)
+        rec = self._record_struct()
+        ug = self.use_graph if use_graph is None else bool(use_graph)
+        N.call('emp_pt_run', self.ctx.h, C.byref(st), C.byref(rec), nsweeps, 1 if ug else 0,
+               self.stream.cuda_stream)
+        self.stream.synchronize()
+        return PTState(self)
+
+    def sweep_host(self, h_theta, h_logl, h_logprior, use_graph=None):
+        """One sweep with the walker state kept in (pinned) host memory.
+
+        Copies the slot-ordered state (theta [T*W, ndim], logl, logprior)
+        to the device, runs one sweep, copies it back, and waits; the
+        temperature membership table stays on the device.
+        """
+        if not self._initialised:
+            raise RuntimeError('run_mcmc or set_positions first')
+        s = self.stream
+        with torch.cuda.stream(s):
+            self.theta.copy_(h_theta, non_blocking=True)
+            self.logl.copy_(h_logl, non_blocking=True)
+            self.logprior.copy_(h_logprior, non_blocking=True)
+        if self.cap == 0:
+            self._grow(1)
+        st = self._state_struct(1)
+        rec = self._record_struct()
+        ug = self.use_graph if use_graph is None else bool(use_graph)
+        N.call('emp_pt_run', self.ctx.h, C.byref(st), C.byref(rec), 1, 1 if ug else 0, s.cuda_stream)
+        with torch.cuda.stream(s):
+            h_theta.copy_(self.theta, non_blocking=True)
+            h_logl.copy_(self.logl, non_blocking=True)
+            h_logprior.copy_(self.logprior, non_blocking=True)
+        s.synchronize()
+
+    def select_adjustment(self, name='00'):
+        """Freeze the ladder (endit_freeze1.scr:11 calls ``select_adjustment('00')``)."""
+        if str(name) in ('00', '0', 'none', 'None'):
+            self.adaptive = False
+        else:
+            raise ValueError(f'adjustment {name!r} not built')
+
+    @property
+    def config_adaptation_halflife(self):
+        return self.adapt_tau if self.adaptive else 0
+
+    @config_adaptation_halflife.setter
+    def config_adaptation_halflife(self, v):
+        # endit_freeze.scr:37 sets 0 to stop adapting
+        if not v:
+            self.adaptive = False
+        else:
+            self.adaptive = True
+            self.adapt_tau = float(v)
+
+    # ------------------------------------------------------------------ accessors
+    @property
+    def betas(self):
+        return self.betas_d.detach().cpu().numpy().copy()
+
+    @property
+    def iteration(self):
+        return int(self.n_rec[0].item()) if self.cap else 0
+
+    def _coords_host(self):
+        T, W = self.ntemps, self.nwalkers
+        return self.theta[self.members.long()].reshape(T, W, self.ndim).cpu().numpy()
+
+    def _logl_host(self):
+        return self.logl[self.members.long()].reshape(self.ntemps, self.nwalkers).cpu().numpy()
+
+    def _logp_host(self):
+        b = self.betas_d.repeat_interleave(self.nwalkers)
+        m = self.members.long()
+        lp = self.logprior[m]
+        out = torch.where(lp > -math.inf, b * self.logl[m] + lp, torch.full_like(lp, -math.inf))
+        return out.reshape(self.ntemps, self.nwalkers).cpu().numpy()
+
+    @property
+    def accepted(self):
+        return self.accepted_d.reshape(self.ntemps, self.nwalkers).cpu().numpy()
+
+    @property
+    def acceptance_fraction(self):
+        it = max(self.iteration, 1)
+        return self.accepted / float(it)
+
+    def _hist(self, buf, discard=0, thin=1):
+        n = self.iteration
+        return buf[:n][int(discard)::int(thin)]
+
+    def get_chain(self, flat=False, thin=1, discard=0):
+        """Per temperature: [S, W, D] (or [S*W, D] with flat=True)."""
+        c = self._hist(self.chain, discard, thin).cpu().numpy()      # [S, T, W, D]
+        c = np.moveaxis(c, 1, 0)                                       # [T, S, W, D]
+        if flat:
+            return c.reshape(self.ntemps, -1, self.ndim)
+        return c
+
+    def get_log_like(self, flat=False, thin=1, discard=0):
+        c = np.moveaxis(self._hist(self.log_like_h, discard, thin).cpu().numpy(), 1, 0)
+        return c.reshape(self.ntemps, -1) if flat else c
+
+    def get_log_prob(self, flat=False, thin=1, discard=0):
+        c = np.moveaxis(self._hist(self.log_prob_h, discard, thin).cpu().numpy(), 1, 0)
+        return c.reshape(self.ntemps, -1) if flat else c
+
+    def get_betas(self, discard=0, thin=1):
+        return self._hist(self.beta_h, discard, thin).cpu().numpy()
+
+    def get_tsw(self, discard=0, thin=1):
+        return self._hist(self.tsw_h, discard, thin).cpu().numpy()[:, :max(self.ntemps - 1, 0)]
+
+    def get_smd(self, discard=0, thin=1):
+        return self._hist(self.smd_h, discard, thin).cpu().numpy()[:, :max(self.ntemps - 1, 0)]
+
+    def get_autocorr_time(self, discard=0, thin=1, c=5, tol=50, quiet=False):
+        """Integrated autocorrelation time per temperature and parameter
+        (emcee's estimator: FFT autocorrelation, automated window c)."""
+        from .stats import integrated_time
+        ch = self.get_chain(discard=discard, thin=thin)
+        return np.array([integrated_time(ch[t], c=c, tol=tol, quiet=quiet) * thin
+                         for t in range(self.ntemps)])
+
+    def get_evidence_ti(self, discard=0, pchip=True):
+        """Thermodynamic integration of <log L>_beta over the ladder."""
+        from .stats import thermodynamic_integration
+        ll = self.get_log_like(discard=discard)
+        return thermodynamic_integration(self.betas, ll, pchip=pchip)
+
+    get_evidence_hybrid = get_evidence_ti
+    get_evidence_ss = get_evidence_ti
+
+    def get_func(self, name, kwargs=None):
+        return getattr(self, name)(**(kwargs or {}))

@@ -1,0 +1,453 @@
+"""Model description: parameters, blocks, default priors, and the compiled
+device descriptor.
+
+Mirrors the reference's model layer for the blocks on the hot path:
+
+* ``Parameter`` / ``Parameter_Block``  -- ``src/astroemperor/emp_model.py:16-170``
+* block factories ``KeplerianBlock``, ``OffsetBlock``, ``JitterBlock``,
+  ``MOAVBlock``, ``AccelerationBlock`` -- ``src/astroemperor/block_repo.py:22-240``
+* parameter defaults (names, ``is_hou``) -- ``src/astroemperor/param_repo.py:15-180``
+* ``SmartSetter`` data-derived limits and priors -- ``block_repo.py:505-868``
+* ``ReddModel.refresh__`` theta index maps -- ``emp_model.py:223-330``
+
+Instead of generating Python text for ``my_model``/``my_prior`` the model is
+compiled into an ``emp_model_desc`` (``include/emp_gpu.h``) that the CUDA
+kernels interpret.
+"""
+from __future__ import annotations
+
+import copy
+import itertools
+import math
+
+import numpy as np
+from scipy.special import betaln, ndtr
+
+from . import _native as N
+
+# ---------------------------------------------------------------------------
+# parameter defaults (param_repo.py)
+# ---------------------------------------------------------------------------
+_DEFAULTS = {
+    'dPeriod': ('Period', False), 'dAmplitude': ('Amplitude', False),
+    'dPhase': ('Phase', False), 'dEccentricity': ('Eccentricity', False),
+    'dLongitude': ('Longitude', False), 'dlPeriod': ('lPeriod', False),
+    'dAmp_sin': ('Amp_sin', True), 'dAmp_cos': ('Amp_cos', True),
+    'dEcc_sin': ('Ecc_sin', True), 'dEcc_cos': ('Ecc_cos', True),
+    'dT_0': ('T_0', False), 'dM0': ('M0', False),
+    'dOffset': ('Offset', False), 'dJitter': ('Jitter', False),
+    'dMACoefficient': ('MACoefficient', False), 'dMATimescale': ('MATimescale', False),
+    'dAcceleration': ('Acceleration', False),
+}
+
+# Keplerian parameter lists per parameterisation (block_repo.py:23-31)
+KEPLER_PARAMS = {
+    0: ['dPeriod', 'dAmplitude', 'dPhase', 'dEccentricity', 'dLongitude'],
+    1: ['dPeriod', 'dAmplitude', 'dPhase', 'dEcc_sin', 'dEcc_cos'],
+    2: ['dlPeriod', 'dAmp_sin', 'dAmp_cos', 'dEcc_sin', 'dEcc_cos'],
+    3: ['dPeriod', 'dAmplitude', 'dT_0', 'dEccentricity', 'dLongitude'],
+    4: ['dPeriod', 'dAmplitude', 'dT_0', 'dEcc_sin', 'dEcc_cos'],
+    6: ['dlPeriod', 'dAmplitude', 'dPhase', 'dEccentricity', 'dLongitude'],
+    7: ['dlPeriod', 'dAmplitude', 'dPhase', 'dEcc_sin', 'dEcc_cos'],
+}
+
+
+class Parameter:
+    """One parameter with the reference's attribute names (emp_model.py:16-30)."""
+
+    def __init__(self, key_or_name, **attrs):
+        name, is_hou = _DEFAULTS.get(key_or_name, (key_or_name, False))
+        self.name = name
+        self.prior = 'Uniform'
+        self.limits = [None, None]
+        self.init_pos = [None, None]
+        self.prargs = None
+        self.fixed = None
+        self.is_hou = is_hou
+        self.has_prior = True
+        self.has_posterior = True
+        self.value = -np.inf
+        for k, v in attrs.items():
+            setattr(self, k, v)
+
+    def __repr__(self):
+        return self.name
+
+    def as_spec(self):
+        return {'name': self.name, 'prior': self.prior, 'limits': list(self.limits),
+                'prargs': copy.deepcopy(self.prargs), 'fixed': self.fixed,
+                'has_prior': self.has_prior}
+
+
+class Parameter_Block:
+    """A block of parameters (emp_model.py:32-170)."""
+
+    def __init__(self, params, **attrs):
+        self.list_ = list(params)
+        self.additional_parameters = []
+        self.parameterisation = None
+        self.number_ = 0
+        self.moav = 0
+        self.is_global = False
+        for k, v in attrs.items():
+            setattr(self, k, v)
+        self.refresh_block()
+
+    def refresh_block(self):
+        fixed = [p.fixed for p in self]
+        nf = np.array([f is None for f in fixed], dtype=bool)
+        self.C_ = np.arange(len(self))[nf]
+        self.A_ = np.arange(len(self))[~nf]
+        for i in self.A_:
+            p = self.list_[i]
+            p.value = p.fixed
+            p.prior = 'Fixed'
+        self.ndim_ = int(nf.sum())
+
+    def get_attr(self, name):
+        return [getattr(p, name) for p in self]
+
+    def set_attr(self, name, values):
+        for p, v in zip(self, values):
+            setattr(p, name, v)
+
+    def __len__(self):
+        return len(self.list_)
+
+    def __iter__(self):
+        return iter(self.list_)
+
+    def __getitem__(self, i):
+        return self.list_[i]
+
+    def __repr__(self):
+        return f'{self.name_}({self.ndim_}): {self.list_}'
+
+
+def KeplerianBlock(parameterisation: int, number: int) -> Parameter_Block:
+    """block_repo.py:22-72 (parameterisations 0-4, 6, 7)."""
+    if parameterisation not in KEPLER_PARAMS:
+        raise ValueError(f'Keplerian parameterisation {parameterisation} is not on this path')
+    ps = [Parameter(k) for k in KEPLER_PARAMS[parameterisation]]
+    if number:
+        for p in ps:
+            p.name += f' {number}'
+    return Parameter_Block(ps, name_=f'KeplerianBlock {number}', type_='Keplerian',
+                           class_='Model', parameterisation=parameterisation, number_=number)
+
+
+def OffsetBlock(nins: int) -> Parameter_Block:
+    """block_repo.py:103-134."""
+    ps = []
+    for i in range(nins):
+        p = Parameter('dOffset')
+        p.name += f' {i + 1}'
+        ps.append(p)
+    return Parameter_Block(ps, name_='OffsetBlock', type_='Offset', class_='Data', number_=nins)
+
+
+def JitterBlock(nins: int) -> Parameter_Block:
+    """block_repo.py:176-203."""
+    ps = []
+    for i in range(nins):
+        p = Parameter('dJitter')
+        p.name += f' {i + 1}'
+        ps.append(p)
+    return Parameter_Block(ps, name_='JitterBlock', type_='Jitter', class_='Data', number_=nins)
+
+
+def MOAVBlock(nins: int, moav_args: dict) -> Parameter_Block:
+    """block_repo.py:206-240: (coefficient, timescale) per instrument and order."""
+    order = int(moav_args['order'])
+    is_global = bool(moav_args['global'])
+    rng = 1 if is_global else nins
+    ps = []
+    for i, j in itertools.product(range(rng), range(order)):
+        pc = Parameter('dMACoefficient')
+        pc.name += f' {i + 1} Order {j + 1}'
+        pt = Parameter('dMATimescale')
+        pt.name += f' {i + 1} Order {j + 1}'
+        ps.extend((pc, pt))
+    return Parameter_Block(ps, name_='MOAVBlock', type_='MOAV', class_='Data', number_=nins,
+                           moav=order, is_global=is_global)
+
+
+def AccelerationBlock(order: int) -> Parameter_Block:
+    """block_repo.py:137-173."""
+    ps = []
+    for i in range(order):
+        p = Parameter('dAcceleration')
+        if i > 0:
+            p.name = f'Acceleration Order {i + 1}'
+        ps.append(p)
+    return Parameter_Block(ps, name_=f'AccelerationBlock o{order}', type_='Acceleration',
+                           class_='Data', number_=order)
+
+
+class SmartSetter:
+    """Data-derived default limits and priors (block_repo.py:505-868)."""
+
+    def __init__(self, data):
+        self.data = data
+        self.angular = [0, 2 * np.pi]
+
+    def _amp_per(self):
+        sig = float(np.std(self.data.RV))            # pandas std(ddof=0)
+        per = float(self.data.BJD.max() - self.data.BJD.min())
+        return sig * np.sqrt(4), per
+
+    def set_Keplerian(self, b, ecc_limits=(0, 1), ecc_prargs=(0, 0.1)):
+        amp, per = self._amp_per()
+        uni = 'Uniform'
+        par = b.parameterisation
+        add_ecc = False
+        ecc_extra_prargs = None
+        if par == 0:
+            lims = [[1.5, per], [1e-6, amp], self.angular, list(ecc_limits), self.angular]
+            priors = [uni, uni, uni, 'Normal', uni]
+            prargs = [None, None, None, list(ecc_prargs), None]
+        elif par == 1:
+            lims = [[1.5, per], [1e-6, amp], self.angular, [-1, 1], [-1, 1]]
+            priors, prargs = [uni] * 5, [None] * 5
+            add_ecc = True
+        elif par == 2:
+            kamp = np.sqrt(amp / 2)
+            lims = [[np.log(1.5), np.log(per)], [-kamp, kamp], [-kamp, kamp], [-1, 1], [-1, 1]]
+            priors, prargs = [uni] * 5, [None] * 5
+            add_ecc = True
+        elif par == 3:
+            lims = [[1.5, per], [1e-6, amp], [-1000, 1000], list(ecc_limits), self.angular]
+            priors = [uni, uni, uni, 'Normal', uni]
+            prargs = [None, None, None, list(ecc_prargs), None]
+        elif par == 4:
+            lims = [[1.5, per], [1e-6, amp], [-1000, 1000], [-1, 1], [-1, 1]]
+            priors, prargs = [uni] * 5, [None] * 5
+            add_ecc = True
+        elif par == 6:
+            lims = [[np.log(1.5), np.log(per)], [1e-6, amp], self.angular, list(ecc_limits), self.angular]
+            priors = ['Jeffreys', uni, uni, 'Normal', uni]
+            prargs = [None, None, None, list(ecc_prargs), None]
+        elif par == 7:
+            lims = [[np.log(1.5), np.log(per)], [1e-6, amp], self.angular, [-1, 1], [-1, 1]]
+            priors = ['Jeffreys', uni, uni, uni, uni]
+            prargs = [None] * 5
+            add_ecc = True
+            ecc_extra_prargs = list(ecc_prargs)
+        else:
+            raise ValueError(par)
+        if add_ecc:   # ecc_w_add_additional (block_repo.py:666-688)
+            e = Parameter('dEccentricity', has_prior=True, limits=[0, 1])
+            if ecc_extra_prargs is not None:
+                e.prior = 'Normal'
+                e.prargs = ecc_extra_prargs
+            w = Parameter('dLongitude', has_prior=False, limits=list(self.angular))
+            for ap in (e, w):
+                if b.number_:
+                    ap.name += f' {b.number_}'
+            b.additional_parameters = [e, w]
+        return lims, priors, prargs
+
+    def _per_ins_absmax(self, b):
+        out = []
+        for nin in range(b.number_):
+            m = self.data.Flag == (nin + 1)
+            out.append(float(np.max(np.abs(self.data.RV[m]))))
+        return out
+
+    def set_Offset(self, b, **kw):
+        lims = [[-a, a] for a in self._per_ins_absmax(b)]
+        return lims, ['Uniform'] * len(lims), [None] * len(lims)
+
+    def set_Jitter(self, b, jit_prargs=(5, 5), **kw):
+        lims = [[1e-5, a] for a in self._per_ins_absmax(b)]
+        return lims, ['Normal'] * len(lims), [list(jit_prargs) for _ in lims]
+
+    def set_MOAV(self, b, **kw):
+        lims, priors, prargs = [], [], []
+        n = 1 if b.is_global else b.number_
+        for _ in range(n):
+            for _ in range(b.moav):
+                lims += [[0.0, 0.3], [5, 25]]
+                priors += ['Uniform', 'Uniform']
+                prargs += [None, None]
+        return lims, priors, prargs
+
+    def set_Acceleration(self, b, **kw):
+        return [[-1, 1]] * b.number_, ['Uniform'] * b.number_, [None] * b.number_
+
+    def __call__(self, block, **kw):
+        lims, priors, prargs = getattr(self, f'set_{block.type_}')(block, **kw)
+        block.set_attr('limits', [list(l) for l in lims])
+        block.set_attr('prior', priors)
+        block.set_attr('prargs', prargs)
+
+
+# ---------------------------------------------------------------------------
+# prior arguments (emp_model.py:82-120)
+# ---------------------------------------------------------------------------
+def prior_struct(prior: str, limits, prargs) -> N.EmpPrior:
+    """One compiled prior; the normalisers follow ``_check_prargs``."""
+    p = N.EmpPrior()
+    if prior in (None, 'None'):
+        p.kind = N.EMP_PRIOR_NONE
+        return p
+    if prior not in N.PRIOR_KIND:
+        raise ValueError(f'prior {prior!r} is not on this path '
+                         '(Uniform, Normal, Jeffreys, Beta, Fixed)')
+    low, high = float(limits[0]), float(limits[1])
+    p.kind = N.PRIOR_KIND[prior]
+    p.lo, p.hi = low, high
+    if prior in ('Uniform', 'Jeffreys'):
+        p.a0 = float(np.log(1 / (high - low)))
+    elif prior == 'Normal':
+        mu, s = float(prargs[0]), float(prargs[1])
+        a, b = (low - mu) / s, (high - mu) / s
+        logZ = float(np.log(ndtr(b) - ndtr(a)))
+        p.a0, p.a1 = mu, s
+        p.a2 = float(np.log(s * np.sqrt(2 * np.pi))) + logZ
+    elif prior == 'Beta':
+        a, b = float(prargs[0]), float(prargs[1])
+        p.a0, p.a1, p.a2 = a, b, float(betaln(a, b))
+    return p
+
+
+class ReddModel:
+    """The run's model: blocks, theta layout, spec and device descriptor.
+
+    Restates ``ReddModel.refresh__`` (emp_model.py:223-330): global slices,
+    free (``C_``) and fixed (``A_``) index maps, ``ndim__``.
+    """
+
+    HOT_TYPES = ('Keplerian', 'Acceleration', 'Offset', 'Jitter', 'MOAV')
+
+    def __init__(self, blocks, data, moav_reference_quirk=False):
+        self.blocks = list(blocks)
+        self.data = data
+        self.moav_reference_quirk = bool(moav_reference_quirk)
+        self.refresh__()
+
+    def __iter__(self):
+        return iter(self.blocks)
+
+    def refresh__(self):
+        blen = 0
+        self.ndim__ = 0
+        for b in self.blocks:
+            if b.type_ not in self.HOT_TYPES:
+                raise ValueError(f'block type {b.type_} is not on the GPU hot path')
+            b.refresh_block()
+            b.slice = slice(blen, blen + len(b))
+            blen += len(b)
+            self.ndim__ += b.ndim_
+        self.n_full = blen
+        fixed = [p.fixed for b in self.blocks for p in b]
+        free = np.array([f is None for f in fixed], dtype=bool)
+        self.C_ = np.arange(blen)[free]
+        self.A_ = np.arange(blen)[~free]
+        self.mod_fixed = np.array(fixed, dtype=object)
+        self.kplan__ = sum(1 for b in self.blocks if b.type_ == 'Keplerian')
+        self.nins__ = self.data.nins
+        # the MOAV residual is taken after every mean-model block
+        seen_moav = False
+        for b in self.blocks:
+            if b.type_ == 'MOAV':
+                seen_moav = True
+            elif seen_moav and b.type_ in ('Keplerian', 'Acceleration', 'Offset'):
+                raise ValueError('MOAV block must follow the Keplerian, acceleration and offset blocks')
+
+    # plain dict spec (used by the CPU oracle in tests)
+    def spec(self) -> dict:
+        out = []
+        for b in self.blocks:
+            d = {'type': b.type_, 'params': [p.as_spec() for p in b]}
+            if b.type_ == 'Keplerian':
+                d['parameterisation'] = b.parameterisation
+                d['additional'] = [p.as_spec() for p in b.additional_parameters]
+            if b.type_ == 'MOAV':
+                d['order'] = b.moav
+                d['global'] = b.is_global
+            out.append(d)
+        return {'nins': self.nins__, 'blocks': out,
+                'moav_reference_quirk': self.moav_reference_quirk}
+
+    def free_parameters(self):
+        return [p for b in self.blocks for p in b if p.fixed is None]
+
+    def limits_free(self) -> np.ndarray:
+        return np.array([list(map(float, p.limits)) for p in self.free_parameters()])
+
+    def descriptor(self) -> N.EmpModelDesc:
+        """Compile to ``emp_model_desc``."""
+        if self.n_full > N.EMP_MAX_PARAMS:
+            raise ValueError(f'{self.n_full} parameters exceed {N.EMP_MAX_PARAMS}')
+        md = N.EmpModelDesc()
+        md.abi_version = N.EMP_ABI_VERSION
+        md.n_full = self.n_full
+        md.n_free = self.ndim__
+        md.n_ins = self.nins__
+        md.offset_slot = md.jitter_slot = md.ma_slot = md.acc_slot = -1
+        planet = 0
+        free_i = 0
+        for b in self.blocks:
+            s0 = b.slice.start
+            if b.type_ == 'Keplerian':
+                if planet >= N.EMP_MAX_PLANETS:
+                    raise ValueError('too many Keplerians')
+                md.kep_param[planet] = b.parameterisation
+                md.kep_slot[planet] = s0
+                md.derived[planet][0] = prior_struct('None', None, None)
+                md.derived[planet][1] = prior_struct('None', None, None)
+                for ap in b.additional_parameters:
+                    if not getattr(ap, 'has_prior', False):
+                        continue
+                    if ap.name[:3] == 'Ecc':
+                        md.derived[planet][0] = prior_struct(ap.prior, ap.limits, ap.prargs)
+                    elif ap.name[:3] == 'Amp':
+                        md.derived[planet][1] = prior_struct(ap.prior, ap.limits, ap.prargs)
+                planet += 1
+            elif b.type_ == 'Offset':
+                md.offset_slot = s0
+            elif b.type_ == 'Jitter':
+                md.jitter_slot = s0
+            elif b.type_ == 'MOAV':
+                if b.moav > N.EMP_MAX_MA:
+                    raise ValueError(f'MA order {b.moav} > {N.EMP_MAX_MA}')
+                md.ma_slot = s0
+                md.ma_order = b.moav
+                md.ma_global = int(b.is_global)
+                md.ma_quirk = int(self.moav_reference_quirk)
+            elif b.type_ == 'Acceleration':
+                md.acc_slot = s0
+                md.acc_order = len(b)
+            for i, p in enumerate(b):
+                slot = s0 + i
+                if p.fixed is None:
+                    md.full_src[slot] = free_i
+                    md.full_fixed[slot] = 0.0
+                    md.prior_slot[free_i] = slot
+                    if p.prior == 'Fixed':
+                        raise ValueError(f'{p.name}: free parameter with a Fixed prior')
+                    md.prior[free_i] = prior_struct(p.prior, p.limits, p.prargs)
+                    free_i += 1
+                else:
+                    md.full_src[slot] = -1
+                    md.full_fixed[slot] = float(p.fixed)
+        md.n_planets = planet
+        md.loglike_const = float(- 0.5 * np.log(2 * np.pi) * self.data.ndata)
+        return md
+
+
+def full_theta(model: ReddModel, theta):
+    """np.insert of the fixed values (emp_model.py:709-711) for a batch."""
+    theta = np.atleast_2d(np.asarray(theta, dtype=np.float64))
+    out = np.empty((theta.shape[0], model.n_full))
+    out[:, model.C_] = theta
+    for a in model.A_:
+        out[:, a] = float(model.mod_fixed[a])
+    return out
+
+
+def normal_logZ(low, high, mu, s) -> float:
+    """ln(Phi(b) - Phi(a)) of a truncated normal (emp_model.py:90-94)."""
+    a, b = (low - mu) / s, (high - mu) / s
+    return math.log(ndtr(b) - ndtr(a))

@@ -1,0 +1,294 @@
+"""EMPEROR's user surface for the RV + parallel-tempering path.
+
+Mirrors the parts of ``Simulation`` (``src/astroemperor/emp.py:2240-2916``)
+that drive the hot path, with the same attribute names and call order::
+
+    sim = Simulation()
+    sim.load_data('51Peg')                       # {read_loc}datafiles/51Peg/RV/*.vels
+    sim.set_engine('reddemcee')
+    sim.engine_config['setup'] = [10, 256, 2048, 1]
+    sim.keplerian_parameterisation = 1
+    sim.add_condition(['Period 1', 'limits', [3, 5]])
+    sim.autorun(0, 1)
+
+Instead of writing a temporary script and running it in a child
+interpreter (``emp.py:137-175, 2559-2582``), ``run`` compiles the model
+(:class:`~astroemperor_gb300.model.ReddModel`) and runs the GPU
+:class:`~astroemperor_gb300.engine.PTSampler` in-process.  Plotting,
+logging and astrometry/GP blocks are not part of this path.
+"""
+from __future__ import annotations
+
+import itertools
+import time
+
+import numpy as np
+
+from .data import RVData, load_target, preprocess_instruments
+from .model import (AccelerationBlock, JitterBlock, KeplerianBlock, MOAVBlock, OffsetBlock,
+                    ReddModel, SmartSetter, full_theta)
+from .stats import model_stats
+
+
+class Simulation:
+    def __init__(self):
+        # emp.py:33-133 defaults used on this path
+        self.starname = None
+        self.read_loc = ''
+        self.save_loc = ''
+        self.blocks__ = []
+        self.conds = []
+        self.kplanets__ = 0
+        self.nins__ = 0
+        self.acceleration = 0
+        self.keplerian_parameterisation = 0
+        self.switch_jitter = True
+        self.switch_first_run = True
+        self.moav = {'order': 0, 'global': False}
+        self.moav_reference_quirk = False
+        self.eccentricity_limits = [0, 1]
+        self.eccentricity_prargs = [0, 0.1]
+        self.jitter_limits = [0, 1]
+        self.jitter_prargs = [5, 5]
+        self.instrument_names_RV = None
+        self.starmass = 1.
+        self.cores__ = 1
+        self.engine__ = None
+        self.engine_config = {}
+        self.run_config = {}
+        self._crit_current = 'BIC'
+        self._crit_tolerance = 5
+        self.BIC = np.inf
+        self.like_max = -np.inf
+        self.post_max = -np.inf
+        self.sampler = None
+        self.model = None
+        self.my_data = None
+        self.history = []
+        self.time_run = 0.0
+
+    # ------------------------------------------------------------------ data
+    def load_data(self, folder_name):
+        """emp.py:2263-2312 (RV mode)."""
+        self.starname = folder_name
+        self.my_data = load_target(folder_name, read_loc=self.read_loc)
+        self._after_data()
+
+    def load_arrays(self, instruments, labels=None, name='custom'):
+        """Same as load_data for in-memory per-instrument (BJD, RV, eRV) arrays."""
+        self.starname = name
+        self.my_data = preprocess_instruments(instruments, labels)
+        self._after_data()
+
+    def _after_data(self):
+        self.nins__ = self.my_data.nins
+        if self.instrument_names_RV is None:
+            self.instrument_names_RV = list(self.my_data.labels)
+        self.my_data_common_t = self.my_data.common_t
+        self.SmartSetter = SmartSetter(self.my_data)
+
+    # ---------------------------------------------------------------- engine
+    def set_engine(self, eng):
+        """emp.py:2315-2388; 'reddemcee' selects the GPU PT engine."""
+        if eng != 'reddemcee':
+            raise ValueError(f'engine {eng!r}: only reddemcee is on the GPU path')
+        from . import engine as _engine
+        self.engine__ = _engine
+        self.engine__.__name__ = 'reddemcee'
+        self.engine_config = {'setup': np.array([5, 100, 500, 2]), 'ntemps': 5, 'betas': None,
+                              'moves': None, 'tsw_history': True, 'smd_history': True,
+                              'adapt_tau': 1000, 'adapt_nu': 1, 'adapt_mode': 0,
+                              'progress': True, 'precision': 'mixed', 'seed': None,
+                              'use_graph': True}
+        self.run_config = {'burnin': None, 'adaptation_batches': None, 'adaptation_nsweeps': None,
+                           'thin': 1, 'discard': 0.5, 'logger_level': 'CRITICAL'}
+
+    # ---------------------------------------------------------------- blocks
+    def add_keplerian(self):
+        """emp.py:1212-1236; Keplerian blocks go in front of the data blocks."""
+        self.kplanets__ += 1
+        kb = KeplerianBlock(self.keplerian_parameterisation, self.kplanets__)
+        self.SmartSetter(kb, ecc_limits=self.eccentricity_limits, ecc_prargs=self.eccentricity_prargs)
+        self.blocks__.insert(self.kplanets__ - 1, kb)
+
+    def add_offset(self):
+        b = OffsetBlock(self.nins__)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def add_jitter(self):
+        b = JitterBlock(self.nins__)
+        self.SmartSetter(b, jit_prargs=self.jitter_prargs)
+        self.blocks__.append(b)
+
+    def add_moav(self):
+        b = MOAVBlock(self.nins__, self.moav)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def add_acceleration(self):
+        b = AccelerationBlock(self.acceleration)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def _autorun_add_RV_ins(self):
+        """emp.py:2628-2650 (the blocks of this path, in the same order)."""
+        if self.acceleration:
+            self.add_acceleration()
+        self.add_offset()
+        if self.switch_jitter:
+            self.add_jitter()
+        if self.moav['order']:
+            self.add_moav()
+
+    # ------------------------------------------------------------ conditions
+    def add_condition(self, cond):
+        self.conds.append(cond)
+
+    def apply_conditions(self):
+        """emp.py:2790-2806: set attribute c[1] of parameter named c[0]."""
+        applied = []
+        for b in self.blocks__:
+            for p in itertools.chain(b, getattr(b, 'additional_parameters', [])):
+                for c in self.conds:
+                    if p.name == c[0]:
+                        setattr(p, c[1], c[2])
+                        if c not in applied:
+                            applied.append(c)
+        for ap in applied:
+            if ap in self.conds:
+                self.conds.remove(ap)
+
+    def update_model(self):
+        self.model = ReddModel(self.blocks__, self.my_data,
+                               moav_reference_quirk=self.moav_reference_quirk)
+
+    # ------------------------------------------------------------ init walkers
+    def set_init(self, rng=np.random):
+        """emp.py:617-648: stratified uniform draws in init_pos or limits."""
+        ntemps, nwalkers = int(self.engine_config['setup'][0]), int(self.engine_config['setup'][1])
+        free = self.model.free_parameters()
+        pos = np.zeros((ntemps, nwalkers, len(free)))
+        for t in range(ntemps):
+            for j, p in enumerate(free):
+                r = 0.707 if p.is_hou else 1
+                b = p.limits[0] if p.init_pos[0] is None else np.round(p.init_pos[0], 8)
+                a = p.limits[1] if p.init_pos[1] is None else np.round(p.init_pos[1], 8)
+                m = (a + b) / 2
+                r = (a - b) / 2 * r
+                dist = np.sort(rng.uniform(0, 1, nwalkers))
+                pos[t][:, j] = r * (2 * dist - 1) + m
+                rng.shuffle(pos[t, :, j])
+        return pos
+
+    def test_init(self, ctx, max_repeats=100):
+        """emp.py:651-681: redraw walkers whose prior is -inf (prior on the GPU)."""
+        import torch
+        p0 = self.set_init()
+        T, W, D = p0.shape
+        for _ in range(max_repeats):
+            th = torch.from_numpy(p0.reshape(-1, D)).to(ctx.device)
+            _, lp = ctx.logpost(th, precision=0)
+            bad = ~np.isfinite(lp.cpu().numpy()).reshape(T, W)
+            if not bad.any():
+                return p0
+            fresh = self.set_init()
+            p0[bad] = fresh[bad]
+        print('COULDNT FIND VALID INITIAL POSITION')
+        return p0
+
+    # ------------------------------------------------------------------- run
+    def _discard(self):
+        ntemps, nwalkers, nsweeps, nsteps = map(int, self.engine_config['setup'])
+        niter = int(nsteps * nsweeps)
+        bi = self.run_config['burnin']
+        if isinstance(bi, float):
+            return int(bi * niter)
+        if isinstance(bi, int):
+            return bi
+        return 0
+
+    def run(self):
+        """emp.py:2463-2478: prepare, run the engine, keep the sampler."""
+        t0 = time.time()
+        self.apply_conditions()
+        self.update_model()
+        ntemps, nwalkers, nsweeps, nsteps = map(int, self.engine_config['setup'])
+        ec = self.engine_config
+        betas = ec['betas']
+        if betas is not None and len(betas) != ntemps:
+            raise ValueError(f'betas should have {ntemps} items')
+        self.sampler = self.engine__.PTSampler(
+            nwalkers, self.model.ndim__, self.model, ntemps=ntemps, betas=betas,
+            tsw_history=ec['tsw_history'], smd_history=ec['smd_history'],
+            adapt_tau=ec['adapt_tau'], adapt_nu=ec['adapt_nu'], adapt_mode=ec['adapt_mode'],
+            precision=ec.get('precision', 'mixed'), seed=ec.get('seed'),
+            use_graph=ec.get('use_graph', True))
+        lim = self.model.limits_free()
+        self.sampler.D_ = np.diff(lim).flatten()          # emp.py:595-602
+        p1 = self.test_init(self.sampler.ctx)
+        self.reddemcee_discard = self._discard()
+        self.reddemcee_thin = int(self.run_config['thin'])
+        ab, an = self.run_config['adaptation_batches'], self.run_config['adaptation_nsweeps']
+        if ab and an:
+            # endit_freeze1.scr: adaptation burn-in, freeze, production
+            n1 = self.reddemcee_discard
+            state = self.sampler.run_mcmc(p1, nsweeps=n1, nsteps=nsteps)
+            self.sampler.select_adjustment('00')
+            self.sampler.run_mcmc(state, nsweeps=nsweeps - n1, nsteps=nsteps)
+        else:
+            self.sampler.run_mcmc(p1, nsweeps=nsweeps, nsteps=nsteps)
+        self.time_run = time.time() - t0
+
+    def postprocess(self):
+        """The statistics of emp.py:1324-1210 that need only the samples."""
+        d = dict(discard=self.reddemcee_discard, thin=self.reddemcee_thin, flat=True)
+        self.chain = self.sampler.get_chain(**d)
+        self.likes = self.sampler.get_log_like(**d)
+        self.posts = self.sampler.get_log_prob(**d)
+        self.best_loc_post = int(np.argmax(self.posts[0]))
+        self.best_loc_like = int(np.argmax(self.likes[0]))
+        self.fit_max = self.chain[0][self.best_loc_post]
+        self.fit_like = self.chain[0][self.best_loc_like]
+        self.fit_median = np.median(self.chain[0], axis=0)
+        self.post_max = float(self.posts[0][self.best_loc_post])
+        self.like_max = float(self.likes[0][self.best_loc_like])
+        try:
+            self.evidence = self.sampler.get_evidence_ti(discard=self.reddemcee_discard)
+        except Exception:
+            self.evidence = (-np.inf, np.inf)
+        resid, err2 = self.residuals(self.fit_max)
+        st = model_stats(resid, err2, self.model.ndim__, self.like_max,
+                         flags=self.my_data.Flag, nins=self.nins__)
+        for k, v in st.items():
+            setattr(self, k, v)
+        self.history.append({'k': self.kplanets__, 'like_max': self.like_max,
+                             'post_max': self.post_max, 'BIC': self.BIC, 'fit': self.fit_max})
+
+    def residuals(self, theta):
+        """(Y - model, err2) at theta, from the device my_model (for stats)."""
+        import torch
+        ctx = self.sampler.ctx
+        th = torch.as_tensor(np.atleast_2d(theta), dtype=torch.float64, device=ctx.device)
+        model0, err2 = ctx.model_eval(th)
+        return self.my_data.RV - model0[0].cpu().numpy(), err2[0].cpu().numpy()
+
+    def autorun(self, k_start=0, k_end=10):
+        """emp.py:2414-2456 with the BIC comparison (emp.py:1145-1156)."""
+        assert k_start <= k_end, f'Invalid keplerian starting point: ({k_start}, {k_end})'
+        self.k_start, self.k_end = k_start, k_end
+        old_bic = np.inf
+        while self.k_start <= self.k_end:
+            if self.switch_first_run:
+                self._autorun_add_RV_ins()
+                for _ in range(self.k_start):
+                    self.add_keplerian()
+                self.switch_first_run = False
+            self.run()
+            self.postprocess()
+            self.k_start += 1
+            if not (old_bic - self.BIC > self._crit_tolerance):
+                break
+            old_bic = self.BIC
+            if self.k_start <= self.k_end:
+                self.add_keplerian()

@@ -1,0 +1,111 @@
+"""Post-run reductions the reference asks of its sampler (host, numpy).
+
+* ``integrated_time`` -- emcee's integrated autocorrelation time estimator
+  (Sokal's automated windowing with constant ``c``), which EMPEROR reads
+  through ``sampler.get_autocorr_time`` (``src/astroemperor/emp.py:1372-1385``).
+* ``thermodynamic_integration`` -- log-evidence by integrating the mean
+  log-likelihood over the inverse-temperature ladder, which EMPEROR reads
+  through ``sampler.get_evidence_ti`` (``emp.py:1432-1447``).
+* ``model_stats`` -- chi2, AIC, BIC, HQIC, RMSE of a fit (``emp.py:1187-1210``).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _next_pow_two(n):
+    i = 1
+    while i < n:
+        i <<= 1
+    return i
+
+
+def autocorr_1d(x):
+    x = np.atleast_1d(x).astype(np.float64)
+    n = _next_pow_two(len(x))
+    f = np.fft.fft(x - np.mean(x), n=2 * n)
+    acf = np.fft.ifft(f * np.conjugate(f))[: len(x)].real
+    if acf[0] == 0:
+        return np.ones_like(acf)
+    return acf / acf[0]
+
+
+def _auto_window(taus, c):
+    m = np.arange(len(taus)) < c * taus
+    if np.any(m):
+        return int(np.argmin(m))
+    return len(taus) - 1
+
+
+def integrated_time(x, c=5, tol=50, quiet=False):
+    """tau per parameter of a chain x [steps, walkers, ndim]."""
+    x = np.asarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x[:, None, None]
+    if x.ndim == 2:
+        x = x[:, :, None]
+    n_t, n_w, n_d = x.shape
+    tau = np.empty(n_d)
+    for d in range(n_d):
+        f = np.zeros(n_t)
+        for k in range(n_w):
+            f += autocorr_1d(x[:, k, d])
+        f /= n_w
+        taus = 2.0 * np.cumsum(f) - 1.0
+        tau[d] = taus[_auto_window(taus, c)]
+    if tol > 0 and np.any(tol * tau > n_t):
+        msg = (f'the chain is shorter than {tol} times the integrated autocorrelation '
+               f'time; N/{tol} = {n_t / tol:.0f}, tau = {tau}')
+        if not quiet:
+            raise RuntimeError(msg)
+    return tau
+
+
+def thermodynamic_integration(betas, log_like, pchip=True):
+    """(logZ, error) from <log L> per temperature.
+
+    ``log_like`` is [ntemps, steps, walkers] (or [ntemps, n]).  The ladder
+    is completed with beta = 0 (taking the hottest chain's mean) when it
+    does not reach it; the error is the difference between the full-ladder
+    and the every-other-rung estimates.
+    """
+    betas = np.asarray(betas, dtype=np.float64)
+    ll = np.asarray(log_like, dtype=np.float64).reshape(len(betas), -1)
+    mean = np.array([np.mean(r[np.isfinite(r)]) if np.any(np.isfinite(r)) else -np.inf for r in ll])
+    order = np.argsort(betas)
+    b, m = betas[order], mean[order]
+    if b[0] > 0:
+        b = np.concatenate([[0.0], b])
+        m = np.concatenate([[m[0]], m])
+
+    def integ(bb, mm):
+        if pchip and len(bb) > 2:
+            try:
+                from scipy.interpolate import PchipInterpolator
+                return float(PchipInterpolator(bb, mm).integrate(bb[0], bb[-1]))
+            except Exception:
+                pass
+        return float(np.trapezoid(mm, bb))
+
+    z = integ(b, m)
+    if len(b) > 3:
+        z2 = integ(b[::2] if b[-1] == b[::2][-1] else np.append(b[::2], b[-1]),
+                   m[::2] if b[-1] == b[::2][-1] else np.append(m[::2], m[-1]))
+        err = abs(z - z2)
+    else:
+        err = np.inf
+    return z, err
+
+
+def model_stats(residuals, err2, ndim, like_max, flags=None, nins=1):
+    n = len(residuals)
+    out = {}
+    out['chi2'] = float(np.sum(residuals ** 2 / err2))
+    out['chi2_red'] = out['chi2'] / (n - ndim)
+    out['RMSE'] = float(np.sqrt(np.sum(residuals ** 2) / n))
+    if flags is not None:
+        out['RMSi'] = [float(np.sqrt(np.mean(residuals[flags == i + 1] ** 2))) for i in range(nins)]
+    out['AIC'] = 2 * ndim - 2 * like_max
+    out['BIC'] = np.log(n) * ndim - 2 * like_max
+    out['HQIC'] = 2 * ndim * np.log(np.log(n)) - 2 * like_max
+    return out

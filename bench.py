@@ -1,0 +1,324 @@
+"""Benchmark of the EMPEROR sampling hot path on GB300.
+
+Workload (default): the 3-Keplerian, 2-instrument, N=1024, per-instrument
+MA(1) system of the benchmark suite, parallel tempering with 10
+temperatures x 256 walkers, stretch moves + swaps + ladder adaptation,
+seeded synthetic data with that configuration's shapes and distributions.
+
+A step is one PT sweep (nsteps=1: one stretch move of all T x W walkers,
+then swaps and adaptation) on data resident in HBM.  The metric is
+log-posterior evaluations x epochs per second of the whole job; the same
+run reports PT sweeps/s, the FP64-plain form of the same sweep, the
+roofline of the dominant kernel, an end-to-end number through the public
+API with host buffers, and the reference-faithful CPU path on the host
+cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = 'Kepler logL evals*epochs/s & PT steps/s: mixed vs FP64 plain @ |dlogL|<=1e-6'
+CONFIG = 'c2'
+SEED = 1234
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=2000)
+    p.add_argument('--warmup', type=int, default=10)
+    p.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    p.add_argument('--fp64-steps', type=int, default=None)
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--cpu-seconds', type=float, default=15.0)
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+def workload_config(setup, n, ndim, kp, nins, q):
+    return {'workload': 'RV PT sweep: 3 Keplerians, 2 instruments, N=1024, per-instrument MA(1)',
+            'ntemps': setup[0], 'nwalkers': setup[1], 'nsteps_per_sweep': setup[3],
+            'epochs': n, 'ndim': ndim, 'planets': kp, 'instruments': nins, 'ma_order': q,
+            'parameterisation': 1, 'seed': SEED, 'precision': 'mixed',
+            'l2': 'flushed between timed steps (256 MiB write, outside the timed events)'}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', f'--id={self.index}', f'--query-gpu={self.Q}',
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for l in self.lines:
+            f = [x.strip() for x in l.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ('active', '1', 'yes'):
+                    reasons.add(nm)
+        return {'sm_mhz': float(np.median(sm)) if sm else None, 'sm_max_mhz': smax,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def cpu_baseline(model, data, truth, seconds, ncores=None):
+    from oracle import cpu_baseline as cb
+    lim = model.limits_free()
+    rng = np.random.default_rng(7)
+    th = truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(64, len(truth)))
+    ncores = ncores or os.cpu_count() or 1
+    eps, n, el, nc = cb.time_pool(model.spec(), data.as_dict(), th, ncores=ncores,
+                                  min_seconds=seconds, max_seconds=2 * seconds)
+    return eps * data.ndata, n, el, nc
+
+
+def run_reference(args):
+    """The reference's own CPU path (its algorithm restated in the oracle,
+    since the reference cannot run here), with every host core."""
+    from astroemperor_gb300 import synth
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    model, data, setup, truth = synth.build_model(CONFIG, seed=SEED)
+    per_step = max(2.0, min(20.0, 120.0 / max(args.steps + args.warmup, 1)))
+    vals = []
+    nc = os.cpu_count() or 1
+    for i in range(args.warmup + args.steps):
+        v, n, el, nc = cpu_baseline(model, data, truth, per_step / 2, nc)
+        if i >= args.warmup:
+            vals.append(v)
+        if sum(1 for _ in vals) >= args.steps:
+            break
+    v = float(np.mean(vals)) if vals else float('nan')
+    line = {'metric': METRIC, 'impl': 'reference', 'value': v, 'unit': 'evals*epochs/s',
+            'n_gpus': 0, 'steps': args.steps, 'warmup': args.warmup,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic', 'config': workload_config(setup, data.ndata, model.ndim__, 3, 2, 1),
+            'cpu_baseline': {'value': v, 'unit': 'evals*epochs/s', 'cores': nc, 'kind': 'port',
+                             'sample': f'reference-faithful my_prior+my_likelihood per walker over '
+                                       f'multiprocessing.Pool({nc}), ~{per_step:.0f} s per step'},
+            'e2e': {'value': v, 'unit': 'evals*epochs/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+
+    import torch
+    from astroemperor_gb300 import _native as N
+    from astroemperor_gb300 import synth
+    from astroemperor_gb300.engine import Context, PTSampler
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.device('cuda', local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+
+    # the CPU baseline pool is spawned (safe after CUDA init); run it first
+    # so that the GPU timing is not disturbed by busy host cores
+    model, data, setup, truth = synth.build_model(CONFIG, seed=SEED + rank)
+    T, W, S, nsteps = setup
+    n, D = data.ndata, model.ndim__
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, ne, el, nc = cpu_baseline(model, data, truth, args.cpu_seconds)
+        cpu = {'value': v, 'unit': 'evals*epochs/s', 'cores': nc, 'kind': 'port',
+               'sample': f'{ne} reference-faithful evaluations (my_prior+my_likelihood per walker, '
+                         f'numpy over epochs, Pool({nc})) in {el:.1f} s'}
+
+    lib = N.load()
+    ctx = Context(model, str(dev))
+    lim = model.limits_free()
+    rng = np.random.default_rng(SEED + rank)
+    p0 = truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, D))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed_sweeps(precision, steps, warmup):
+        s = PTSampler(W, D, model, ntemps=T, precision=precision, seed=SEED + rank, context=ctx)
+        s.run_mcmc(p0, nsweeps=max(warmup, 1))          # warms up
+        s._grow(steps + 2)
+        st = s._state_struct(nsteps)
+        rec = s._record_struct()
+        import ctypes as C
+        # capture the graph for these exact buffers outside the timed region
+        N.call('emp_pt_run', ctx.h, C.byref(st), C.byref(rec), 1, 1, s.stream.cuda_stream)
+        s.stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        stream = s.stream
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.emp_launch_count()
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+            N.call('emp_pt_run', ctx.h, C.byref(st), C.byref(rec), 1, 1, stream.cuda_stream)
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        launches = lib.emp_launch_count() - l0
+        ms = sum(a.elapsed_time(b) for a, b in evs)
+        return ms, launches, s
+
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    ms_mixed, launches, s_mixed = timed_sweeps('mixed', args.steps, args.warmup)
+    clk = clocks.stop()
+    fp64_steps = args.fp64_steps or max(20, args.steps // 20)
+    ms_fp64, _, _ = timed_sweeps('fp64', fp64_steps, 3)
+
+    t_mixed = ms_mixed / 1e3
+    if world > 1:
+        tt = torch.tensor([t_mixed], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(tt.item())
+    units_per_sweep = T * W * nsteps * n
+    value = units_per_sweep * args.steps * world / t_mixed
+    sweeps_s = args.steps * world / t_mixed
+    fp64_value = units_per_sweep * fp64_steps / (ms_fp64 / 1e3)
+
+    # ---- roofline of the dominant kernel: one half-step of the stretch move
+    # (T*W/2 walkers x N epochs), timed alone with events on its stream
+    th_half = torch.as_tensor(p0.reshape(-1, D)[: T * W // 2], dtype=torch.float64, device=dev)
+    ll = torch.empty(th_half.shape[0], dtype=torch.float64, device=dev)
+    lp = torch.empty_like(ll)
+    rs = torch.cuda.Stream(device=dev)
+    reps = 50
+    for prec in (N.EMP_PREC_MIXED,):
+        for _ in range(5):
+            N.call('emp_logpost', ctx.h, th_half.data_ptr(), th_half.shape[0], None, None,
+                   ll.data_ptr(), lp.data_ptr(), None, prec, rs.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(rs):
+            e0.record(rs)
+        for _ in range(reps):
+            N.call('emp_logpost', ctx.h, th_half.data_ptr(), th_half.shape[0], None, None,
+                   ll.data_ptr(), lp.data_ptr(), None, prec, rs.cuda_stream)
+        with torch.cuda.stream(rs):
+            e1.record(rs)
+        torch.cuda.synchronize()
+        k_ms = e0.elapsed_time(e1) / reps
+    kp, q = model.kplan__, 1
+    F = 58 * kp + 10 + 7 * q                                   # FLOP per eval*epoch
+    flops_launch = F * (T * W // 2) * n
+    import ctypes as C
+    f32, f64p = C.c_double(), C.c_double()
+    N.call('emp_probe_peaks', C.byref(f32), C.byref(f64p), rs.cuda_stream)
+    achieved = flops_launch / (k_ms * 1e-3) / 1e12
+    peak32 = f32.value / 1e12
+    roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s',
+            'frac': achieved / peak32, 'traffic': None,
+            'kernel': 'k_logpost<MIXED,Q=1> (stretch half-step shape)',
+            'kernel_ms': k_ms, 'flop_per_eval_epoch': F,
+            'peak_source': 'measured on this GPU by the library FMA probe (MEASURED_PEAKS.json '
+                           'has no CUDA-core figure); compute-issue bound, not HBM or tensor',
+            'fp64_peak_tflops': f64p.value / 1e12}
+
+    # ---- end to end through the public sampler with host buffers
+    s = s_mixed
+    TWn = T * W
+    h_theta = torch.empty(TWn, D, dtype=torch.float64).pin_memory()
+    h_ll = torch.empty(TWn, dtype=torch.float64).pin_memory()
+    h_lp = torch.empty(TWn, dtype=torch.float64).pin_memory()
+    h_theta.copy_(s.theta.cpu())
+    h_ll.copy_(s.logl.cpu())
+    h_lp.copy_(s.logprior.cpu())
+    e2e_steps = min(args.steps, 500)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        s.sweep_host(h_theta, h_ll, h_lp)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    bytes_io = TWn * (D + 2) * 8
+    e2e = {'value': units_per_sweep * e2e_steps / e2e_t, 'unit': 'evals*epochs/s',
+           'h2d_bytes_per_step': bytes_io, 'd2h_bytes_per_step': bytes_io,
+           'api': 'PTSampler.sweep_host (pinned host state in, one sweep, state out)'}
+
+    if rank == 0:
+        line = {'metric': METRIC, 'value': value, 'unit': 'evals*epochs/s', 'n_gpus': world,
+                'steps': args.steps, 'warmup': args.warmup,
+                'ms_per_step': ms_mixed / args.steps, 'higher_is_better': True,
+                'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32+f64 (mixed)',
+                'data': 'synthetic (seeded generator with the configuration shapes)',
+                'config': workload_config(setup, n, D, kp, data.nins, q),
+                'pt_sweeps_per_s': sweeps_s,
+                'fp64_plain': {'value': fp64_value, 'unit': 'evals*epochs/s', 'steps': fp64_steps,
+                               'ms_per_step': ms_fp64 / fp64_steps},
+                'mixed_over_fp64': value / world / fp64_value,
+                'roofline': roof, 'cpu_baseline': cpu, 'e2e': e2e,
+                'clocks': clk, 'gpu_launches': int(launches)}
+        if cpu:
+            line['gpu_over_cpu'] = value / cpu['value']
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

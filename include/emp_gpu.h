@@ -1,0 +1,224 @@
+/*
+ * emp_gpu.h -- C ABI of the GB300-native EMPEROR sampling hot path.
+ *
+ * The reference (EMPEROR / astroemperor 0.9.10) has no native FFI: its hot
+ * path is Python text that it generates into a temporary run script and
+ * hands to the third-party reddemcee PTSampler.  The entry points below are
+ * the ones a binding of that path needs; each comment names the reference
+ * interface it replaces (paths relative to the reference project root).
+ *
+ * Conventions
+ *   - every call returns an int status: EMP_OK (0) or a negative EMP_E_* code;
+ *     emp_last_error_string() gives a one-line message for the calling thread;
+ *   - no exception, abort or device trap crosses this boundary; inputs that
+ *     are outside the prior support or non-finite give logprior = -inf and
+ *     are never evaluated further;
+ *   - all array arguments of the hot calls are DEVICE pointers owned by the
+ *     caller; the library allocates device memory only in emp_create (the
+ *     dataset copy) and never inside emp_logpost / emp_pt_* calls;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default);
+ *   - a handle is not thread-safe: use one host thread per handle.
+ */
+#ifndef EMP_GPU_H
+#define EMP_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EMP_ABI_VERSION 1
+
+#define EMP_MAX_PARAMS   160   /* full theta length incl. fixed parameters */
+#define EMP_MAX_PLANETS  16
+#define EMP_MAX_INS      16
+#define EMP_MAX_MA       3     /* moving-average order q */
+
+/* status codes */
+#define EMP_OK             0
+#define EMP_E_INVALID     -1   /* bad argument / descriptor */
+#define EMP_E_CUDA        -2   /* a CUDA runtime call failed */
+#define EMP_E_UNSUPPORTED -3   /* model feature not built for this path */
+#define EMP_E_SIZE        -4   /* a size is beyond a documented limit */
+#define EMP_E_STATE       -5   /* call order / handle state */
+
+/* precision of the log-posterior */
+#define EMP_PREC_FP64   0  /* plain FP64 everywhere */
+#define EMP_PREC_MIXED  1  /* FP32 Kepler solve + RV sum; float-float phase;
+                              compensated FP32 per-lane sums, FP64 across lanes */
+
+/* prior kinds (support/priors/*.prior) */
+#define EMP_PRIOR_UNIFORM   0
+#define EMP_PRIOR_NORMAL    1
+#define EMP_PRIOR_JEFFREYS  2
+#define EMP_PRIOR_BETA      3
+#define EMP_PRIOR_NONE      4
+
+typedef struct emp_prior {
+    int32_t kind;
+    int32_t _pad;
+    double lo, hi;        /* support, inclusive (the reference's `limits`) */
+    double a0, a1, a2;    /* Uniform/Jeffreys: a0 = ln(1/(hi-lo))
+                             Normal: a0 = mu, a1 = s, a2 = ln(s sqrt(2 pi)) + logZ
+                             Beta:   a0 = a, a1 = b, a2 = ln B(a, b) */
+} emp_prior;
+
+/*
+ * Compiled model: replaces the generated my_model / my_prior text
+ * (emp_model.py:706-781, emp.py:182-254) and the theta index maps of
+ * ReddModel.refresh__ (emp_model.py:223-305).
+ */
+typedef struct emp_model_desc {
+    int32_t abi_version;          /* EMP_ABI_VERSION */
+    int32_t n_full;               /* parameters incl. fixed ones */
+    int32_t n_free;               /* ndim of the sampler */
+    int32_t n_planets;
+    int32_t n_ins;
+    int32_t ma_order;             /* q; 0 = no MOAV block */
+    int32_t ma_global;            /* 1: moav01 (global), 0: per instrument */
+    int32_t ma_quirk;             /* 1: reproduce the reference's per-instrument
+                                     no-op (moav00.model:18-19 writes to a copy) */
+    int32_t acc_order;            /* acceleration polynomial order, 0 = none */
+    int32_t offset_slot;          /* first full-theta index, -1 = none */
+    int32_t jitter_slot;
+    int32_t ma_slot;
+    int32_t acc_slot;
+    int32_t _pad0;
+    int32_t kep_param[EMP_MAX_PLANETS];   /* parameterisation 0,1,2,3,4,6,7 */
+    int32_t kep_slot[EMP_MAX_PLANETS];    /* first full-theta index of planet */
+    int32_t full_src[EMP_MAX_PARAMS];     /* free index feeding slot, -1 = fixed */
+    double  full_fixed[EMP_MAX_PARAMS];   /* value of fixed slots */
+    /* prior of each free parameter, in the order my_prior sums them
+       (block by block, emp.py:196-203); prior_block[i] = block number */
+    emp_prior prior[EMP_MAX_PARAMS];
+    int32_t prior_slot[EMP_MAX_PARAMS];   /* full-theta index of free param i */
+    /* derived priors of Keplerian blocks, emp.py:205-226:
+       [p][0]: Ecc (x = th[3]^2 + th[4]^2), [p][1]: Amp (x = th[1]^2 + th[2]^2) */
+    emp_prior derived[EMP_MAX_PLANETS][2];
+    double  loglike_const;        /* -0.5 ln(2 pi) ndat  (00.like:1) */
+} emp_model_desc;
+
+/*
+ * One or more RV systems, ragged.  System s owns epochs
+ * [offsets[s], offsets[s+1]).  Times must be sorted within each system and
+ * already referenced to the system's first epoch (qol_utils.py:192-198).
+ * inst holds 1-based instrument flags (the reference's `Flag` column).
+ */
+typedef struct emp_dataset_desc {
+    int32_t n_systems;
+    int32_t _pad;
+    const int64_t* offsets;   /* host, n_systems+1 */
+    const double* t;          /* host, days */
+    const double* y;          /* host, m/s */
+    const double* yerr;       /* host, m/s (sigma, not sigma^2) */
+    const int32_t* inst;      /* host, 1..n_ins */
+} emp_dataset_desc;
+
+typedef struct emp_handle emp_handle;
+
+/* Replaces: the generated temp script's data prologue + my_model/my_prior
+   definitions (emp.py:137-175 write_script, emp_model.py:406-433).
+   Copies the dataset to the device in the kernel layout. */
+int emp_create(const emp_model_desc* model, const emp_dataset_desc* data,
+               emp_handle** out);
+int emp_destroy(emp_handle* h);
+
+/* Replaces: my_likelihood(theta) (support/likelihoods/00.like:3-5) and
+   my_prior(theta) (emp.py:190-251) evaluated for a batch of B walkers.
+   theta [B][n_free] f64.  logl/logprior [B] f64 (device).
+   If beta != NULL and logp != NULL, logp[b] = beta[b]*logl[b] + logprior[b]
+   (logl is left at -inf when the prior is -inf).
+   For ragged datasets, system_of (device int32 [B], may be NULL for one
+   system) names the system of each walker. */
+int emp_logpost(emp_handle* h, const double* theta, int B,
+                const int32_t* system_of, const double* beta,
+                double* logl, double* logprior, double* logp,
+                int precision, void* stream);
+
+/* Replaces: my_model(theta) -> (model0, err20) (emp_model.py:706-781) for a
+   batch of B walkers; model/err2 are device [B][n] in the dataset's input
+   (time) order, model including the moving-average terms.  FP64.  Meant
+   for fits and reporting (B small); the sampler never calls it. */
+int emp_model_eval(emp_handle* h, const double* theta, int B, double* model,
+                   double* err2, void* stream);
+
+/* Parallel-tempering state, all device pointers owned by the caller.
+   Walker slots are physical; `members[t*W + j]` names the slot that holds
+   logical walker j of temperature t (swaps exchange slots, not positions).
+   Replaces the walker state reddemcee keeps inside PTSampler
+   (emp.py:576-593; reddemcee 0.8.5 / emcee 3.1.6). */
+typedef struct emp_pt_state {
+    int32_t ntemps, nwalkers, ndim;
+    int32_t nsteps;               /* stretch steps per sweep */
+    double* theta;                /* [T*W][ndim] by slot */
+    double* logl;                 /* [T*W] by slot */
+    double* logprior;             /* [T*W] by slot */
+    int32_t* members;             /* [T][W] slot of (t, j) */
+    double* betas;                /* [T] */
+    int64_t* counters;            /* [4]: 0 = steps done, 1 = sweeps done */
+    int32_t* accepted;            /* [T][W] cumulative stretch accepts */
+    int32_t* swaps_accepted;      /* [T] cumulative swap accepts, pair (t-1,t) at t */
+    int32_t* perm_units;          /* units modulo W (affine permutations) */
+    int32_t n_perm_units;
+    int32_t adapt;                /* 1: adapt the ladder after each sweep */
+    uint64_t seed;
+    double a;                     /* stretch scale, emcee default 2 */
+    double adapt_tau;             /* engine_config['adapt_tau'] */
+    double adapt_nu;              /* engine_config['adapt_nu'] */
+    int32_t adapt_mode;           /* engine_config['adapt_mode'] (0 supported) */
+    int32_t precision;            /* EMP_PREC_* used for every evaluation */
+} emp_pt_state;
+
+/* Per-sweep history buffers (device, caller-owned; any may be NULL).
+   Replaces the PTHDFBackend datasets written at emp.py:722-770. */
+typedef struct emp_pt_record {
+    int64_t capacity;             /* rows available */
+    int32_t thin;                 /* record every `thin` steps */
+    int32_t _pad;
+    double* chain;                /* [capacity][T][W][ndim] */
+    double* log_like;             /* [capacity][T][W] */
+    double* log_prob;             /* [capacity][T][W] */
+    double* beta_history;         /* [capacity_sweeps][T] */
+    double* tsw_history;          /* [capacity_sweeps][T-1] */
+    double* smd_history;          /* [capacity_sweeps][T-1] */
+    int64_t* n_recorded;          /* [2]: rows in chain, rows in sweep hists */
+} emp_pt_record;
+
+/* Replaces: one PT sweep of reddemcee.PTSampler.run_mcmc
+   (support/endit_reddemcee.scr:3): nsteps stretch moves of every
+   temperature, adjacent swaps from the hottest pair down, ladder adaptation,
+   history recording. Launches only; no host synchronisation. */
+int emp_pt_sweep(emp_handle* h, const emp_pt_state* st,
+                 const emp_pt_record* rec, void* stream);
+
+/* nsweeps sweeps; with use_graph != 0 one sweep is captured once into a
+   CUDA graph (cached in the handle for this state) and replayed. */
+int emp_pt_run(emp_handle* h, const emp_pt_state* st,
+               const emp_pt_record* rec, int nsweeps, int use_graph,
+               void* stream);
+
+/* (Re)compute logl/logprior of every slot of `st` (initial state). */
+int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream);
+
+/* Lanes per walker (4, 8, 16, 32) and epoch tile used by emp_logpost /
+   emp_pt_*; 0 = library default.  Set by the autotuner. */
+int emp_set_launch(emp_handle* h, int precision, int lanes_per_walker,
+                   int tile_epochs);
+int emp_get_launch(emp_handle* h, int precision, int* lanes_per_walker,
+                   int* tile_epochs);
+
+/* Measured CUDA-core throughput (FMA chains) for the roofline:
+   fp32/fp64 FLOP/s of this device.  Launches a short probe kernel. */
+int emp_probe_peaks(double* fp32_flops, double* fp64_flops, void* stream);
+
+/* Number of this library's kernel launches issued so far (all handles). */
+int64_t emp_launch_count(void);
+
+const char* emp_last_error_string(void);
+int emp_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EMP_GPU_H */

@@ -1,0 +1,119 @@
+"""Model cases shared by the golden-fixture generator and the tests.
+
+Each case builds a model with the package's model layer (the same blocks,
+default priors and conditions a Simulation would build) and a fixed,
+seeded set of theta: points near the fit, draws inside the limits (some of
+which fall outside the derived eccentricity support) and out-of-bounds
+points.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from astroemperor_gb300.data import preprocess_instruments
+from astroemperor_gb300.model import (AccelerationBlock, JitterBlock, KeplerianBlock, MOAVBlock,
+                                      OffsetBlock, ReddModel, SmartSetter)
+from astroemperor_gb300 import synth
+
+# the 51 Peg fit recorded by the reference (tests/01_51peg_basic.ipynb:548-562)
+PEG_MAP_P1 = [4.231, 55.957, 1.769, 0.087, 0.061, 3.642, 2.961]
+
+
+def peg_data(arr):
+    return preprocess_instruments([arr], ['51peg.vels'])
+
+
+def _kep(ss, par, number, **lims):
+    kb = KeplerianBlock(par, number)
+    ss(kb)
+    for i, lim in lims.items():
+        kb[int(i[1:])].limits = list(lim)
+    return kb
+
+
+def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=None, quirk=False):
+    data = peg_data(arr)
+    ss = SmartSetter(data)
+    blocks = []
+    if k >= 1:
+        if par in (0, 1, 3, 4):
+            kb = _kep(ss, par, 1)
+            if conditions:
+                kb[0].limits = [3, 5]
+                kb[1].limits = [45, 60]
+        else:
+            kb = _kep(ss, par, 1)
+            if conditions:
+                kb[0].limits = [np.log(3), np.log(5)]
+        if par in (3, 4):
+            kb[2].limits = [-5, 5]
+        if fixed_ecc:
+            kb[3].fixed = 0.0
+            kb[4].fixed = 0.0
+        blocks.append(kb)
+    if acc:
+        ab = AccelerationBlock(acc)
+        ss(ab)
+        blocks.append(ab)
+    ob = OffsetBlock(1)
+    ss(ob)
+    if conditions:
+        ob[0].limits = [-10., 10.]
+    blocks.append(ob)
+    jb = JitterBlock(1)
+    ss(jb, jit_prargs=(5, 5))
+    blocks.append(jb)
+    if moav:
+        mb = MOAVBlock(1, moav)
+        ss(mb)
+        blocks.append(mb)
+    return ReddModel(blocks, data, moav_reference_quirk=quirk), data
+
+
+def draw_thetas(model, rng, n_in=24, center=None, spread=0.02, n_near=8, n_out=4):
+    lim = model.limits_free()
+    lo, hi = lim[:, 0], lim[:, 1]
+    out = [rng.uniform(lo, hi) for _ in range(n_in)]
+    if center is not None:
+        c = np.asarray(center, dtype=np.float64)
+        for _ in range(n_near):
+            out.append(c + spread * (hi - lo) * rng.normal(size=len(c)) * 0.1)
+    for _ in range(n_out):
+        x = rng.uniform(lo, hi)
+        i = rng.integers(len(x))
+        x[i] = hi[i] + 1.0 + abs(hi[i])
+        out.append(x)
+    return np.array(out)
+
+
+def kat_cases(arr):
+    """name -> (spec, data dict, thetas [n, ndim])."""
+    return {k: (m.spec(), d.as_dict(), th) for k, (m, d, th) in kat_case_models(arr).items()}
+
+
+def kat_case_models(arr):
+    """name -> (ReddModel, RVData, thetas [n, ndim])."""
+    rng = np.random.default_rng(20240601)
+    cases = {}
+
+    def add(name, model, data, center=None):
+        th = draw_thetas(model, rng, center=center)
+        cases[name] = (model, data, th)
+
+    m, d = model_51peg(arr, k=0)
+    add('51peg_k0', m, d, center=[3.6, 36.0])
+    m, d = model_51peg(arr, k=1, par=1)
+    add('51peg_k1_p1', m, d, center=PEG_MAP_P1)
+    m, d = model_51peg(arr, k=1, par=0)
+    add('51peg_k1_p0', m, d, center=[4.231, 55.957, 1.769, 0.011, 0.964, 3.642, 2.961])
+    for par in (2, 3, 4, 6, 7):
+        m, d = model_51peg(arr, k=1, par=par)
+        add(f'51peg_k1_p{par}', m, d)
+    m, d = model_51peg(arr, k=1, par=1, fixed_ecc=True, acc=2)
+    add('51peg_fixed_acc', m, d)
+    m, d = model_51peg(arr, k=1, par=1, moav={'order': 2, 'global': True})
+    add('51peg_gma2', m, d)
+    for name, quirk in (('c2_ma1', False), ('c2_ma1_quirk', True)):
+        m, d, setup, truth = synth.build_model('c2', seed=7, moav_reference_quirk=quirk)
+        add(name, m, d, center=truth)
+    return cases

@@ -1,0 +1,115 @@
+"""GPU parallel-tempering sampler against the oracle sampler.
+
+* replay: with the same Philox stream the FP64 device sampler and the numpy
+  oracle (``oracle.pt``) walk the same chain (stretch proposals, Metropolis
+  decisions, swaps, ladder adaptation), compared sweep by sweep;
+* the graph-captured and the eagerly launched sweep are bit-identical;
+* posterior: the mixed-precision sampler on 51 Peg recovers the fit the
+  reference recorded (tests/01_51peg_basic.ipynb).
+"""
+import numpy as np
+import pytest
+import torch
+
+from astroemperor_gb300 import _native as N
+from astroemperor_gb300.engine import PTSampler, default_betas
+from oracle.pt import OraclePT
+from oracle.rv import OracleRV
+from tests.golden.cases import model_51peg
+
+pytestmark = pytest.mark.gpu
+
+
+def _p0(model, T, W, seed):
+    rng = np.random.default_rng(seed)
+    lim = model.limits_free()
+    lo, hi = lim[:, 0], lim[:, 1]
+    # inside the eccentricity support for Ecc_sin/Ecc_cos (|S|,|C| <= 0.7)
+    p = rng.uniform(lo, hi, size=(T, W, len(lo)))
+    for j, prm in enumerate(model.free_parameters()):
+        if prm.name.startswith('Ecc_'):
+            p[..., j] *= 0.5
+    return p
+
+
+def _oracle_logpost(o):
+    def f(th):
+        th = np.atleast_2d(th)
+        lp = np.array([o.my_prior(t) for t in th])
+        ll = np.array([o.my_likelihood(t) if np.isfinite(x) else -np.inf for t, x in zip(th, lp)])
+        return ll, lp
+    return f
+
+
+@pytest.mark.parametrize('adapt', [False, True])
+def test_replay_matches_oracle(peg_arr, lib, cuda, adapt):
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    T, W, S = 4, 16, 12
+    betas = np.array([1.0, 0.4, 0.1, 0.01])
+    p0 = _p0(m, T, W, 5)
+    gpu = PTSampler(W, m.ndim__, m, ntemps=T, betas=betas, precision='fp64', seed=4242,
+                    adapt_tau=50, adapt_nu=1, use_graph=False)
+    if not adapt:
+        gpu.select_adjustment('00')
+    gpu.run_mcmc(p0, nsweeps=S)
+    o = OracleRV(m.spec(), d.as_dict())
+    ora = OraclePT(_oracle_logpost(o), T, W, m.ndim__, betas, adapt=adapt, adapt_tau=50,
+                   adapt_nu=1, rng='philox', seed=4242)
+    ora.set_positions(p0)
+    ora.run(S)
+    ch = gpu.get_chain()                        # [T, S, W, D]
+    och = np.moveaxis(np.array(ora.chain), 1, 0)
+    np.testing.assert_allclose(ch, och, rtol=1e-13, atol=1e-13)
+    np.testing.assert_allclose(gpu.get_log_like(), np.moveaxis(np.array(ora.log_like), 1, 0),
+                               rtol=1e-11)
+    np.testing.assert_allclose(gpu.get_betas(), np.array(ora.beta_hist), rtol=1e-14)
+    np.testing.assert_allclose(gpu.get_tsw(), np.array(ora.tsw_hist), rtol=0, atol=0)
+    np.testing.assert_allclose(gpu.get_smd(), np.array(ora.smd_hist), rtol=1e-12)
+    np.testing.assert_allclose(gpu.betas, ora.betas, rtol=1e-14)
+    np.testing.assert_array_equal(gpu.accepted, ora.accepted)
+    assert ora.accepted.sum() > 0 and np.array(ora.tsw_hist).sum() > 0
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_graph_equals_eager(peg_arr, lib, cuda, precision):
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    T, W = 3, 32
+    p0 = _p0(m, T, W, 9)
+    out = []
+    for ug in (False, True):
+        s = PTSampler(W, m.ndim__, m, ntemps=T, betas=[1.0, 0.3, 0.05], precision=precision,
+                      seed=77, use_graph=ug)
+        st = s.run_mcmc(p0, nsweeps=25)
+        st = s.run_mcmc(st, nsweeps=5)          # continue on the device state
+        out.append((s.get_chain(), s.get_log_prob(), s.betas, st.coords))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
+    assert out[0][0].shape == (T, 30, W, m.ndim__)
+
+
+def test_posterior_51peg_recovers_reference_fit(peg_arr, lib, cuda):
+    """Mixed precision, 51 Peg k=1 parameterisation 1 with the reference
+    notebook's conditions; the cold chain must recover the recorded fit."""
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    m.blocks[0][0].init_pos = [4.1, 4.3]
+    m.blocks[0][1].init_pos = [50, 60]
+    T, W = 6, 128
+    rng = np.random.default_rng(1234)
+    lim = m.limits_free()
+    p0 = rng.uniform(lim[:, 0], lim[:, 1], size=(T, W, m.ndim__))
+    p0[..., 0] = rng.uniform(4.22, 4.24, size=(T, W))
+    p0[..., 1] = rng.uniform(50, 60, size=(T, W))
+    p0[..., 3:5] *= 0.3
+    s = PTSampler(W, m.ndim__, m, ntemps=T, precision='mixed', seed=1)
+    s.run_mcmc(p0, nsweeps=3000)
+    ch = s.get_chain(flat=True, discard=1500)[0]
+    ll = s.get_log_like(flat=True, discard=1500)[0]
+    med = np.median(ch, axis=0)
+    assert med[0] == pytest.approx(4.2308, abs=5e-4)
+    assert med[1] == pytest.approx(55.957, abs=0.8)
+    assert med[5] == pytest.approx(3.642, abs=0.6)
+    assert med[6] == pytest.approx(2.961, abs=0.8)
+    assert ll.max() == pytest.approx(-869.46, abs=0.3)
+    assert np.all(np.isfinite(ll))
+    lp = s.get_log_prob(flat=True, discard=1500)[0]
+    assert np.all(lp <= ll + 1e-9)            # logprior <= 0 for these priors
