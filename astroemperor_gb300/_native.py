@@ -53,6 +53,9 @@ class EmpModelDesc(C.Structure):
         ('prior_slot', C.c_int32 * EMP_MAX_PARAMS),
         ('derived', (EmpPrior * 2) * EMP_MAX_PLANETS),
         ('loglike_const', C.c_double),
+        ('prior_const', C.c_double),
+        ('n_prior_var', C.c_int32), ('_pad1', C.c_int32),
+        ('prior_var', C.c_int32 * (EMP_MAX_PARAMS + 2 * EMP_MAX_PLANETS)),
     ]
 
 

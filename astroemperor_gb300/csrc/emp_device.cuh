@@ -131,7 +131,7 @@ struct KArgs {
 struct Smem {
     int tile_bytes;        // staged epochs
     int group_bytes;       // per walker group
-    int off_full, off_thp, off_pc, off_ins, off_acc, off_red, off_scan, off_misc;
+    int off_full, off_thp, off_pc, off_ins, off_acc, off_red, off_scan, off_pterm, off_misc;
     int total;
 
     __host__ __device__ static int align16(int x) { return (x + 15) & ~15; }
@@ -150,68 +150,12 @@ struct Smem {
         off_acc = o;  o += align16(8 * (acc_order > 0 ? acc_order : 1));
         off_red = o;  o += align16(8 * 4 * ((L + 31) / 32));
         off_scan = o; o += align16(rs * 2 * (kMaxQ + kMaxQ * kMaxQ) * L);
+        off_pterm = o; o += align16(8 * (n_free + 2 * n_planets + 1));
         off_misc = o; o += 64;
         group_bytes = align16(o);
         total = tile_bytes + G * group_bytes;
     }
 };
-
-// ----------------------------------------------------------------------------
-// priors (support/priors/*.prior), FP64
-// ----------------------------------------------------------------------------
-__device__ __forceinline__ double prior_term(const emp_prior& p, double x) {
-    if (!(x >= p.lo && x <= p.hi)) return -INFINITY;    // NaN -> -inf
-    switch (p.kind) {
-        case EMP_PRIOR_UNIFORM:
-        case EMP_PRIOR_JEFFREYS:
-            return p.a0;
-        case EMP_PRIOR_NORMAL: {
-            double z = (x - p.a0) / p.a1;
-            return -0.5 * z * z - p.a2;
-        }
-        case EMP_PRIOR_BETA:
-            // ln pdf = (a-1) ln x + (b-1) ln(1-x) - ln B(a,b)
-            return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
-        default:
-            return 0.0;
-    }
-}
-
-// whole my_prior of one full theta (emp.py:190-251): free parameters in
-// block order, each Keplerian block followed by its derived priors.
-static __device__ double log_prior(const emp_model_desc* md, const double* full) {
-    double lp = 0.0;
-    int nf = md->n_free;
-    int np = md->n_planets;
-    int planet = 0;
-    for (int i = 0; i < nf; ++i) {
-        int slot = md->prior_slot[i];
-        // close finished Keplerian blocks
-        while (planet < np && slot >= md->kep_slot[planet] + 5) {
-            for (int k = 0; k < 2; ++k) {
-                const emp_prior& dp = md->derived[planet][k];
-                if (dp.kind == EMP_PRIOR_NONE) continue;
-                const double* th = full + md->kep_slot[planet];
-                double x = k == 0 ? th[3] * th[3] + th[4] * th[4] : th[1] * th[1] + th[2] * th[2];
-                lp += prior_term(dp, x);
-            }
-            ++planet;
-        }
-        emp_prior p = md->prior[i];
-        lp += prior_term(p, full[slot]);
-    }
-    while (planet < np) {
-        for (int k = 0; k < 2; ++k) {
-            const emp_prior& dp = md->derived[planet][k];
-            if (dp.kind == EMP_PRIOR_NONE) continue;
-            const double* th = full + md->kep_slot[planet];
-            double x = k == 0 ? th[3] * th[3] + th[4] * th[4] : th[1] * th[1] + th[2] * th[2];
-            lp += prior_term(dp, x);
-        }
-        ++planet;
-    }
-    return lp;
-}
 
 // ----------------------------------------------------------------------------
 // per-planet elements (FP64): per, K, phase (rad, or NAN with tp), tp, e, w

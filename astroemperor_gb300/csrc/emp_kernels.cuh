@@ -13,18 +13,100 @@
 //   my_likelihood (support/likelihoods/00.like:3-5),
 // and in kModeStretch additionally the emcee stretch proposal and the
 // Metropolis test of one half of a temperature's ensemble.
+//
+// FP64 is a scarce pipe on this GPU (a warp-wide FP64 instruction occupies
+// the sub-partition's FP64 unit for tens of cycles), so the per-walker
+// prologue of the mixed kernel keeps FP64 to the few operations whose
+// rounding must match the reference: the stretch proposal, e = S^2 + C^2,
+// exp of log-periods, the varying prior terms and the final sums.  Bounds
+// of priors are compared exactly on the integer pipe.
 #pragma once
 #include "emp_device.cuh"
 
 namespace emp {
 
-template <int PREC>
-__device__ __forceinline__ void planet_consts(const Elements& el,
-                                              typename P<PREC>::R* pc);
+// ----------------------------------------------------------------------------
+// exact double comparisons on the integer pipe
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ long long dkey(double x) {
+    long long b = __double_as_longlong(x);
+    if (b == (long long)0x8000000000000000ULL) b = 0;          // -0.0 == +0.0
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool d_isnan(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+// lo <= x <= hi as IEEE comparisons (false for NaN)
+__device__ __forceinline__ bool in_support(double x, double lo, double hi) {
+    if (d_isnan(x)) return false;
+    const long long k = dkey(x);
+    return k >= dkey(lo) && k <= dkey(hi);
+}
 
-template <>
-__device__ __forceinline__ void planet_consts<EMP_PREC_FP64>(const Elements& el, double* pc) {
-    double freq = 2. * kPi / el.per;                       // kep01.model:11
+// value of a prior term that varies with x (Normal, Beta); x in support
+__device__ __forceinline__ double prior_var_term(const emp_prior& p, double x) {
+    if (p.kind == EMP_PRIOR_NORMAL) {
+        const double z = (x - p.a0) / p.a1;
+        return -0.5 * z * z - p.a2;
+    }
+    if (p.kind == EMP_PRIOR_BETA) return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
+    return 0.0;
+}
+
+__device__ __forceinline__ double derived_x(const double* th, int k) {
+    return k == 0 ? th[3] * th[3] + th[4] * th[4] : th[1] * th[1] + th[2] * th[2];
+}
+
+// ----------------------------------------------------------------------------
+// float-float helpers (mixed precision phase)
+// ----------------------------------------------------------------------------
+struct FF { float hi, lo; };
+
+__device__ __forceinline__ FF ff_split(double x) {
+    FF r;
+    r.hi = (float)x;
+    r.lo = (float)(x - (double)r.hi);
+    return r;
+}
+// a * b with a, b float-float, |error| ~ 2^-46 |ab|
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    FF r;
+    r.hi = p;
+    r.lo = e + __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi));
+    return r;
+}
+// x - rint(x) of a float-float, normalised to |hi| <= 0.5
+__device__ __forceinline__ FF ff_frac(FF a) {
+    const float n = rintf(a.hi);
+    const float h = __fsub_rn(a.hi, n);               // exact
+    const float s = __fadd_rn(h, a.lo);
+    const float n2 = rintf(s);
+    const float s2 = __fsub_rn(s, n2);
+    FF r;
+    r.hi = s2;
+    r.lo = __fsub_rn(a.lo, __fsub_rn(__fadd_rn(s2, n2), h));   // fast two-sum tail
+    return r;
+}
+// 1/x in float-float (one reciprocal and a residual correction)
+__device__ __forceinline__ FF ff_recip(FF x) {
+    const float r = __frcp_rn(x.hi);
+    float e = __fmaf_rn(-x.hi, r, 1.0f);
+    e = __fmaf_rn(-x.lo, r, e);
+    FF o;
+    o.hi = r;
+    o.lo = __fmul_rn(r, e);
+    return o;
+}
+
+// ----------------------------------------------------------------------------
+// per-planet constants
+// ----------------------------------------------------------------------------
+// FP64: [0]=freq [1]=phase [2]=e [3]=K cw [4]=K sqrt(1-e^2) sw [5]=K e cw [6]=tp [7]=use_tp
+__device__ __forceinline__ void planet_consts_fp64(int par, const double* v, double* pc) {
+    Elements el = planet_elements(par, v);
+    const double freq = 2. * kPi / el.per;                   // kep01.model:11
     pc[0] = freq;
     pc[1] = el.phase;
     pc[2] = el.e;
@@ -35,25 +117,63 @@ __device__ __forceinline__ void planet_consts<EMP_PREC_FP64>(const Elements& el,
     pc[7] = (double)el.use_tp;
 }
 
-template <>
-__device__ __forceinline__ void planet_consts<EMP_PREC_MIXED>(const Elements& el, float* pc) {
-    // cycles = t * (1/P) + ph, reduced to [-0.5, 0.5) in float-float
-    double fc = 1.0 / el.per;
-    double ph = el.use_tp ? -el.tp * fc : el.phase * (1.0 / kTwoPi);
-    ph -= rint(ph);
-    float fh = (float)fc;
-    float phh = (float)ph;
-    pc[0] = fh;
-    pc[1] = (float)(fc - (double)fh);
-    pc[2] = phh;
-    pc[3] = (float)(ph - (double)phh);
-    pc[4] = (float)el.e;
-    pc[5] = (float)(el.K * el.cw);
-    pc[6] = (float)(el.K * sqrt(1.0 - el.e * el.e) * el.sw);
-    pc[7] = (float)(el.K * el.e * el.cw);
+// mixed: [0]=f_hi [1]=f_lo (cycles/day) [2]=ph_hi [3]=ph_lo (cycles)
+//        [4]=e [5]=A=K cw [6]=B=K sqrt(1-e^2) sw [7]=C=K e cw
+__device__ __forceinline__ void planet_consts_mixed(int par, const double* v, float* pc) {
+    double per;
+    float K, e, cw, sw;
+    bool use_tp = false;
+    double phase = 0.0, tp = 0.0;
+    if (par == 0 || par == 3 || par == 6) {
+        per = par == 6 ? exp(v[0]) : v[0];
+        K = (float)v[1];
+        e = (float)v[3];
+        sincosf((float)v[4], &sw, &cw);
+        if (par == 3) { use_tp = true; tp = v[2]; } else { phase = v[2]; }
+    } else if (par == 2) {
+        per = exp(v[0]);
+        const float As = (float)v[1], Ac = (float)v[2];
+        K = As * As + Ac * Ac;
+        float ph = acosf(Ac * rsqrtf(K));
+        if (As < 0.f) ph = 6.28318530717958647692f - ph;
+        phase = (double)ph;
+    } else {
+        per = par == 7 ? exp(v[0]) : v[0];
+        K = (float)v[1];
+        if (par == 4) { use_tp = true; tp = v[2]; } else { phase = v[2]; }
+    }
+    if (par == 1 || par == 2 || par == 4 || par == 7) {
+        const double ed = v[3] * v[3] + v[4] * v[4];        // FP64 as the reference
+        const double thr = (par == 2 || par == 4) ? 1e-5 : 1e-6;
+        e = (float)ed;
+        if (ed < thr) { cw = 1.f; sw = 0.f; }
+        else {
+            const float rs = rsqrtf(e);
+            cw = (float)v[4] * rs;
+            sw = (float)v[3] * rs;
+        }
+    }
+    const FF f = ff_recip(ff_split(per));
+    FF ph;
+    if (use_tp) {
+        FF p = ff_mul(ff_split(tp), f);
+        p.hi = -p.hi; p.lo = -p.lo;
+        ph = ff_frac(p);
+    } else {
+        const FF inv2pi = {0.15915493667125702f, 6.4206382432985265e-09f};   // 1/(2 pi) as float-float
+        ph = ff_frac(ff_mul(ff_split(phase), inv2pi));
+    }
+    pc[0] = f.hi;
+    pc[1] = f.lo;
+    pc[2] = ph.hi;
+    pc[3] = ph.lo;
+    pc[4] = e;
+    pc[5] = K * cw;
+    pc[6] = K * sqrtf((1.f - e) * (1.f + e)) * sw;
+    pc[7] = K * e * cw;
 }
 
-// one Keplerian term at one epoch
+// one Keplerian term at one epoch (FP64)
 __device__ __forceinline__ double rv_term_f64(const double* pc, double t) {
     double M;
     if (pc[7] != 0.0) M = __dmul_rn(pc[0], __dsub_rn(t, pc[6]));   // kep03/04: freq*(X_-tp)
@@ -62,36 +182,85 @@ __device__ __forceinline__ double rv_term_f64(const double* pc, double t) {
     double Mr = fmod(M + kPi, kTwoPi);
     if (Mr < 0.0) Mr += kTwoPi;
     Mr -= kPi;
-    double e = pc[2];
+    const double e = pc[2];
     double s, c;
     kepler_f64(Mr, e, s, c);
     // K (cos(f + w) + e cos w) with cos f = (cos E - e)/(1 - e cos E),
     // sin f = sqrt(1-e^2) sin E / (1 - e cos E)
-    double inv = 1.0 / (1.0 - e * c);
+    const double inv = 1.0 / (1.0 - e * c);
     return (pc[3] * (c - e) - pc[4] * s) * inv + pc[5];
 }
 
-__device__ __forceinline__ float rv_term_mixed(const float* pc, float th, float tl) {
-    // float-float phase: u = th*fh exactly split, plus cross terms and phase
-    // (explicit _rn intrinsics: the error-free transforms must not be
-    // contracted into FMAs by the compiler)
-    float fh = pc[0], fl = pc[1];
-    float p = __fmul_rn(th, fh);
-    float pe = __fmaf_rn(th, fh, -p);                 // exact low part of th*fh
-    float x = __fadd_rn(p, pc[2]);                    // TwoSum(p, ph_hi)
-    float bv = __fsub_rn(x, p);
-    float xe = __fadd_rn(__fsub_rn(p, __fsub_rn(x, bv)), __fsub_rn(pc[2], bv));
-    float nint = rintf(x);
-    float fr = __fsub_rn(x, nint);                    // exact
-    float lo = pe + xe + pc[3] + __fmaf_rn(th, fl, tl * fh);
+// mean anomaly in [-pi, pi] from float-float time and planet constants
+__device__ __forceinline__ float mean_anomaly_mixed(const float* pc, float th, float tl) {
+    // cycles = (th + tl) * (fh + fl) + (ph_hi + ph_lo), reduced mod 1; the
+    // error-free transforms use _rn intrinsics so they are not contracted
+    const float fh = pc[0], fl = pc[1];
+    const float p = __fmul_rn(th, fh);
+    const float pe = __fmaf_rn(th, fh, -p);
+    const float x = __fadd_rn(p, pc[2]);                 // TwoSum(p, ph_hi)
+    const float bv = __fsub_rn(x, p);
+    const float xe = __fadd_rn(__fsub_rn(p, __fsub_rn(x, bv)), __fsub_rn(pc[2], bv));
+    const float fr = __fsub_rn(x, rintf(x));             // exact
+    const float lo = pe + xe + pc[3] + __fmaf_rn(th, fl, tl * fh);
     float cyc = __fadd_rn(fr, lo);
     cyc = __fsub_rn(cyc, rintf(cyc));
-    float M = cyc * 6.28318530717958647692f;
-    float e = pc[4];
-    float s, c;
-    kepler_f32(M, e, s, c);
-    float inv = __frcp_rn(1.f - e * c);
-    return __fmaf_rn(__fmaf_rn(pc[5], c - e, -pc[6] * s), inv, pc[7]);
+    return cyc * 6.28318530717958647692f;
+}
+
+// NE independent FP32 Kepler solves: second-order series start, joint
+// Halley iterations until every |dE| < 1e-3 (cubic convergence leaves
+// ~1e-9), final (sin E, cos E) rotated by the last step.
+template <int NE>
+__device__ __forceinline__ void kepler_f32_n(const float (&M)[NE], float e, float (&s)[NE],
+                                             float (&c)[NE]) {
+    float E[NE], d[NE];
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+        float sM, cM;
+        __sincosf(M[k], &sM, &cM);
+        E[k] = M[k] + e * sM * (1.f + e * cM);
+        d[k] = 0.f;
+    }
+#pragma unroll 1
+    for (int it = 0; it < 16; ++it) {
+        bool more = false;
+#pragma unroll
+        for (int k = 0; k < NE; ++k) {
+            __sincosf(E[k], &s[k], &c[k]);
+            const float f = E[k] - e * s[k] - M[k];
+            const float f1 = 1.f - e * c[k];
+            const float f2 = e * s[k];
+            d[k] = __fdividef(f * f1, f1 * f1 - 0.5f * f * f2);
+            E[k] -= d[k];
+            more |= fabsf(d[k]) >= 1e-3f;
+        }
+        if (!more) break;
+    }
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+        const float d2 = d[k] * d[k];
+        const float cd = 1.f - 0.5f * d2;
+        const float sd = d[k] * (1.f - d2 * (1.f / 6.f));
+        const float sn = s[k] * cd - c[k] * sd;
+        const float cn = c[k] * cd + s[k] * sd;
+        s[k] = sn;
+        c[k] = cn;
+    }
+}
+
+// log u < x with FP32 logarithms; inside a guard band the FP64 values decide
+__device__ __forceinline__ bool metropolis(double nlp, double cur, double z, int dm1, uint32_t uword) {
+    const double u = u32u(uword);
+    const float lz = __logf((float)z);
+    const float lu = __logf((float)u);
+    const float a = (float)(nlp - cur);
+    const float m = a + (float)dm1 * lz - lu;
+    const float guard = 1e-4f * (1.f + fabsf(a) + fabsf(lu) + (float)dm1 * fabsf(lz));
+    if (m > guard) return true;
+    if (m < -guard) return false;
+    // reference arithmetic: ((ndim-1) ln z + nlp) - cur > ln u
+    return __dsub_rn(__dadd_rn(__dmul_rn((double)dm1, log(z)), nlp), cur) > log(u);
 }
 
 template <int PREC, int Q, int L, int NT>
@@ -100,6 +269,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     constexpr int G = NT / L;
     constexpr int PC = P<PREC>::kPC;
     constexpr int NQ = Q > 0 ? Q : 1;
+    constexpr int NE = (PREC == EMP_PREC_MIXED) ? 4 : 1;   // epochs in flight per lane
     extern __shared__ __align__(16) unsigned char smem[];
 
     const emp_model_desc* md = A.md;
@@ -126,13 +296,17 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     double* accc = reinterpret_cast<double*>(gs + lay.off_acc);
     double* red = reinterpret_cast<double*>(gs + lay.off_red);
     R* scan = reinterpret_cast<R*>(gs + lay.off_scan);
+    double* pterm = reinterpret_cast<double*>(gs + lay.off_pterm);
     double* misc = reinterpret_cast<double*>(gs + lay.off_misc);
+    int* flag = reinterpret_cast<int*>(misc + 4);
     constexpr int INSW = 2 + 2 * kMaxQ;
 
     // ---------------- walker identity and theta -------------------------
     int t_idx = 0, j_idx = 0, slot_j = 0;
-    double z = 1.0, logu = 0.0;
+    double z = 1.0;
+    uint32_t uword = 0u;
     if (active) {
+        if (r == 0) flag[0] = 0;
         if (A.mode == kModeLogpost) {
             for (int d = r; d < n_free; d += L) thp[d] = A.theta[(size_t)wk * n_free + d];
         } else if (A.mode == kModeSlots) {
@@ -151,9 +325,9 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             const int k_idx = 2 * kk + (1 - A.half);
             const int slot_k = A.members[t_idx * A.W + k_idx];
             // emcee StretchMove.get_proposal: zz = ((a-1) u + 1)^2 / a
-            double zz = __dadd_rn(__dmul_rn(A.a - 1.0, u53(rr.x, rr.y)), 1.0);
+            const double zz = __dadd_rn(__dmul_rn(A.a - 1.0, u53(rr.x, rr.y)), 1.0);
             z = __dmul_rn(zz, zz) / A.a;
-            logu = log(u32u(rr.w));
+            uword = rr.w;
             const double* sj = A.st_theta + (size_t)slot_j * n_free;
             const double* ck = A.st_theta + (size_t)slot_k * n_free;
             for (int d = r; d < n_free; d += L)
@@ -163,36 +337,62 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     __syncthreads();
     if (active) {
         for (int s = r; s < n_full; s += L) {
-            int src = md->full_src[s];
+            const int src = md->full_src[s];
             full[s] = src >= 0 ? thp[src] : md->full_fixed[s];
         }
     }
     __syncthreads();
 
-    // ---------------- prior and per-walker constants ---------------------
+    // ---------------- prior (lane-parallel) and per-walker constants -------
     if (active) {
-        if (r == 0) misc[0] = log_prior(md, full);
+        for (int d = r; d < n_free; d += L) {
+            const emp_prior& p = md->prior[d];
+            const double x = thp[d];
+            if (!in_support(x, p.lo, p.hi)) flag[0] = 1;
+            else if (p.kind == EMP_PRIOR_NORMAL || p.kind == EMP_PRIOR_BETA) pterm[d] = prior_var_term(p, x);
+        }
+        for (int q2 = r; q2 < 2 * n_planets; q2 += L) {
+            const int p = q2 >> 1, k = q2 & 1;
+            const emp_prior& dp = md->derived[p][k];
+            if (dp.kind == EMP_PRIOR_NONE) continue;
+            const double x = derived_x(full + md->kep_slot[p], k);
+            if (!in_support(x, dp.lo, dp.hi)) flag[0] = 1;
+            else if (dp.kind == EMP_PRIOR_NORMAL || dp.kind == EMP_PRIOR_BETA)
+                pterm[n_free + q2] = prior_var_term(dp, x);
+        }
         for (int p = r; p < n_planets; p += L) {
-            Elements el = planet_elements(md->kep_param[p], full + md->kep_slot[p]);
-            planet_consts<PREC>(el, pcs + p * PC);
+            if (PREC == EMP_PREC_FP64)
+                planet_consts_fp64(md->kep_param[p], full + md->kep_slot[p], (double*)(pcs + p * PC));
+            else
+                planet_consts_mixed(md->kep_param[p], full + md->kep_slot[p], (float*)(pcs + p * PC));
         }
         for (int k = r; k < n_ins; k += L) {
             R* ic = insc + k * INSW;
-            double off = md->offset_slot >= 0 ? full[md->offset_slot + k] : 0.0;
-            double jit = md->jitter_slot >= 0 ? full[md->jitter_slot + k] : 0.0;
+            const double off = md->offset_slot >= 0 ? full[md->offset_slot + k] : 0.0;
+            const double jit = md->jitter_slot >= 0 ? full[md->jitter_slot + k] : 0.0;
             ic[0] = (R)off;
-            ic[1] = (R)(jit * jit);
+            if (PREC == EMP_PREC_FP64) ic[1] = (R)(jit * jit);
+            else { const float jf = (float)jit; ic[1] = (R)(jf * jf); }
 #pragma unroll
             for (int c = 0; c < Q; ++c) {
-                int base = md->ma_global ? md->ma_slot + 2 * c
-                                         : md->ma_slot + 2 * Q * k + 2 * c;
-                double phi = full[base], tau = full[base + 1];
+                const int base = md->ma_global ? md->ma_slot + 2 * c : md->ma_slot + 2 * Q * k + 2 * c;
+                const double phi = full[base], tau = full[base + 1];
                 ic[2 + 2 * c] = (R)phi;
                 if (PREC == EMP_PREC_FP64) ic[3 + 2 * c] = (R)(-1.0 / tau);
-                else ic[3 + 2 * c] = (R)(-1.4426950408889634 / tau);   // exp2 scale
+                else ic[3 + 2 * c] = (R)(-1.44269504f / (float)tau);   // exp2 scale
             }
         }
         for (int j = r; j < acc_order; j += L) accc[j] = full[md->acc_slot + j];
+    }
+    __syncthreads();
+    if (active && r == 0) {
+        double lp = -INFINITY;
+        if (flag[0] == 0) {
+            lp = md->prior_const;
+            const int nv = md->n_prior_var;
+            for (int i = 0; i < nv; ++i) lp += pterm[md->prior_var[i]];
+        }
+        misc[0] = lp;
     }
     __syncthreads();
     const double lp = active ? misc[0] : -INFINITY;
@@ -202,7 +402,6 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     const int n = A.d.n;
     const int tile = A.tile;
     unsigned char* ts = smem;
-    // tile arrays
     R* s_t0;  R* s_t1;  R* s_y;  R* s_s2;  int* s_in;  R* s_dt;
     if (PREC == EMP_PREC_FP64) {
         s_t0 = reinterpret_cast<R*>(ts);
@@ -253,7 +452,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
         }
         __syncthreads();
 
-        // per-lane sequential pass over the lane's chunk
+        // per-lane sequential pass over the lane's chunk, NE epochs at a time
         KSum<R> ks; ks.init();
         R xh[NQ];
         R gh[NQ][NQ];
@@ -268,75 +467,106 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
         if (valid) {
             const int nr = max(0, min(C, nt - r * C));
 #pragma unroll 1
-            for (int kk = 0; kk < nr; ++kk) {
-                const int pos = kk * L + ((r + kk) & (L - 1));
-                R model = R(0);
+            for (int k0 = 0; k0 < nr; k0 += NE) {
+                int pos[NE];
+                bool ok[NE];
+                R model[NE];
+#pragma unroll
+                for (int e = 0; e < NE; ++e) {
+                    const int kk = k0 + e < nr ? k0 + e : nr - 1;
+                    ok[e] = k0 + e < nr;
+                    pos[e] = kk * L + ((r + kk) & (L - 1));
+                    model[e] = R(0);
+                }
                 if (PREC == EMP_PREC_FP64) {
-                    const double t = (double)s_t0[pos];
-                    if (acc_order > 0) {
-                        // np.polyval(concat(theta_acc, [0]), X_ - X_[0])
-                        double x = t - A.d.t0, pv = 0.0;
-                        for (int j = 0; j < acc_order; ++j) pv = pv * x + accc[j];
-                        pv = pv * x;
+#pragma unroll
+                    for (int e = 0; e < NE; ++e) {
+                        const double t = (double)s_t0[pos[e]];
+                        double m = 0.0;
                         for (int p = 0; p < n_planets; ++p)
-                            model = (R)((double)model + rv_term_f64((const double*)(pcs + p * PC), t));
-                        model = (R)((double)model + pv);
-                    } else {
-                        for (int p = 0; p < n_planets; ++p)
-                            model = (R)((double)model + rv_term_f64((const double*)(pcs + p * PC), t));
+                            m += rv_term_f64((const double*)(pcs + p * PC), t);
+                        if (acc_order > 0) {
+                            // np.polyval(concat(theta_acc, [0]), X_ - X_[0])
+                            double x = t - A.d.t0, pv = 0.0;
+                            for (int j = 0; j < acc_order; ++j) pv = pv * x + accc[j];
+                            m += pv * x;
+                        }
+                        model[e] = (R)m;
                     }
                 } else {
-                    const float th = (float)s_t0[pos], tl = (float)s_t1[pos];
-                    for (int p = 0; p < n_planets; ++p)
-                        model += (R)rv_term_mixed((const float*)(pcs + p * PC), th, tl);
+                    float th[NE], tl[NE];
+#pragma unroll
+                    for (int e = 0; e < NE; ++e) { th[e] = (float)s_t0[pos[e]]; tl[e] = (float)s_t1[pos[e]]; }
+                    for (int p = 0; p < n_planets; ++p) {
+                        const float* pc = (const float*)(pcs + p * PC);
+                        float M[NE], sn[NE], cs[NE];
+#pragma unroll
+                        for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e]);
+                        const float ec = pc[4];
+                        kepler_f32_n<NE>(M, ec, sn, cs);
+#pragma unroll
+                        for (int e = 0; e < NE; ++e) {
+                            const float inv = __frcp_rn(1.f - ec * cs[e]);
+                            model[e] += (R)__fmaf_rn(__fmaf_rn(pc[5], cs[e] - ec, -pc[6] * sn[e]), inv, pc[7]);
+                        }
+                    }
                     if (acc_order > 0) {
-                        float x = (th - (float)A.d.t0) + tl, pv = 0.f;
-                        for (int j = 0; j < acc_order; ++j) pv = pv * x + (float)accc[j];
-                        model += (R)(pv * x);
+#pragma unroll
+                        for (int e = 0; e < NE; ++e) {
+                            const float x = (th[e] - (float)A.d.t0) + tl[e];
+                            float pv = 0.f;
+                            for (int j = 0; j < acc_order; ++j) pv = pv * x + (float)accc[j];
+                            model[e] += (R)(pv * x);
+                        }
                     }
                 }
-                const int ki = s_in[pos];
-                const R* ic = insc + ki * INSW;
-                model += ic[0];
-                const R err2 = s_s2[pos] + ic[1];
-                R b = s_y[pos] - model;
-                R w, lt;
-                if (PREC == EMP_PREC_FP64) { w = R(1) / err2; lt = (R)log((double)err2); }
-                else { w = (R)__frcp_rn((float)err2); lt = (R)(__log2f((float)err2) * 0.69314718055994531f); }
-                if (Q == 0) {
-                    ks.add(b * b * w + lt);
-                } else {
-                    R x = b;
-                    R gn[NQ];
 #pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) gn[q2] = R(0);
+                for (int e = 0; e < NE; ++e) {
+                    if (!ok[e]) continue;
+                    const int ps = pos[e];
+                    const int ki = s_in[ps];
+                    const R* ic = insc + ki * INSW;
+                    const R mod = model[e] + ic[0];
+                    const R err2 = s_s2[ps] + ic[1];
+                    const R b = s_y[ps] - mod;
+                    R w, lt;
+                    if (PREC == EMP_PREC_FP64) { w = R(1) / err2; lt = (R)log((double)err2); }
+                    else { w = (R)__frcp_rn((float)err2); lt = (R)(__log2f((float)err2) * 0.69314718055994531f); }
+                    if (Q == 0) {
+                        ks.add(b * b * w + lt);
+                    } else {
+                        R x = b;
+                        R gn[NQ];
 #pragma unroll
-                    for (int c = 0; c < Q; ++c) {
-                        R dtc = s_dt[c * tile + pos];
-                        R a;
-                        if (PREC == EMP_PREC_FP64) a = ic[2 + 2 * c] * (R)exp((double)(dtc * ic[3 + 2 * c]));
-                        else a = ic[2 + 2 * c] * (R)exp2f((float)(dtc * ic[3 + 2 * c]));
-                        x -= a * xh[c];
+                        for (int q2 = 0; q2 < NQ; ++q2) gn[q2] = R(0);
 #pragma unroll
-                        for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
-                    }
+                        for (int c = 0; c < Q; ++c) {
+                            const R dtc = s_dt[c * tile + ps];
+                            R a;
+                            if (PREC == EMP_PREC_FP64) a = ic[2 + 2 * c] * (R)exp((double)(dtc * ic[3 + 2 * c]));
+                            else a = ic[2 + 2 * c] * (R)exp2f((float)(dtc * ic[3 + 2 * c]));
+                            x -= a * xh[c];
 #pragma unroll
-                    for (int m = NQ - 1; m > 0; --m) {
-                        xh[m] = xh[m - 1];
+                            for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
+                        }
 #pragma unroll
-                        for (int q2 = 0; q2 < NQ; ++q2) gh[m][q2] = gh[m - 1][q2];
-                    }
-                    xh[0] = x;
+                        for (int m = NQ - 1; m > 0; --m) {
+                            xh[m] = xh[m - 1];
 #pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) gh[0][q2] = gn[q2];
-                    const R wx = w * x;
-                    ks.add(wx * x + lt);
+                            for (int q2 = 0; q2 < NQ; ++q2) gh[m][q2] = gh[m - 1][q2];
+                        }
+                        xh[0] = x;
 #pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) {
-                        S1[q2] += wx * gn[q2];
-                        const R wg = w * gn[q2];
+                        for (int q2 = 0; q2 < NQ; ++q2) gh[0][q2] = gn[q2];
+                        const R wx = w * x;
+                        ks.add(wx * x + lt);
 #pragma unroll
-                        for (int q3 = 0; q3 < NQ; ++q3) S2[q2][q3] += wg * gn[q3];
+                        for (int q2 = 0; q2 < NQ; ++q2) {
+                            S1[q2] += wx * gn[q2];
+                            const R wg = w * gn[q2];
+#pragma unroll
+                            for (int q3 = 0; q3 < NQ; ++q3) S2[q2][q3] += wg * gn[q3];
+                        }
                     }
                 }
             }
@@ -403,14 +633,14 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     u[m] = v;
                 }
             }
-            double extra = 0.0;
+            R extra = R(0);
 #pragma unroll
             for (int q2 = 0; q2 < NQ; ++q2) {
-                extra += 2.0 * (double)u[q2] * (double)S1[q2];
+                extra += R(2) * u[q2] * S1[q2];
 #pragma unroll
-                for (int q3 = 0; q3 < NQ; ++q3) extra += (double)u[q2] * (double)u[q3] * (double)S2[q2][q3];
+                for (int q3 = 0; q3 < NQ; ++q3) extra += u[q2] * u[q3] * S2[q2][q3];
             }
-            tile_part += extra;
+            tile_part += (double)extra;
             // carry for the next tile = full prefix applied to carry
             {
                 const R* pm = src + (L - 1) * MS;
@@ -465,9 +695,11 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             const double lpj = A.st_logprior[slot_j];
             const double llj = A.st_logl[slot_j];
             const double cur = lpj > -INFINITY ? __dadd_rn(__dmul_rn(beta, llj), lpj) : -INFINITY;
-            const double nlp = valid ? __dadd_rn(__dmul_rn(beta, logl), lp) : -INFINITY;
-            const double lnpdiff = __dadd_rn(__dmul_rn((double)(n_free - 1), log(z)), nlp) - cur;
-            const int acc = (valid && lnpdiff > logu) ? 1 : 0;
+            int acc = 0;
+            if (valid) {
+                const double nlp = __dadd_rn(__dmul_rn(beta, logl), lp);
+                acc = metropolis(nlp, cur, z, n_free - 1, uword) ? 1 : 0;
+            }
             misc[1] = acc ? 1.0 : 0.0;
             if (acc) {
                 A.st_logl[slot_j] = logl;

@@ -22,10 +22,8 @@ __global__ void __launch_bounds__(256) k_model_mean(const emp_model_desc* md, De
         full[s] = src >= 0 ? th[src] : md->full_fixed[s];
     }
     __syncthreads();
-    for (int p = threadIdx.x; p < np; p += blockDim.x) {
-        Elements el = planet_elements(md->kep_param[p], full + md->kep_slot[p]);
-        planet_consts<EMP_PREC_FP64>(el, pcs + 8 * p);
-    }
+    for (int p = threadIdx.x; p < np; p += blockDim.x)
+        planet_consts_fp64(md->kep_param[p], full + md->kep_slot[p], pcs + 8 * p);
     for (int k = threadIdx.x; k < ni; k += blockDim.x) {
         ins[2 * k] = md->offset_slot >= 0 ? full[md->offset_slot + k] : 0.0;
         double j = md->jitter_slot >= 0 ? full[md->jitter_slot + k] : 0.0;

@@ -46,60 +46,126 @@ struct SwapArgs {
     int record_chain;
 };
 
+// log(u) < x decided with an FP32 logarithm; inside a guard band around
+// the boundary the FP64 logarithm decides, so every decision equals the
+// FP64 test (the FP32 log of a 32-bit uniform is within 2e-5 of the FP64 one)
+__device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
+    const float lf = __logf((float)u32u(word));
+    const double d = x - (double)lf;
+    const double guard = 1e-4 * (1.0 + fabs((double)lf));
+    if (d > guard) return true;
+    if (d < -guard) return false;
+    return log(u32u(word)) < x;
+}
+
+// Shared-memory variant when T*W fits; the state of each temperature pair is
+// staged by logical position (slot, logL), all random words are drawn up
+// front by every thread, counts and distances accumulate with shared atomics.
+template <bool SMEM>
 __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
-    __shared__ int s_cnt[32];
-    __shared__ double s_dst[32];
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    __shared__ int s_cnt[kMaxTemps];
+    __shared__ float s_dst[kMaxTemps];
+    __shared__ uint32_t s_perm[kMaxTemps][2];
     __shared__ double s_ratio[kMaxTemps];
     __shared__ double s_smd[kMaxTemps];
     __shared__ double s_invb[kMaxTemps];
+    __shared__ double s_term[kMaxTemps];
 
     const int tid = threadIdx.x;
     const int nth = blockDim.x;
     const uint64_t sweep = (uint64_t)S.counters[1];
     const int T = S.T, W = S.W, D = S.D;
+    const int TW = T * W;
+    double* s_ll = reinterpret_cast<double*>(sm_raw);              // [T*W] logL by position
+    int* s_mem = reinterpret_cast<int*>(s_ll + (SMEM ? TW : 0));    // [T*W] slot by position
+    uint32_t* s_u = reinterpret_cast<uint32_t*>(s_mem + (SMEM ? TW : 0));  // [T*W] words
 
-    for (int t = tid; t < T; t += nth) S.betas_used[t] = S.betas[t];
+    for (int t = tid; t < T; t += nth) {
+        S.betas_used[t] = S.betas[t];
+        s_cnt[t] = 0;
+        s_dst[t] = 0.f;
+        if (t >= 1) {
+            U4 pr = rng_draw(S.seed, (uint32_t)t, sweep, kRngSwapPerm);
+            s_perm[t][0] = (uint32_t)S.units[pr.x % (uint32_t)S.nunits];
+            s_perm[t][1] = pr.y % (uint32_t)W;
+        }
+    }
+    if (SMEM) {
+        for (int k = tid; k < TW; k += nth) {
+            const int sl = S.members[k];
+            s_mem[k] = sl;
+            s_ll[k] = S.logl[sl];
+            s_u[k] = k >= W ? rng_draw(S.seed, (uint32_t)k, sweep, kRngSwapAcc).x : 0u;
+        }
+    }
     __syncthreads();
 
     for (int i = T - 1; i >= 1; --i) {
-        U4 pr = rng_draw(S.seed, (uint32_t)i, sweep, kRngSwapPerm);
-        const uint32_t m = (uint32_t)S.units[pr.x % (uint32_t)S.nunits];
-        const uint32_t b = pr.y % (uint32_t)W;
+        const uint32_t m = s_perm[i][0];
+        const uint32_t b = s_perm[i][1];
         const double dbeta = S.betas[i - 1] - S.betas[i];
-        int cnt = 0;
-        double dist = 0.0;
         for (int j = tid; j < W; j += nth) {
             const int jp = (int)(((uint64_t)m * (uint64_t)j + b) % (uint64_t)W);
             const int ia = i * W + j, ib = (i - 1) * W + jp;
-            const int sa = S.members[ia], sb = S.members[ib];
-            U4 ra = rng_draw(S.seed, (uint32_t)ia, sweep, kRngSwapAcc);
-            const double paccept = dbeta * (S.logl[sa] - S.logl[sb]);
-            if (log(u32u(ra.x)) < paccept) {
-                S.members[ia] = sb;
-                S.members[ib] = sa;
-                ++cnt;
+            int sa, sb;
+            double la, lb;
+            uint32_t word;
+            if (SMEM) {
+                sa = s_mem[ia]; sb = s_mem[ib]; la = s_ll[ia]; lb = s_ll[ib]; word = s_u[ia];
+            } else {
+                sa = S.members[ia]; sb = S.members[ib]; la = S.logl[sa]; lb = S.logl[sb];
+                word = rng_draw(S.seed, (uint32_t)ia, sweep, kRngSwapAcc).x;
+            }
+            const double paccept = dbeta * (la - lb);
+            if (log_uniform_below(word, paccept)) {
+                if (SMEM) {
+                    s_mem[ia] = sb; s_mem[ib] = sa; s_ll[ia] = lb; s_ll[ib] = la;
+                } else {
+                    S.members[ia] = sb; S.members[ib] = sa;
+                }
+                atomicAdd(&s_cnt[i], 1);
                 const double* xa = S.theta + (size_t)sa * D;
                 const double* xb = S.theta + (size_t)sb * D;
-                double ss = 0.0;
-                for (int d = 0; d < D; ++d) { double v = xa[d] - xb[d]; ss += v * v; }
-                dist += sqrt(ss);
+                float ss = 0.f;
+                for (int d = 0; d < D; ++d) {
+                    const float v = (float)(xa[d] - xb[d]);
+                    ss = fmaf(v, v, ss);
+                }
+                atomicAdd(&s_dst[i], sqrtf(ss));
             }
         }
-        // block reduction
-        for (int o = 16; o > 0; o >>= 1) {
-            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-            dist += __shfl_xor_sync(0xffffffffu, dist, o);
+        __syncthreads();
+    }
+    if (SMEM)
+        for (int k = tid; k < TW; k += nth) S.members[k] = s_mem[k];
+    for (int t = tid + 1; t < T; t += nth) {
+        const int c = s_cnt[t];
+        s_ratio[t - 1] = (double)c / (double)W;
+        s_smd[t - 1] = c > 0 ? (double)s_dst[t] / (double)c : 0.0;
+        S.swaps_accepted[t] += c;
+    }
+    __syncthreads();
+    // ladder adaptation, the exponentials and reciprocals in parallel
+    const bool adapt = S.adapt && T > 2;
+    if (adapt) {
+        const double kappa = S.adapt_tau / ((double)sweep + S.adapt_tau) / S.adapt_nu;
+        for (int t = tid; t < T - 1; t += nth) s_invb[t] = 1.0 / S.betas[t];
+        __syncthreads();
+        for (int k = tid; k < T - 2; k += nth) {
+            const double dS = kappa * (s_ratio[k] - s_ratio[k + 1]);
+            s_term[k] = __dmul_rn(s_invb[k + 1] - s_invb[k], exp(dS));
         }
-        if ((tid & 31) == 0) { s_cnt[tid >> 5] = cnt; s_dst[tid >> 5] = dist; }
         __syncthreads();
         if (tid == 0) {
-            int c = 0; double dd = 0.0;
-            for (int w = 0; w < (nth + 31) / 32; ++w) { c += s_cnt[w]; dd += s_dst[w]; }
-            s_ratio[i - 1] = (double)c / (double)W;
-            s_smd[i - 1] = c > 0 ? dd / (double)c : 0.0;
-            S.swaps_accepted[i] += c;
+            double cum = s_invb[0];
+            for (int k = 0; k < T - 2; ++k) {
+                cum = __dadd_rn(cum, s_term[k]);
+                s_term[k] = cum;
+            }
         }
         __syncthreads();
+        for (int k = tid; k < T - 2; k += nth) S.betas[k + 1] = 1.0 / s_term[k];
     }
 
     if (tid == 0) {
@@ -107,7 +173,7 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
         const int64_t row = S.n_rec[1];
         const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
         if (rec_sweep && row < S.cap) {
-            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = S.betas[t];
+            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = S.betas_used[t];
             if (S.tsw_hist) for (int k = 0; k < T - 1; ++k) S.tsw_hist[row * (T - 1) + k] = s_ratio[k];
             if (S.smd_hist) for (int k = 0; k < T - 1; ++k) S.smd_hist[row * (T - 1) + k] = s_smd[k];
             S.n_rec[1] = row + 1;
@@ -118,17 +184,6 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
             S.n_rec[0] = crow + 1;
         } else {
             *S.chain_row = -1;
-        }
-        // ladder adaptation (mode 0: swap-acceptance equalisation)
-        if (S.adapt && T > 2) {
-            const double kappa = S.adapt_tau / ((double)sweep + S.adapt_tau) / S.adapt_nu;
-            for (int t = 0; t < T - 1; ++t) s_invb[t] = 1.0 / S.betas[t];
-            double cum = s_invb[0];
-            for (int k = 0; k < T - 2; ++k) {
-                const double dS = kappa * (s_ratio[k] - s_ratio[k + 1]);
-                cum = __dadd_rn(cum, __dmul_rn(s_invb[k + 1] - s_invb[k], exp(dS)));
-                S.betas[k + 1] = 1.0 / cum;
-            }
         }
         S.counters[0] += S.nsteps;
         S.counters[1] += 1;

@@ -90,7 +90,11 @@ struct emp_handle {
     cudaStream_t own = nullptr;
     GraphCache gc;
     bool attr_done[2][4][6] = {};
+    bool swap_attr = false;
 };
+
+// dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
+static const size_t kSwapSmemMax = 200 * 1024;
 
 namespace {
 
@@ -154,6 +158,16 @@ int validate_model(const emp_model_desc* m) {
         if (src >= m->n_free) return fail(EMP_E_INVALID, "full_src[%d]=%d >= n_free", s, src);
         if (src >= 0) seen[src]++;
         else if (!isfinite(m->full_fixed[s])) return fail(EMP_E_INVALID, "fixed value of slot %d not finite", s);
+    }
+    if (m->n_prior_var < 0 || m->n_prior_var > m->n_free + 2 * m->n_planets)
+        return fail(EMP_E_INVALID, "n_prior_var=%d out of range", m->n_prior_var);
+    for (int i = 0; i < m->n_prior_var; ++i) {
+        const int v = m->prior_var[i];
+        if (v < 0 || v >= m->n_free + 2 * m->n_planets)
+            return fail(EMP_E_INVALID, "prior_var[%d]=%d out of range", i, v);
+        const emp_prior& p = v < m->n_free ? m->prior[v] : m->derived[(v - m->n_free) >> 1][(v - m->n_free) & 1];
+        if (p.kind != EMP_PRIOR_NORMAL && p.kind != EMP_PRIOR_BETA)
+            return fail(EMP_E_INVALID, "prior_var[%d] names a constant prior", i);
     }
     for (int i = 0; i < m->n_free; ++i) {
         if (seen[i] != 1) return fail(EMP_E_INVALID, "free parameter %d mapped %d times", i, seen[i]);
@@ -286,8 +300,18 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
     S.cap = have_rec ? rec->capacity : 0;
     S.thin = have_rec ? std::max(1, rec->thin) : 1;
     S.record_chain = have_rec && (rec->chain || rec->log_like || rec->log_prob);
-    int nth = std::min(1024, std::max(32, ((st->nwalkers + 31) / 32) * 32));
-    k_swap<<<1, nth, 0, s>>>(S);
+    int nth = 1024;
+    const size_t swap_smem = (size_t)st->ntemps * st->nwalkers * 16;
+    if (swap_smem <= kSwapSmemMax) {
+        if (!h->swap_attr) {
+            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+            h->swap_attr = true;
+        }
+        k_swap<true><<<1, nth, swap_smem, s>>>(S);
+    } else {
+        k_swap<false><<<1, nth, 0, s>>>(S);
+    }
     g_launches.fetch_add(1);
     ++kcount;
     CUDA_TRY(cudaGetLastError());
@@ -581,6 +605,11 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, 
             CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           227 * 1024));
             h->attr_done[st->precision][h->q][li] = true;
+        }
+        if (!h->swap_attr) {
+            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+            h->swap_attr = true;
         }
         CUDA_TRY(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
         int nk = 0;

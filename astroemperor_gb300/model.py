@@ -434,6 +434,33 @@ class ReddModel:
                     md.full_fixed[slot] = float(p.fixed)
         md.n_planets = planet
         md.loglike_const = float(- 0.5 * np.log(2 * np.pi) * self.data.ndata)
+        # constant prior terms summed in my_prior's order (block by block,
+        # each Keplerian block followed by its derived priors)
+        const, var = 0.0, []
+        planet = 0
+        fi = 0
+        for b in self.blocks:
+            for p in b:
+                if p.fixed is not None:
+                    continue
+                pr = md.prior[fi]
+                if pr.kind in (N.PRIOR_KIND['Uniform'], N.PRIOR_KIND['Jeffreys']):
+                    const += pr.a0
+                else:
+                    var.append(fi)
+                fi += 1
+            if b.type_ == 'Keplerian':
+                for k in range(2):
+                    pr = md.derived[planet][k]
+                    if pr.kind in (N.PRIOR_KIND['Uniform'], N.PRIOR_KIND['Jeffreys']):
+                        const += pr.a0
+                    elif pr.kind != N.EMP_PRIOR_NONE:
+                        var.append(self.ndim__ + 2 * planet + k)
+                planet += 1
+        md.prior_const = float(const)
+        md.n_prior_var = len(var)
+        for i, v in enumerate(var):
+            md.prior_var[i] = v
         return md
 
 

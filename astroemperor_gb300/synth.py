@@ -125,8 +125,9 @@ def build_model(name: str, seed: int = 1234, parameterisation: int = 1,
 
     Blocks follow ``Simulation._autorun_add_RV_ins`` order (Keplerians first,
     then offset, jitter, MOAV).  Limits are widened where the generating
-    values sit outside the defaults (MA coefficient 0.4 > 0.3,
-    ``block_repo.py:730``; periods kept inside [1.5, span]).
+    values sit outside or on the edge of the defaults (MA coefficient 0.4 >
+    0.3 and timescale 5 d on the lower edge of [5, 25], ``block_repo.py:730``);
+    each period gets a +-10% search box around its generating value.
     """
     instruments, truth = make_system(name, seed)
     data = preprocess_instruments(instruments, [f'INS{k + 1}' for k in range(len(instruments))])
@@ -153,6 +154,8 @@ def build_model(name: str, seed: int = 1234, parameterisation: int = 1,
         for p in mb:
             if p.name.startswith('MACoefficient'):
                 p.limits = [0.0, 1.0]
+            elif p.name.startswith('MATimescale'):
+                p.limits = [1.0, 50.0]
         blocks.append(mb)
     model = ReddModel(blocks, data, moav_reference_quirk=moav_reference_quirk)
     theta = truth_theta(model, truth, data, parameterisation)

@@ -120,7 +120,8 @@ def cpu_baseline(model, data, truth, seconds, ncores=None):
     from oracle import cpu_baseline as cb
     lim = model.limits_free()
     rng = np.random.default_rng(7)
-    th = truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(64, len(truth)))
+    th = np.clip(truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(64, len(truth))),
+                 lim[:, 0], lim[:, 1])
     ncores = ncores or os.cpu_count() or 1
     eps, n, el, nc = cb.time_pool(model.spec(), data.as_dict(), th, ncores=ncores,
                                   min_seconds=seconds, max_seconds=2 * seconds)
@@ -192,7 +193,8 @@ def main():
     ctx = Context(model, str(dev))
     lim = model.limits_free()
     rng = np.random.default_rng(SEED + rank)
-    p0 = truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, D))
+    p0 = np.clip(truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, D)),
+                 lim[:, 0], lim[:, 1])
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def timed_sweeps(precision, steps, warmup):

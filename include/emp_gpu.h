@@ -97,6 +97,14 @@ typedef struct emp_model_desc {
        [p][0]: Ecc (x = th[3]^2 + th[4]^2), [p][1]: Amp (x = th[1]^2 + th[2]^2) */
     emp_prior derived[EMP_MAX_PLANETS][2];
     double  loglike_const;        /* -0.5 ln(2 pi) ndat  (00.like:1) */
+    /* sum, in my_prior's order, of the constant terms (Uniform, Jeffreys) of
+       free and derived priors; the device adds the other terms to it */
+    double  prior_const;
+    int32_t n_prior_var;          /* terms that vary with theta (Normal, Beta) */
+    int32_t _pad1;
+    /* their indices: i < n_free -> free parameter i,
+       n_free + 2p + k -> derived prior k of planet p */
+    int32_t prior_var[EMP_MAX_PARAMS + 2 * EMP_MAX_PLANETS];
 } emp_model_desc;
 
 /*

@@ -64,7 +64,8 @@ def test_replay_matches_oracle(peg_arr, lib, cuda, adapt):
                                rtol=1e-11)
     np.testing.assert_allclose(gpu.get_betas(), np.array(ora.beta_hist), rtol=1e-14)
     np.testing.assert_allclose(gpu.get_tsw(), np.array(ora.tsw_hist), rtol=0, atol=0)
-    np.testing.assert_allclose(gpu.get_smd(), np.array(ora.smd_hist), rtol=1e-12)
+    # mean swap distances are accumulated in FP32 on the device
+    np.testing.assert_allclose(gpu.get_smd(), np.array(ora.smd_hist), rtol=1e-5)
     np.testing.assert_allclose(gpu.betas, ora.betas, rtol=1e-14)
     np.testing.assert_array_equal(gpu.accepted, ora.accepted)
     assert ora.accepted.sum() > 0 and np.array(ora.tsw_hist).sum() > 0
