@@ -76,6 +76,7 @@ class EmpPtState(C.Structure):
         ('seed', C.c_uint64), ('a', C.c_double),
         ('adapt_tau', C.c_double), ('adapt_nu', C.c_double),
         ('adapt_mode', C.c_int32), ('precision', C.c_int32),
+        ('work', C.c_void_p), ('work_bytes', C.c_int64),
     ]
 
 
@@ -99,6 +100,7 @@ SIGNATURES = {
     'emp_pt_run': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord), C.c_int,
                              C.c_int, C.c_void_p]),
     'emp_pt_evaluate': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.c_void_p]),
+    'emp_pt_work_bytes': (C.c_int64, [C.c_int, C.c_int, C.c_int]),
     'emp_set_launch': (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     'emp_get_launch': (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     'emp_probe_peaks': (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),

@@ -20,9 +20,38 @@ namespace emp {
 
 constexpr int kMaxTemps = 256;
 
+// Caller-owned workspace of one PT state (emp_pt_work_bytes).  The swap
+// kernel fills it; the record kernel reads and resets the smd part.
+struct Work {
+    double* betas_used;   // [kMaxTemps] ladder of the running sweep
+    int64_t* rows;        // [0] chain row, [1] sweep-history row (-1: none)
+    int* pair_count;      // [kMaxTemps] accepted swaps of pair (t-1, t) this sweep
+    float* smd_acc;       // [kMaxTemps] distance sums (zero between sweeps)
+    unsigned int* ticket; // [1] blocks of the record kernel done (zero between sweeps)
+    int64_t* nrec_none;   // [2] zero row counters used when nothing is recorded
+    int2* pairs;          // [T*W] accepted (slot_a, slot_b) of pair t at [t*W + k]
+};
+
+__host__ __device__ inline size_t work_bytes(int T, int W) {
+    return 8 * (size_t)kMaxTemps + 16 + 4 * (size_t)kMaxTemps + 4 * (size_t)kMaxTemps + 16 + 16 +
+           8 * (size_t)T * (size_t)W;
+}
+
+__host__ __device__ inline Work carve_work(void* base) {
+    char* p = static_cast<char*>(base);
+    Work w;
+    w.betas_used = reinterpret_cast<double*>(p); p += 8 * kMaxTemps;
+    w.rows = reinterpret_cast<int64_t*>(p);      p += 16;
+    w.pair_count = reinterpret_cast<int*>(p);    p += 4 * kMaxTemps;
+    w.smd_acc = reinterpret_cast<float*>(p);     p += 4 * kMaxTemps;
+    w.ticket = reinterpret_cast<unsigned int*>(p); p += 16;
+    w.nrec_none = reinterpret_cast<int64_t*>(p); p += 16;
+    w.pairs = reinterpret_cast<int2*>(p);
+    return w;
+}
+
 struct SwapArgs {
     int T, W, D, nsteps;
-    const double* theta;
     const double* logl;
     int* members;
     double* betas;
@@ -34,12 +63,11 @@ struct SwapArgs {
     int adapt_mode;
     double adapt_tau, adapt_nu;
     uint64_t seed;
-    double* betas_used;       // [T] scratch: ladder of this sweep
-    int64_t* chain_row;       // scratch: row the record kernel writes, -1 none
+    Work work;
     // histories
     double* beta_hist;
     double* tsw_hist;
-    double* smd_hist;
+    int have_smd;
     int64_t* n_rec;           // [2]
     int64_t cap;
     int thin;
@@ -58,33 +86,33 @@ __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
     return log(u32u(word)) < x;
 }
 
-// Shared-memory variant when T*W fits; the state of each temperature pair is
-// staged by logical position (slot, logL), all random words are drawn up
-// front by every thread, counts and distances accumulate with shared atomics.
+// One CTA.  With SMEM the positions of every temperature (slot, logL) are
+// staged in shared memory and all random words are drawn up front by every
+// thread; the temperature pairs are then visited from the hottest down with
+// one barrier between pairs.  Accepted exchanges are logged for the swap
+// distance, which the record kernel computes across the whole GPU.
 template <bool SMEM>
 __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     __shared__ int s_cnt[kMaxTemps];
-    __shared__ float s_dst[kMaxTemps];
     __shared__ uint32_t s_perm[kMaxTemps][2];
     __shared__ double s_ratio[kMaxTemps];
-    __shared__ double s_smd[kMaxTemps];
     __shared__ double s_invb[kMaxTemps];
     __shared__ double s_term[kMaxTemps];
 
     const int tid = threadIdx.x;
     const int nth = blockDim.x;
     const uint64_t sweep = (uint64_t)S.counters[1];
-    const int T = S.T, W = S.W, D = S.D;
+    const int T = S.T, W = S.W;
     const int TW = T * W;
+    Work& wk = S.work;
     double* s_ll = reinterpret_cast<double*>(sm_raw);              // [T*W] logL by position
     int* s_mem = reinterpret_cast<int*>(s_ll + (SMEM ? TW : 0));    // [T*W] slot by position
     uint32_t* s_u = reinterpret_cast<uint32_t*>(s_mem + (SMEM ? TW : 0));  // [T*W] words
 
     for (int t = tid; t < T; t += nth) {
-        S.betas_used[t] = S.betas[t];
+        wk.betas_used[t] = S.betas[t];
         s_cnt[t] = 0;
-        s_dst[t] = 0.f;
         if (t >= 1) {
             U4 pr = rng_draw(S.seed, (uint32_t)t, sweep, kRngSwapPerm);
             s_perm[t][0] = (uint32_t)S.units[pr.x % (uint32_t)S.nunits];
@@ -124,26 +152,21 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
                 } else {
                     S.members[ia] = sb; S.members[ib] = sa;
                 }
-                atomicAdd(&s_cnt[i], 1);
-                const double* xa = S.theta + (size_t)sa * D;
-                const double* xb = S.theta + (size_t)sb * D;
-                float ss = 0.f;
-                for (int d = 0; d < D; ++d) {
-                    const float v = (float)(xa[d] - xb[d]);
-                    ss = fmaf(v, v, ss);
-                }
-                atomicAdd(&s_dst[i], sqrtf(ss));
+                const int k = atomicAdd(&s_cnt[i], 1);
+                wk.pairs[i * W + k] = make_int2(sa, sb);
             }
         }
         __syncthreads();
     }
     if (SMEM)
         for (int k = tid; k < TW; k += nth) S.members[k] = s_mem[k];
-    for (int t = tid + 1; t < T; t += nth) {
-        const int c = s_cnt[t];
-        s_ratio[t - 1] = (double)c / (double)W;
-        s_smd[t - 1] = c > 0 ? (double)s_dst[t] / (double)c : 0.0;
-        S.swaps_accepted[t] += c;
+    for (int t = tid; t < T; t += nth) {
+        const int c = t >= 1 ? s_cnt[t] : 0;
+        wk.pair_count[t] = c;
+        if (t >= 1) {
+            s_ratio[t - 1] = (double)c / (double)W;
+            S.swaps_accepted[t] += c;
+        }
     }
     __syncthreads();
     // ladder adaptation, the exponentials and reciprocals in parallel
@@ -172,18 +195,19 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
         // histories of this sweep (ladder used during the sweep)
         const int64_t row = S.n_rec[1];
         const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
+        wk.rows[1] = -1;
         if (rec_sweep && row < S.cap) {
-            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = S.betas_used[t];
+            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = wk.betas_used[t];
             if (S.tsw_hist) for (int k = 0; k < T - 1; ++k) S.tsw_hist[row * (T - 1) + k] = s_ratio[k];
-            if (S.smd_hist) for (int k = 0; k < T - 1; ++k) S.smd_hist[row * (T - 1) + k] = s_smd[k];
+            if (S.have_smd) wk.rows[1] = row;
             S.n_rec[1] = row + 1;
         }
         const int64_t crow = S.n_rec[0];
         if (S.record_chain && rec_sweep && crow < S.cap) {
-            *S.chain_row = crow;
+            wk.rows[0] = crow;
             S.n_rec[0] = crow + 1;
         } else {
-            *S.chain_row = -1;
+            wk.rows[0] = -1;
         }
         S.counters[0] += S.nsteps;
         S.counters[1] += 1;
@@ -196,36 +220,79 @@ struct RecArgs {
     const double* logl;
     const double* logprior;
     const int* members;
-    const double* betas_used;
-    const int64_t* chain_row;
+    Work work;
     double* chain;
     double* log_like;
     double* log_prob;
+    double* smd_hist;
 };
 
+// History rows of one sweep across the GPU: chain, log-likelihood and
+// tempered log-posterior by logical position, and the mean Euclidean
+// distance between the walkers of each accepted swap (one warp per swap;
+// the last block to finish turns the sums into means and resets them).
 __global__ void __launch_bounds__(256) k_record(RecArgs R) {
-    const int64_t row = *R.chain_row;
-    if (row < 0) return;
+    __shared__ int s_last;
+    const int64_t row = R.work.rows[0];
     const int64_t TW = (int64_t)R.T * R.W;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (R.chain) {
-        const int64_t tot = TW * R.D;
-        double* dst = R.chain + row * tot;
-        for (int64_t idx = g0; idx < tot; idx += stride) {
-            const int64_t tj = idx / R.D;
-            const int d = (int)(idx - tj * R.D);
-            dst[idx] = R.theta[(int64_t)R.members[tj] * R.D + d];
+    if (row >= 0) {
+        if (R.chain) {
+            const int64_t tot = TW * R.D;
+            double* dst = R.chain + row * tot;
+            for (int64_t idx = g0; idx < tot; idx += stride) {
+                const int64_t tj = idx / R.D;
+                const int d = (int)(idx - tj * R.D);
+                dst[idx] = R.theta[(int64_t)R.members[tj] * R.D + d];
+            }
+        }
+        for (int64_t idx = g0; idx < TW; idx += stride) {
+            const int slot = R.members[idx];
+            const double ll = R.logl[slot], lp = R.logprior[slot];
+            if (R.log_like) R.log_like[row * TW + idx] = ll;
+            if (R.log_prob) {
+                const int t = (int)(idx / R.W);
+                R.log_prob[row * TW + idx] = lp > -INFINITY ? __dadd_rn(__dmul_rn(R.work.betas_used[t], ll), lp) : -INFINITY;
+            }
         }
     }
-    for (int64_t idx = g0; idx < TW; idx += stride) {
-        const int slot = R.members[idx];
-        const double ll = R.logl[slot], lp = R.logprior[slot];
-        if (R.log_like) R.log_like[row * TW + idx] = ll;
-        if (R.log_prob) {
-            const int t = (int)(idx / R.W);
-            R.log_prob[row * TW + idx] = lp > -INFINITY ? __dadd_rn(__dmul_rn(R.betas_used[t], ll), lp) : -INFINITY;
+    const int64_t srow = R.work.rows[1];
+    if (R.smd_hist == nullptr || srow < 0 || R.T < 2) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t tasks = (int64_t)(R.T - 1) * R.W;
+    for (int64_t task = warp; task < tasks; task += nwarps) {
+        const int i = (int)(task / R.W) + 1;
+        const int k = (int)(task - (int64_t)(i - 1) * R.W);
+        if (k >= R.work.pair_count[i]) continue;
+        const int2 pr = R.work.pairs[i * R.W + k];
+        const double* xa = R.theta + (size_t)pr.x * R.D;
+        const double* xb = R.theta + (size_t)pr.y * R.D;
+        float ss = 0.f;
+        for (int d = lane; d < R.D; d += 32) {
+            const float v = (float)(xa[d] - xb[d]);
+            ss = fmaf(v, v, ss);
         }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if (lane == 0) atomicAdd(&R.work.smd_acc[i], sqrtf(ss));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = (atomicAdd(R.work.ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        for (int i = threadIdx.x + 1; i < R.T; i += blockDim.x) {
+            const int c = R.work.pair_count[i];
+            const float sum = atomicExch(&R.work.smd_acc[i], 0.f);
+            R.smd_hist[srow * (R.T - 1) + i - 1] = c > 0 ? (double)sum / (double)c : 0.0;
+        }
+        if (threadIdx.x == 0) *R.work.ticket = 0u;
     }
 }
 

@@ -84,8 +84,6 @@ struct emp_handle {
     DevData dd{};
     int L[2] = {0, 0};
     int tile[2] = {0, 0};
-    double* scratch = nullptr; // betas_used [kMaxTemps] + chain_row
-    int64_t* chain_row = nullptr;
     int* dev2orig = nullptr;
     cudaStream_t own = nullptr;
     GraphCache gc;
@@ -182,10 +180,14 @@ int validate_model(const emp_model_desc* m) {
     return EMP_OK;
 }
 
+// default lanes per walker when the autotuner has not set one: about 16
+// epochs per lane for the mixed kernel (measured best for N=1024 at 1280
+// walkers), more lanes for the FP64 kernel, whose per-epoch work is longer
 int pick_default_L(int prec, int n) {
-    (void)prec;
-    if (n >= 4096) return 64;
-    return 32;
+    int target = prec == EMP_PREC_FP64 ? n / 8 : n / 16;
+    int L = 8;
+    while (L < target && L < (prec == EMP_PREC_FP64 ? 128 : 64)) L <<= 1;
+    return L;
 }
 
 int pick_tile(const emp_handle* h, int prec, int L, int G, Smem& lay) {
@@ -255,6 +257,11 @@ int check_state(const emp_handle* h, const emp_pt_state* st) {
     if (!(st->a > 1.0)) return fail(EMP_E_INVALID, "stretch scale a=%g must be > 1", st->a);
     if (st->adapt && !(st->adapt_tau > 0 && st->adapt_nu > 0))
         return fail(EMP_E_INVALID, "adapt_tau and adapt_nu must be > 0");
+    if (!st->work) return fail(EMP_E_INVALID, "state workspace is NULL");
+    if (st->work_bytes < (int64_t)work_bytes(st->ntemps, st->nwalkers))
+        return fail(EMP_E_SIZE, "workspace of %lld B < %zu B needed", (long long)st->work_bytes,
+                    work_bytes(st->ntemps, st->nwalkers));
+    if (((uintptr_t)st->work) & 15) return fail(EMP_E_INVALID, "workspace not 16-byte aligned");
     return EMP_OK;
 }
 
@@ -285,22 +292,21 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
     }
     SwapArgs S{};
     S.T = st->ntemps; S.W = st->nwalkers; S.D = st->ndim; S.nsteps = st->nsteps;
-    S.theta = st->theta; S.logl = st->logl; S.members = st->members; S.betas = st->betas;
+    S.logl = st->logl; S.members = st->members; S.betas = st->betas;
     S.counters = st->counters; S.swaps_accepted = st->swaps_accepted;
     S.units = st->perm_units; S.nunits = st->n_perm_units;
     S.adapt = st->adapt; S.adapt_mode = st->adapt_mode;
     S.adapt_tau = st->adapt_tau; S.adapt_nu = st->adapt_nu; S.seed = st->seed;
-    S.betas_used = h->scratch;
-    S.chain_row = h->chain_row;
-    bool have_rec = rec && rec->n_recorded;
+    S.work = carve_work(st->work);
+    const bool have_rec = rec && rec->n_recorded;
     S.beta_hist = have_rec ? rec->beta_history : nullptr;
     S.tsw_hist = have_rec ? rec->tsw_history : nullptr;
-    S.smd_hist = have_rec ? rec->smd_history : nullptr;
-    S.n_rec = have_rec ? rec->n_recorded : h->chain_row + 1;   // dummy pair when not recording
+    S.have_smd = have_rec && rec->smd_history != nullptr;
+    S.n_rec = have_rec ? rec->n_recorded : S.work.nrec_none;
     S.cap = have_rec ? rec->capacity : 0;
     S.thin = have_rec ? std::max(1, rec->thin) : 1;
     S.record_chain = have_rec && (rec->chain || rec->log_like || rec->log_prob);
-    int nth = 1024;
+    const int nth = 1024;
     const size_t swap_smem = (size_t)st->ntemps * st->nwalkers * 16;
     if (swap_smem <= kSwapSmemMax) {
         if (!h->swap_attr) {
@@ -315,14 +321,17 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
     g_launches.fetch_add(1);
     ++kcount;
     CUDA_TRY(cudaGetLastError());
-    if (S.record_chain) {
+    if (S.record_chain || S.have_smd) {
         RecArgs R{};
         R.T = st->ntemps; R.W = st->nwalkers; R.D = st->ndim;
         R.theta = st->theta; R.logl = st->logl; R.logprior = st->logprior;
-        R.members = st->members; R.betas_used = h->scratch; R.chain_row = h->chain_row;
+        R.members = st->members; R.work = S.work;
         R.chain = rec->chain; R.log_like = rec->log_like; R.log_prob = rec->log_prob;
-        int64_t tot = (int64_t)st->ntemps * st->nwalkers * (rec->chain ? st->ndim : 1);
-        int grid = (int)std::min<int64_t>(std::max<int64_t>(1, (tot + 255) / 256), 152 * 8);
+        R.smd_hist = rec->smd_history;
+        const int64_t tot = (int64_t)st->ntemps * st->nwalkers * (rec->chain ? st->ndim : 1);
+        const int64_t warps = (int64_t)(st->ntemps - 1) * st->nwalkers;
+        const int64_t want = std::max((tot + 255) / 256, (warps + 7) / 8);
+        const int grid = (int)std::min<int64_t>(std::max<int64_t>(1, want), 152 * 8);
         k_record<<<grid, 256, 0, s>>>(R);
         g_launches.fetch_add(1);
         ++kcount;
@@ -425,7 +434,6 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_ha
     size_t o_sf = take(4 * (size_t)n), o_dtf = take(4 * qn), o_in = take(4 * (size_t)n);
     size_t o_perm = take(4 * (size_t)n);
     size_t o_md = take(sizeof(emp_model_desc));
-    size_t o_sc = take(8 * (kMaxTemps + 4));
     cudaError_t e = cudaMalloc(&h->dbuf, bytes);
     if (e != cudaSuccess) {
         delete h;
@@ -448,8 +456,6 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_ha
     }
     h->md_dev = (emp_model_desc*)(b + o_md);
     h->dev2orig = (int*)(b + o_perm);
-    h->scratch = (double*)(b + o_sc);
-    h->chain_row = (int64_t*)(h->scratch + kMaxTemps);
     h->dd.n = n;
     h->dd.q = q;
     h->dd.t0 = t[0];
@@ -463,12 +469,6 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_ha
     h->dd.s2_32 = (const float*)(b + o_sf);
     h->dd.dt32 = (const float*)(b + o_dtf);
     h->dd.inst = (const int*)(b + o_in);
-    e = cudaMemset(h->scratch, 0, 8 * (kMaxTemps + 4));
-    if (e != cudaSuccess) {
-        cudaFree(h->dbuf);
-        delete h;
-        return fail(EMP_E_CUDA, "cudaMemset failed: %s", cudaGetErrorString(e));
-    }
     *out = h;
     return EMP_OK;
 }
@@ -548,6 +548,12 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, dou
         CUDA_TRY(cudaGetLastError());
     }
     return EMP_OK;
+}
+
+int64_t emp_pt_work_bytes(int ntemps, int nwalkers, int ndim) {
+    (void)ndim;
+    if (ntemps < 1 || nwalkers < 1) return 0;
+    return (int64_t)work_bytes(ntemps, nwalkers);
 }
 
 int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream) {

@@ -269,6 +269,8 @@ class PTSampler:
         self.swaps_d = torch.zeros(T, **i32)
         self.units = torch.tensor(perm_units(W), **i32)
         self.n_rec = torch.zeros(2, dtype=torch.int64, device=dev)
+        wb = int(self.ctx.lib.emp_pt_work_bytes(T, W, D))
+        self.work = torch.zeros(wb, dtype=torch.uint8, device=dev)
         self.cap = 0
         self.chain = self.log_like_h = self.log_prob_h = None
         self.beta_h = self.tsw_h = self.smd_h = None
@@ -288,6 +290,7 @@ class PTSampler:
         st.a = self.a
         st.adapt_tau, st.adapt_nu, st.adapt_mode = self.adapt_tau, self.adapt_nu, self.adapt_mode
         st.precision = self.precision
+        st.work, st.work_bytes = _ptr(self.work), int(self.work.numel())
         return st
 
     def _record_struct(self) -> N.EmpPtRecord:

@@ -176,7 +176,13 @@ typedef struct emp_pt_state {
     double adapt_nu;              /* engine_config['adapt_nu'] */
     int32_t adapt_mode;           /* engine_config['adapt_mode'] (0 supported) */
     int32_t precision;            /* EMP_PREC_* used for every evaluation */
+    void* work;                   /* device workspace of emp_pt_work_bytes() bytes */
+    int64_t work_bytes;
 } emp_pt_state;
+
+/* Bytes of the workspace a PT state of this shape needs (swap log, per-sweep
+   rows, the ladder of the running sweep). */
+int64_t emp_pt_work_bytes(int ntemps, int nwalkers, int ndim);
 
 /* Per-sweep history buffers (device, caller-owned; any may be NULL).
    Replaces the PTHDFBackend datasets written at emp.py:722-770. */
