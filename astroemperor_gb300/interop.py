@@ -1,0 +1,73 @@
+"""Adapters from EMPEROR's own objects to this package.
+
+A maintainer who wires the GPU engine into EMPEROR hands it the reference's
+``Parameter_Block`` list (``self.model`` after ``update_model``,
+``emp.py:2391-2399``) and its ``my_data`` DataFrame (columns BJD, RV, eRV,
+Flag, already preprocessed by ``DataWrapper.get_data__``).  The blocks are
+read by attribute only (duck typing), so this module needs neither pandas
+nor the reference installed.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .data import RVData
+from .model import (AccelerationBlock, JitterBlock, KeplerianBlock, MOAVBlock, OffsetBlock,
+                    Parameter, ReddModel)
+
+
+def data_from_frame(df, labels=None, common_t=0.0) -> RVData:
+    """RVData from a table with BJD, RV, eRV, Flag columns (already referenced)."""
+    bjd = np.asarray(df['BJD'], dtype=np.float64)
+    order = np.argsort(bjd, kind='mergesort')
+    flag = np.asarray(df['Flag'], dtype=np.int64)[order]
+    nins = int(flag.max())
+    return RVData(BJD=bjd[order], RV=np.asarray(df['RV'], dtype=np.float64)[order],
+                  eRV=np.asarray(df['eRV'], dtype=np.float64)[order], Flag=flag,
+                  common_t=float(common_t),
+                  labels=list(labels) if labels else [f'INS{k + 1}' for k in range(nins)])
+
+
+def _copy_params(src_block, dst_block):
+    for ps, pd in zip(src_block, dst_block):
+        for attr in ('name', 'prior', 'limits', 'prargs', 'fixed', 'init_pos', 'is_hou'):
+            if hasattr(ps, attr):
+                setattr(pd, attr, getattr(ps, attr))
+        # the reference stores normalised prargs ([mu, s, logZ] / logZ) after
+        # refresh__; the compiler recomputes the normalisers from (mu, s)
+        if pd.prior == 'Normal' and pd.prargs is not None:
+            pd.prargs = list(pd.prargs)[:2]
+        elif pd.prior in ('Uniform', 'Jeffreys'):
+            pd.prargs = None
+    return dst_block
+
+
+def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False) -> ReddModel:
+    """ReddModel from the reference's block list (emp_model.py:32-170 objects)."""
+    out = []
+    for b in blocks:
+        t = b.type_
+        if t == 'Keplerian':
+            nb = KeplerianBlock(int(b.parameterisation), int(b.number_))
+            extra = []
+            for ap in getattr(b, 'additional_parameters', []):
+                p = Parameter(getattr(ap, 'name', 'extra'))
+                for attr in ('name', 'prior', 'limits', 'prargs', 'has_prior'):
+                    if hasattr(ap, attr):
+                        setattr(p, attr, getattr(ap, attr))
+                if p.prior == 'Normal' and p.prargs is not None:
+                    p.prargs = list(p.prargs)[:2]
+                extra.append(p)
+            nb.additional_parameters = extra
+        elif t == 'Offset':
+            nb = OffsetBlock(len(b))
+        elif t == 'Jitter':
+            nb = JitterBlock(len(b))
+        elif t == 'MOAV':
+            nb = MOAVBlock(int(b.number_), {'order': int(b.moav), 'global': bool(b.is_global)})
+        elif t == 'Acceleration':
+            nb = AccelerationBlock(len(b))
+        else:
+            raise ValueError(f'block type {t!r} is not on the GPU hot path')
+        out.append(_copy_params(b, nb))
+    return ReddModel(out, data, moav_reference_quirk=moav_reference_quirk)

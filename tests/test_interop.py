@@ -1,0 +1,46 @@
+"""Adapter from the reference's block objects (duck-typed stand-ins)."""
+from types import SimpleNamespace
+
+import numpy as np
+
+from astroemperor_gb300.interop import data_from_frame, model_from_blocks
+from oracle.rv import OracleRV, check_prargs
+from tests.golden.cases import model_51peg
+
+
+def _ref_like(block, normalise=True):
+    """A stand-in with the attributes of the reference's Parameter_Block after
+    refresh__ (prargs replaced by their normalised form, emp_model.py:82-98)."""
+    ps = []
+    for p in block:
+        pr = p.prargs
+        if normalise:
+            pr = check_prargs(p.prior, p.limits, p.prargs)
+        ps.append(SimpleNamespace(name=p.name, prior=p.prior, limits=list(p.limits), prargs=pr,
+                                  fixed=p.fixed, init_pos=list(p.init_pos), is_hou=p.is_hou))
+    extra = [SimpleNamespace(name=a.name, prior=a.prior, limits=list(a.limits),
+                             prargs=check_prargs(a.prior, a.limits, a.prargs), has_prior=a.has_prior)
+             for a in getattr(block, 'additional_parameters', [])]
+
+    class B(list):
+        pass
+    b = B(ps)
+    b.type_ = block.type_
+    b.parameterisation = block.parameterisation
+    b.number_ = block.number_
+    b.moav = block.moav
+    b.is_global = block.is_global
+    b.additional_parameters = extra
+    return b
+
+
+def test_model_from_reference_blocks(peg_arr):
+    m, d = model_51peg(peg_arr, k=1, par=1, moav={'order': 1, 'global': True})
+    frame = {'BJD': d.BJD, 'RV': d.RV, 'eRV': d.eRV, 'Flag': d.Flag}
+    d2 = data_from_frame(frame, common_t=d.common_t)
+    m2 = model_from_blocks([_ref_like(b) for b in m.blocks], d2)
+    a, b = m.descriptor(), m2.descriptor()
+    assert bytes(a) == bytes(b)
+    o = OracleRV(m2.spec(), d2.as_dict())
+    th = np.array([4.231, 55.957, 1.769, 0.087, 0.061, 3.642, 2.961, 0.1, 10.0])
+    assert np.isfinite(o.my_prior(th)) and np.isfinite(o.my_likelihood(th))
