@@ -97,6 +97,8 @@ SIGNATURES = {
                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     'emp_model_eval': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     'emp_pt_sweep': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord), C.c_void_p]),
+    'emp_pt_sweep_static': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord),
+                                      C.c_void_p]),
     'emp_pt_run': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord), C.c_int,
                              C.c_int, C.c_void_p]),
     'emp_pt_evaluate': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.c_void_p]),

@@ -576,6 +576,74 @@ int emp_pt_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec
     return enqueue_sweep(h, st, rec, (cudaStream_t)stream, nullptr);
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Sweep without any allocation by the caller or the library.
+//
+// Some callers cannot call cudaMalloc at all: code that runs while a larger
+// application graph is being captured (allocation is illegal inside stream
+// capture), and host programs whose device memory is one fixed arena handed
+// out by their own allocator.  emp_pt_sweep_static serves them: the sweep's
+// workspace (the swap log, the per-sweep rows, the ladder of the running
+// sweep) lives in the file-scope array below instead of a caller buffer.
+//
+// The array holds one PT state of up to kStaticMaxWalkers = ntemps*nwalkers
+// walkers (about 260 KB); every GPU that loads this library keeps it until
+// the process exits.  All calls share it and it keeps the last call's
+// contents, so each call first clears the part that must start at zero;
+// calls that overlap on the GPU (other streams, other threads) race on it.
+// ---------------------------------------------------------------------------
+static const int kStaticMaxWalkers = 32768;
+static const size_t kStaticHeaderBytes = 8 * (size_t)kMaxTemps + 16 + 4 * (size_t)kMaxTemps +
+                                         4 * (size_t)kMaxTemps + 16 + 16;
+static const size_t kStaticWorkBytes =
+    ((kStaticHeaderBytes + 8 * (size_t)kStaticMaxWalkers) + 255) & ~(size_t)255;
+static __device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
+
+static std::mutex g_static_mu;
+static void* g_static_ptr[64] = {};
+
+// device address of g_static_work on the current device; looked up once per
+// device (the host-side name of the array is not a device address)
+static int static_work_address(void** out) {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) return fail(EMP_E_INVALID, "device %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    if (!g_static_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_work);
+        if (e != cudaSuccess || p == nullptr)
+            return fail(EMP_E_CUDA, "cudaGetSymbolAddress(static workspace): %s", cudaGetErrorString(e));
+        g_static_ptr[dev] = p;
+    }
+    *out = g_static_ptr[dev];
+    return EMP_OK;
+}
+
+extern "C" int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec,
+                                   void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (!st) return fail(EMP_E_INVALID, "state is NULL");
+    const int64_t walkers = (int64_t)st->ntemps * st->nwalkers;
+    if (walkers > kStaticMaxWalkers)
+        return fail(EMP_E_SIZE, "ntemps*nwalkers=%lld exceeds the static workspace limit of %d walkers",
+                    (long long)walkers, kStaticMaxWalkers);
+    void* ws = nullptr;
+    int rc = static_work_address(&ws);
+    if (rc) return rc;
+    emp_pt_state local = *st;
+    local.work = ws;
+    local.work_bytes = (int64_t)kStaticWorkBytes;
+    if ((rc = check_state(h, &local))) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemsetAsync(ws, 0, kStaticHeaderBytes, s));
+    return enqueue_sweep(h, &local, rec, s, nullptr);
+}
+
+extern "C" {
+
 int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, int nsweeps,
                int use_graph, void* stream) {
     if (!h) return fail(EMP_E_INVALID, "handle is NULL");
