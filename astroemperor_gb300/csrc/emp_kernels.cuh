@@ -46,7 +46,7 @@ __device__ __forceinline__ bool in_support(double x, double lo, double hi) {
 // value of a prior term that varies with x (Normal, Beta); x in support
 __device__ __forceinline__ double prior_var_term(const emp_prior& p, double x) {
     if (p.kind == EMP_PRIOR_NORMAL) {
-        const double z = (x - p.a0) / p.a1;
+        const double z = (x - p.a0) * p.a1;                // a1 = 1/s
         return -0.5 * z * z - p.a2;
     }
     if (p.kind == EMP_PRIOR_BETA) return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
@@ -263,6 +263,137 @@ __device__ __forceinline__ bool metropolis(double nlp, double cur, double z, int
     return __dsub_rn(__dadd_rn(__dmul_rn((double)dm1, log(z)), nlp), cur) > log(u);
 }
 
+// ----------------------------------------------------------------------------
+// affine maps out = G u + x of the MA state (x: NQ, G: NQ x NQ row-major)
+// ----------------------------------------------------------------------------
+template <typename R, int NQ>
+__device__ __forceinline__ void map_identity(R* m) {
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        m[i] = R(0);
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) m[NQ + i * NQ + j] = (i == j) ? R(1) : R(0);
+    }
+}
+// a <- a o b  (b first, then a): (Ga Gb, Ga xb + xa)
+template <typename R, int NQ>
+__device__ __forceinline__ void map_compose(R* a, const R* b) {
+    R o[NQ + NQ * NQ];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        R v = a[i];
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) v += a[NQ + i * NQ + k] * b[k];
+        o[i] = v;
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) {
+            R g = R(0);
+#pragma unroll
+            for (int k = 0; k < NQ; ++k) g += a[NQ + i * NQ + k] * b[NQ + k * NQ + j];
+            o[NQ + i * NQ + j] = g;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NQ + NQ * NQ; ++k) a[k] = o[k];
+}
+// b <- a o b  (b first, then a)
+template <typename R, int NQ>
+__device__ __forceinline__ void map_compose_left(const R* a, R* b) {
+    R o[NQ + NQ * NQ];
+#pragma unroll
+    for (int k = 0; k < NQ + NQ * NQ; ++k) o[k] = a[k];
+    map_compose<R, NQ>(o, b);
+#pragma unroll
+    for (int k = 0; k < NQ + NQ * NQ; ++k) b[k] = o[k];
+}
+template <typename R, int NQ>
+__device__ __forceinline__ void map_apply(const R* m, const R* u, R* out) {
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        R v = m[i];
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) v += m[NQ + i * NQ + k] * u[k];
+        out[i] = v;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// lane accumulators and their group sums (FP64 plain; float-float mixed, so
+// that the mixed kernel's sums need no FP64 instruction until the end)
+// ----------------------------------------------------------------------------
+template <int PREC> struct LaneAcc;
+
+template <> struct LaneAcc<EMP_PREC_FP64> {
+    double v;
+    __device__ __forceinline__ void init() { v = 0.0; }
+    __device__ __forceinline__ void add(double x) { v += x; }
+    template <int L>
+    __device__ __forceinline__ double group_sum(double* red, int r) const {
+        constexpr int WL = L < 32 ? L : 32;
+        double s = v;
+#pragma unroll
+        for (int o = WL / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, WL);
+        if (L > 32) {
+            __syncthreads();
+            if ((r & 31) == 0) red[r >> 5] = s;
+            __syncthreads();
+            if (r == 0) {
+                double t = 0.0;
+                for (int w = 0; w < L / 32; ++w) t += red[w];
+                s = t;
+            }
+        }
+        return s;
+    }
+};
+
+// TwoSum of floats: s + e == a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+template <> struct LaneAcc<EMP_PREC_MIXED> {
+    float hi, lo;
+    __device__ __forceinline__ void init() { hi = 0.f; lo = 0.f; }
+    __device__ __forceinline__ void add(float x) {
+        float s, e;
+        two_sum(hi, x, s, e);
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    template <int L>
+    __device__ __forceinline__ double group_sum(double* red, int r) const {
+        constexpr int WL = L < 32 ? L : 32;
+        float h = hi, l = lo;
+#pragma unroll
+        for (int o = WL / 2; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, h, o, WL);
+            const float ol = __shfl_xor_sync(0xffffffffu, l, o, WL);
+            float s, e;
+            two_sum(h, oh, s, e);
+            h = s;
+            l = __fadd_rn(__fadd_rn(l, ol), e);
+        }
+        if (L > 32) {
+            float* rf = reinterpret_cast<float*>(red);
+            __syncthreads();
+            if ((r & 31) == 0) { rf[2 * (r >> 5)] = h; rf[2 * (r >> 5) + 1] = l; }
+            __syncthreads();
+            if (r == 0) {
+                for (int w = 1; w < L / 32; ++w) {
+                    float s, e;
+                    two_sum(h, rf[2 * w], s, e);
+                    h = s;
+                    l = __fadd_rn(__fadd_rn(l, rf[2 * w + 1]), e);
+                }
+            }
+        }
+        return (double)h + (double)l;
+    }
+};
+
 template <int PREC, int Q, int L, int NT>
 __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     using R = typename P<PREC>::R;
@@ -321,20 +452,26 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             const uint64_t it = (uint64_t)A.counters[0] + (uint64_t)A.step_in_sweep;
             U4 rr = rng_draw(A.seed, (uint32_t)(t_idx * A.W + j_idx), it,
                              kRngStretch0 + (uint32_t)A.half);
-            const int kk = (int)mulhi32(rr.z, (uint32_t)Wh);
-            const int k_idx = 2 * kk + (1 - A.half);
-            const int slot_k = A.members[t_idx * A.W + k_idx];
-            // emcee StretchMove.get_proposal: zz = ((a-1) u + 1)^2 / a
-            const double zz = __dadd_rn(__dmul_rn(A.a - 1.0, u53(rr.x, rr.y)), 1.0);
-            z = __dmul_rn(zz, zz) / A.a;
             uword = rr.w;
-            const double* sj = A.st_theta + (size_t)slot_j * n_free;
-            const double* ck = A.st_theta + (size_t)slot_k * n_free;
-            for (int d = r; d < n_free; d += L)
-                thp[d] = __dsub_rn(ck[d], __dmul_rn(__dsub_rn(ck[d], sj[d]), z));
+            // one warp per group forms z and the proposal (FP64, the
+            // reference's operation order); the others only wait
+            if (r < 32) {
+                const int kk = (int)mulhi32(rr.z, (uint32_t)Wh);
+                const int k_idx = 2 * kk + (1 - A.half);
+                const int slot_k = A.members[t_idx * A.W + k_idx];
+                // emcee StretchMove.get_proposal: zz = ((a-1) u + 1)^2 / a
+                const double zz = __dadd_rn(__dmul_rn(A.a - 1.0, u53(rr.x, rr.y)), 1.0);
+                z = __dmul_rn(zz, zz) / A.a;
+                if (r == 0) misc[2] = z;
+                const double* sj = A.st_theta + (size_t)slot_j * n_free;
+                const double* ck = A.st_theta + (size_t)slot_k * n_free;
+                for (int d = r; d < n_free; d += (L < 32 ? L : 32))
+                    thp[d] = __dsub_rn(ck[d], __dmul_rn(__dsub_rn(ck[d], sj[d]), z));
+            }
         }
     }
     __syncthreads();
+    if (A.mode == kModeStretch) z = misc[2];
     if (active) {
         for (int s = r; s < n_full; s += L) {
             const int src = md->full_src[s];
@@ -419,7 +556,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
         s_dt = reinterpret_cast<R*>(s_in + tile);
     }
 
-    double dsum = 0.0;                     // lane total, FP64
+    LaneAcc<PREC> acc;                     // lane total: FP64, or float-float
+    acc.init();
     R carry[NQ];
 #pragma unroll
     for (int m = 0; m < NQ; ++m) carry[m] = R(0);
@@ -571,68 +709,59 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                 }
             }
         }
-        double tile_part = (double)ks.s - (double)ks.c;
+        if (valid) {
+            acc.add((R)ks.s);
+            acc.add((R)(-ks.c));
+        }
 
         if (Q > 0) {
-            // join the lane chunks: inclusive scan of affine maps
-            // out = Gm u + xm over the group's lanes (Hillis-Steele, smem)
+            // join the lane chunks: inclusive scan of the affine maps
+            // out = G u + x of the group's lanes (warp shuffles; warp totals
+            // through shared memory when a group spans several warps)
             constexpr int MS = NQ + NQ * NQ;   // map size
-            R* buf0 = scan;
-            R* buf1 = scan + MS * L;
-            {
-                R* mp = buf0 + r * MS;
+            constexpr int WL = L < 32 ? L : 32;
+            const int lw = r & (WL - 1);
+            R mv[MS];
 #pragma unroll
-                for (int m = 0; m < NQ; ++m) {
-                    mp[m] = xh[m];
+            for (int m = 0; m < NQ; ++m) {
+                mv[m] = xh[m];
 #pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) mp[NQ + m * NQ + q2] = gh[m][q2];
-                }
+                for (int q2 = 0; q2 < NQ; ++q2) mv[NQ + m * NQ + q2] = gh[m][q2];
             }
-            __syncthreads();
-            R* src = buf0;
-            R* dst = buf1;
-            for (int off = 1; off < L; off <<= 1) {
-                R* o = dst + r * MS;
-                const R* a = src + r * MS;
-                if (r >= off) {
-                    const R* bq = src + (r - off) * MS;   // earlier prefix
-                    // (Ga, xa) o (Gb, xb) = (Ga Gb, Ga xb + xa)
 #pragma unroll
-                    for (int m = 0; m < NQ; ++m) {
-                        R v = a[m];
+            for (int off = 1; off < WL; off <<= 1) {
+                R pv[MS];
 #pragma unroll
-                        for (int q2 = 0; q2 < NQ; ++q2) v += a[NQ + m * NQ + q2] * bq[q2];
-                        o[m] = v;
+                for (int k = 0; k < MS; ++k) pv[k] = __shfl_up_sync(0xffffffffu, mv[k], off, WL);
+                if (lw >= off) map_compose<R, NQ>(mv, pv);
+            }
+            R ex[MS];
 #pragma unroll
-                        for (int q3 = 0; q3 < NQ; ++q3) {
-                            R gv = R(0);
+            for (int k = 0; k < MS; ++k) ex[k] = __shfl_up_sync(0xffffffffu, mv[k], 1, WL);
+            if (lw == 0) map_identity<R, NQ>(ex);
+            R wpre[MS], all[MS];
+            map_identity<R, NQ>(wpre);
+            if (L > 32) {
+                R* tot = scan;                                   // [L/32][MS]
+                if (lw == WL - 1) {
 #pragma unroll
-                            for (int q2 = 0; q2 < NQ; ++q2) gv += a[NQ + m * NQ + q2] * bq[NQ + q2 * NQ + q3];
-                            o[NQ + m * NQ + q3] = gv;
-                        }
-                    }
-                } else {
-#pragma unroll
-                    for (int m = 0; m < MS; ++m) o[m] = a[m];
+                    for (int k = 0; k < MS; ++k) tot[(r >> 5) * MS + k] = mv[k];
                 }
                 __syncthreads();
-                R* tmp = src; src = dst; dst = tmp;
-            }
-            // incoming state of this lane = prefix(r-1) applied to carry
-            R u[NQ];
-            if (r == 0) {
+                const int w = r >> 5;
+                for (int k = 0; k < w; ++k) map_compose_left<R, NQ>(tot + k * MS, wpre);
 #pragma unroll
-                for (int m = 0; m < NQ; ++m) u[m] = carry[m];
+                for (int k = 0; k < MS; ++k) all[k] = wpre[k];
+                for (int k = w; k < L / 32; ++k) map_compose_left<R, NQ>(tot + k * MS, all);
             } else {
-                const R* pm = src + (r - 1) * MS;
 #pragma unroll
-                for (int m = 0; m < NQ; ++m) {
-                    R v = pm[m];
-#pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) v += pm[NQ + m * NQ + q2] * carry[q2];
-                    u[m] = v;
-                }
+                for (int k = 0; k < MS; ++k) all[k] = __shfl_sync(0xffffffffu, mv[k], WL - 1, WL);
             }
+            // incoming state of this lane: its exclusive prefix after the
+            // earlier warps, applied to the tile's incoming state
+            R cw[NQ], u[NQ];
+            map_apply<R, NQ>(wpre, carry, cw);
+            map_apply<R, NQ>(ex, cw, u);
             R extra = R(0);
 #pragma unroll
             for (int q2 = 0; q2 < NQ; ++q2) {
@@ -640,41 +769,17 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
 #pragma unroll
                 for (int q3 = 0; q3 < NQ; ++q3) extra += u[q2] * u[q3] * S2[q2][q3];
             }
-            tile_part += (double)extra;
-            // carry for the next tile = full prefix applied to carry
-            {
-                const R* pm = src + (L - 1) * MS;
-                R nc[NQ];
+            if (valid) acc.add(extra);
+            R nc[NQ];
+            map_apply<R, NQ>(all, carry, nc);
 #pragma unroll
-                for (int m = 0; m < NQ; ++m) {
-                    R v = pm[m];
-#pragma unroll
-                    for (int q2 = 0; q2 < NQ; ++q2) v += pm[NQ + m * NQ + q2] * carry[q2];
-                    nc[m] = v;
-                }
-#pragma unroll
-                for (int m = 0; m < NQ; ++m) carry[m] = nc[m];
-            }
+            for (int m = 0; m < NQ; ++m) carry[m] = nc[m];
         }
-        if (valid) dsum += tile_part;
     }
 
     // ---------------- group reduction ------------------------------------
-    double v = dsum;
-    constexpr int WL = L < 32 ? L : 32;
-#pragma unroll
-    for (int o = WL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o, WL);
-    if (L > 32) {
-        __syncthreads();
-        if ((r & 31) == 0) red[r >> 5] = v;
-        __syncthreads();
-        if (r == 0) {
-            double s = 0.0;
-            for (int w = 0; w < L / 32; ++w) s += red[w];
-            v = s;
-        }
-    }
-    const double logl = valid ? (-0.5 * v + md->loglike_const) : -INFINITY;
+    const double v = acc.template group_sum<L>(red, r);
+    const double logl = (valid && r == 0) ? (-0.5 * v + md->loglike_const) : -INFINITY;
 
     // ---------------- epilogue --------------------------------------------
     if (A.mode == kModeLogpost) {

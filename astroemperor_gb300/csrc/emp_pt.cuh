@@ -79,8 +79,9 @@ struct SwapArgs {
 // FP64 test (the FP32 log of a 32-bit uniform is within 2e-5 of the FP64 one)
 __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
     const float lf = __logf((float)u32u(word));
-    const double d = x - (double)lf;
-    const double guard = 1e-4 * (1.0 + fabs((double)lf));
+    const float xf = (float)x;
+    const float d = xf - lf;
+    const float guard = 1e-4f * (1.f + fabsf(lf)) + 1e-6f * fabsf(xf);
     if (d > guard) return true;
     if (d < -guard) return false;
     return log(u32u(word)) < x;

@@ -102,7 +102,7 @@ int validate_prior(const emp_prior& p, const char* what, int i) {
     if (p.kind == EMP_PRIOR_NONE) return EMP_OK;
     if (!(p.lo <= p.hi)) return fail(EMP_E_INVALID, "%s %d: limits not ordered", what, i);
     if (p.kind == EMP_PRIOR_NORMAL && !(p.a1 > 0))
-        return fail(EMP_E_INVALID, "%s %d: Normal scale must be > 0", what, i);
+        return fail(EMP_E_INVALID, "%s %d: Normal 1/scale must be > 0", what, i);
     return EMP_OK;
 }
 

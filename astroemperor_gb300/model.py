@@ -303,7 +303,7 @@ def prior_struct(prior: str, limits, prargs) -> N.EmpPrior:
         mu, s = float(prargs[0]), float(prargs[1])
         a, b = (low - mu) / s, (high - mu) / s
         logZ = float(np.log(ndtr(b) - ndtr(a)))
-        p.a0, p.a1 = mu, s
+        p.a0, p.a1 = mu, 1.0 / s          # the device multiplies by 1/s
         p.a2 = float(np.log(s * np.sqrt(2 * np.pi))) + logZ
     elif prior == 'Beta':
         a, b = float(prargs[0]), float(prargs[1])

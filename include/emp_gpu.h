@@ -60,7 +60,7 @@ typedef struct emp_prior {
     int32_t _pad;
     double lo, hi;        /* support, inclusive (the reference's `limits`) */
     double a0, a1, a2;    /* Uniform/Jeffreys: a0 = ln(1/(hi-lo))
-                             Normal: a0 = mu, a1 = s, a2 = ln(s sqrt(2 pi)) + logZ
+                             Normal: a0 = mu, a1 = 1/s, a2 = ln(s sqrt(2 pi)) + logZ
                              Beta:   a0 = a, a1 = b, a2 = ln B(a, b) */
 } emp_prior;
 

@@ -46,7 +46,7 @@ def test_descriptor_layout(peg_arr):
     assert md.derived[0][1].kind == N.EMP_PRIOR_NONE
     assert md.loglike_const == -0.5 * np.log(2 * np.pi) * 256
     p = md.prior[6]                                          # jitter Normal(5,5)
-    assert p.kind == N.PRIOR_KIND['Normal'] and p.a0 == 5 and p.a1 == 5
+    assert p.kind == N.PRIOR_KIND["Normal"] and p.a0 == 5 and p.a1 == 0.2
     th = np.arange(7.0)
     ft = full_theta(m, th)[0]
     assert list(ft) == [0, 1, 2, 0, 0, 3, 4, 5, 6]
@@ -69,7 +69,7 @@ def test_prior_structs_reproduce_oracle_prior(peg_arr):
                 lp = -np.inf
                 break
             if p.kind == 1:
-                lp += -0.5 * ((x - p.a0) / p.a1) ** 2 - p.a2
+                lp += -0.5 * ((x - p.a0) * p.a1) ** 2 - p.a2
             else:
                 lp += p.a0
         assert lp == pytest.approx(o.my_prior(th), rel=1e-13, abs=1e-13)
