@@ -225,7 +225,7 @@ class PTSampler:
     def __init__(self, nwalkers, ndim, model: ReddModel, ntemps=5, pool=None, backend=None,
                  betas=None, tsw_history=True, smd_history=True, adapt_tau=1000, adapt_nu=1,
                  adapt_mode=0, precision='mixed', seed=None, a=2.0, device='cuda:0',
-                 use_graph=True, moves=None, context: Optional[Context] = None):
+                 use_graph=True, moves=None, context: Optional[Context] = None, autotune=True):
         if model.ndim__ != ndim:
             raise ValueError(f'ndim={ndim} but the model has {model.ndim__} free parameters')
         if nwalkers % 2:
@@ -247,6 +247,8 @@ class PTSampler:
         self.precision = PRECISIONS[precision]
         self.a = float(a)
         self.use_graph = bool(use_graph)
+        self.autotune = bool(autotune)
+        self.launch = None                 # (lanes per walker, tile, ms) chosen by the autotuner
         if seed is None:
             seed = int(np.random.randint(0, 2 ** 62))
         self.seed = int(seed)
@@ -343,6 +345,11 @@ class PTSampler:
             p0 = initial_state.coords if isinstance(initial_state, PTState) else initial_state
             self.set_positions(p0)
         nsweeps = int(nsweeps)
+        if self.autotune and self.launch is None:
+            from .autotune import autotune
+            self.stream.synchronize()
+            half = self.theta[: self.ntemps * (self.nwalkers // 2)]
+            self.launch = autotune(self.ctx, half, self.precision)
         self._grow(nsweeps)
         st = self._state_struct(nsteps)
         rec = self._record_struct()

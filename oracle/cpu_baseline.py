@@ -65,6 +65,28 @@ def time_pool(spec, data, thetas, ncores=None, min_seconds=10.0, max_seconds=30.
     return n / el, n, el, ncores
 
 
+class PoolTimer:
+    """A reference-faithful pool kept open across timed steps."""
+
+    def __init__(self, spec, data, ncores=None):
+        self.ncores = int(ncores or os.cpu_count() or 1)
+        ctx = mp.get_context('spawn')
+        self.pool = ctx.Pool(self.ncores, initializer=_init, initargs=(faithful_spec(spec), data))
+
+    def warm(self, thetas):
+        self.pool.map(_eval, list(thetas[:self.ncores]), chunksize=1)
+
+    def step(self, thetas):
+        """Seconds to evaluate ``thetas`` one walker per task."""
+        t0 = time.perf_counter()
+        self.pool.map(_eval, list(thetas), chunksize=1)
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+
 def time_single(spec, data, thetas, min_seconds=2.0):
     """Single-process evals/s (no pool)."""
     o = rv.OracleRV(faithful_spec(spec), data)
