@@ -1,0 +1,657 @@
+// emp_grad.cuh -- adjoint kernel: d logL / d theta and d logprior / d theta.
+//
+// The reference has no gradient; this is the reverse mode of its
+// my_likelihood (support/likelihoods/00.like:3-5) through my_model
+// (emp_model.py:706-781) for Keplerian parameterisations 0 and 1 (kep00/
+// kep01.model), acceleration, offsets, jitters and the moving average
+// (moav01 recurrence, globally or per instrument).
+//
+// One walker per group of L lanes; the whole series is staged once per CTA
+// (lane-chunk layout as in k_logpost) and each group keeps its residuals r
+// and adjoints lambda = dL/dr in shared memory.  Passes:
+//   1. forward (FP32 Kepler solves, 4 epochs in flight): b = y - model;
+//   2. MA join: scan of affine maps across lanes -> incoming state; cheap
+//      forward re-run gives r and logL;
+//   3. backward map: each lane's chunk of the recurrence
+//      lambda_i = -w_i r_i - sum_c a_{c,i+1+c} lambda_{i+1+c}
+//      as an affine function of its incoming state, reverse scan across lanes;
+//   4. backward: lambda, gradients of offsets, jitters, MA coefficients and
+//      timescales (per-instrument accumulators in registers, <= 4 instruments);
+//   5. per planet: E recomputed (not stored), dE/dM = 1/(1 - e cos E) and
+//      dE/de = sin E/(1 - e cos E) by the implicit function theorem, and the
+//      five parameter derivatives accumulated against -lambda.
+// Sums are float-float across lanes and finished in FP64.
+#pragma once
+#include "emp_kernels.cuh"
+
+namespace emp {
+
+constexpr int kGradMaxIns = 4;
+constexpr int kGradPC = 16;   // floats per planet
+
+struct GArgs {
+    const emp_model_desc* md;
+    DevData d;
+    int nwalk;
+    const double* theta;      // [B][n_free]
+    double* logl;             // [B]
+    double* logprior;         // [B]
+    double* grad_logl;        // [B][n_free]
+    double* grad_logprior;    // [B][n_free]
+};
+
+struct GSmem {
+    int tile_bytes, group_bytes, total;
+    int off_full, off_pc, off_ins, off_acc, off_red, off_scan, off_pterm, off_gfull, off_misc, off_r, off_l;
+    __host__ __device__ void build(int q, int L, int G, int n, int n_full, int n_free, int n_planets,
+                                   int n_ins, int acc_order) {
+        const int C = (n + L - 1) / L;
+        const int slots = C * L;
+        tile_bytes = Smem::align16((4 * 4 + 4 + 4 * q) * slots + 64);
+        int o = 0;
+        off_full = o;  o += Smem::align16(8 * n_full);
+        off_pc = o;    o += Smem::align16(4 * kGradPC * (n_planets > 0 ? n_planets : 1));
+        off_ins = o;   o += Smem::align16(4 * (2 + 2 * kMaxQ) * (n_ins > 0 ? n_ins : 1));
+        off_acc = o;   o += Smem::align16(8 * (acc_order > 0 ? acc_order : 1));
+        off_red = o;   o += Smem::align16(8 * 4 * ((L + 31) / 32));
+        off_scan = o;  o += Smem::align16(4 * (kMaxQ + kMaxQ * kMaxQ) * ((L + 31) / 32));
+        off_pterm = o; o += Smem::align16(8 * (n_free + 2 * n_planets + 1));
+        off_gfull = o; o += Smem::align16(8 * n_full);
+        off_misc = o;  o += 64;
+        off_r = o;     o += Smem::align16(4 * slots);
+        off_l = o;     o += Smem::align16(4 * slots);
+        group_bytes = Smem::align16(o);
+        total = tile_bytes + G * group_bytes;
+    }
+};
+
+// gradient of a prior term (Normal, Beta; constant priors give 0)
+__device__ __forceinline__ double prior_var_grad(const emp_prior& p, double x) {
+    if (p.kind == EMP_PRIOR_NORMAL) return -(x - p.a0) * p.a1 * p.a1;
+    if (p.kind == EMP_PRIOR_BETA) return (p.a0 - 1.0) / x - (p.a1 - 1.0) / (1.0 - x);
+    return 0.0;
+}
+
+// planet constants for the adjoint: [0..3] phase as in planet_consts_mixed,
+// [4]=e [5]=cw [6]=sw [7]=K [8]=q=sqrt(1-e^2) [9]=S or 0 [10]=C or 0
+// [11]=1/e^1.5 (0 below the omega threshold) [12]=parameterisation
+__device__ __forceinline__ void planet_grad_consts(int par, const double* v, float* pc) {
+    float tmp[8];
+    planet_consts_mixed(par, v, tmp);
+    pc[0] = tmp[0]; pc[1] = tmp[1]; pc[2] = tmp[2]; pc[3] = tmp[3];
+    const float e = tmp[4];
+    float K, cw, sw;
+    if (par == 0) {
+        K = (float)v[1];
+        sincosf((float)v[4], &sw, &cw);
+        pc[9] = 0.f; pc[10] = 0.f; pc[11] = 0.f;
+    } else {   // 1
+        K = (float)v[1];
+        const double ed = v[3] * v[3] + v[4] * v[4];
+        if (ed < 1e-6) { cw = 1.f; sw = 0.f; pc[11] = 0.f; }
+        else {
+            const float rs = rsqrtf(e);
+            cw = (float)v[4] * rs;
+            sw = (float)v[3] * rs;
+            pc[11] = rs * rs * rs;
+        }
+        pc[9] = (float)v[3];
+        pc[10] = (float)v[4];
+    }
+    pc[4] = e; pc[5] = cw; pc[6] = sw; pc[7] = K;
+    pc[8] = sqrtf((1.f - e) * (1.f + e));
+    pc[12] = (float)par;
+}
+
+template <int Q, int L, int NT>
+__global__ void __launch_bounds__(NT) k_grad(GArgs A) {
+    constexpr int G = NT / L;
+    constexpr int NQ = Q > 0 ? Q : 1;
+    constexpr int NE = 4;
+    constexpr int INSW = 2 + 2 * kMaxQ;
+    constexpr int KI = kGradMaxIns;
+    extern __shared__ __align__(16) unsigned char smem[];
+    using R = float;
+
+    const emp_model_desc* md = A.md;
+    const int n_full = md->n_full, n_free = md->n_free, n_planets = md->n_planets;
+    const int n_ins = md->n_ins, acc_order = md->acc_order;
+    const int n = A.d.n;
+    GSmem lay;
+    lay.build(Q, L, G, n, n_full, n_free, n_planets, n_ins, acc_order);
+
+    const int tid = threadIdx.x;
+    const int g = tid / L;
+    const int r = tid - g * L;
+    const int wk = blockIdx.x * G + g;
+    const bool active = wk < A.nwalk;
+    unsigned char* gs = smem + lay.tile_bytes + g * lay.group_bytes;
+    double* full = reinterpret_cast<double*>(gs + lay.off_full);
+    float* pcs = reinterpret_cast<float*>(gs + lay.off_pc);
+    float* insc = reinterpret_cast<float*>(gs + lay.off_ins);
+    double* accc = reinterpret_cast<double*>(gs + lay.off_acc);
+    double* red = reinterpret_cast<double*>(gs + lay.off_red);
+    float* scan = reinterpret_cast<float*>(gs + lay.off_scan);
+    double* pterm = reinterpret_cast<double*>(gs + lay.off_pterm);
+    double* gfull = reinterpret_cast<double*>(gs + lay.off_gfull);
+    double* misc = reinterpret_cast<double*>(gs + lay.off_misc);
+    int* flag = reinterpret_cast<int*>(misc + 4);
+    float* rb = reinterpret_cast<float*>(gs + lay.off_r);
+    float* lb = reinterpret_cast<float*>(gs + lay.off_l);
+
+    // ---------------- theta, prior and its gradient, constants -------------
+    if (active) {
+        if (r == 0) flag[0] = 0;
+        for (int s = r; s < n_full; s += L) {
+            const int src = md->full_src[s];
+            full[s] = src >= 0 ? A.theta[(size_t)wk * n_free + src] : md->full_fixed[s];
+            gfull[s] = 0.0;
+        }
+    }
+    __syncthreads();
+    if (active) {
+        for (int d = r; d < n_free; d += L) {
+            const emp_prior& p = md->prior[d];
+            const double x = full[md->prior_slot[d]];
+            double gp = 0.0;
+            if (!in_support(x, p.lo, p.hi)) flag[0] = 1;
+            else if (p.kind == EMP_PRIOR_NORMAL || p.kind == EMP_PRIOR_BETA) {
+                pterm[d] = prior_var_term(p, x);
+                gp = prior_var_grad(p, x);
+            }
+            A.grad_logprior[(size_t)wk * n_free + d] = gp;
+        }
+        for (int p = r; p < n_planets; p += L)
+            planet_grad_consts(md->kep_param[p], full + md->kep_slot[p], pcs + p * kGradPC);
+        for (int k = r; k < n_ins; k += L) {
+            float* ic = insc + k * INSW;
+            ic[0] = (float)(md->offset_slot >= 0 ? full[md->offset_slot + k] : 0.0);
+            ic[1] = (float)(md->jitter_slot >= 0 ? full[md->jitter_slot + k] : 0.0);   // J itself
+#pragma unroll
+            for (int c = 0; c < Q; ++c) {
+                const int base = md->ma_global ? md->ma_slot + 2 * c : md->ma_slot + 2 * Q * k + 2 * c;
+                ic[2 + 2 * c] = (float)full[base];
+                ic[3 + 2 * c] = (float)full[base + 1];               // tau itself
+            }
+        }
+        for (int j = r; j < acc_order; j += L) accc[j] = full[md->acc_slot + j];
+    }
+    __syncthreads();
+    if (active) {
+        // derived priors (value and gradient through th[3], th[4] or th[1], th[2])
+        for (int q2 = r; q2 < 2 * n_planets; q2 += L) {
+            const int p = q2 >> 1, k = q2 & 1;
+            const emp_prior& dp = md->derived[p][k];
+            if (dp.kind == EMP_PRIOR_NONE) continue;
+            const double* th = full + md->kep_slot[p];
+            const double x = derived_x(th, k);
+            if (!in_support(x, dp.lo, dp.hi)) { flag[0] = 1; continue; }
+            if (dp.kind == EMP_PRIOR_NORMAL || dp.kind == EMP_PRIOR_BETA) {
+                pterm[n_free + q2] = prior_var_term(dp, x);
+                const double gx = prior_var_grad(dp, x);
+                const int i0 = k == 0 ? 3 : 1;
+                // scatter into the free slots of the two components
+                for (int m = 0; m < 2; ++m) {
+                    const int slot = md->kep_slot[p] + i0 + m;
+                    const int src = md->full_src[slot];
+                    if (src >= 0) atomicAdd(&A.grad_logprior[(size_t)wk * n_free + src], gx * 2.0 * th[i0 + m]);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (active && r == 0) {
+        double lp = -INFINITY;
+        if (flag[0] == 0) {
+            lp = md->prior_const;
+            for (int i = 0; i < md->n_prior_var; ++i) lp += pterm[md->prior_var[i]];
+        }
+        misc[0] = lp;
+    }
+    __syncthreads();
+    const double lp = active ? misc[0] : -INFINITY;
+    const bool valid = active && lp > -INFINITY;
+
+    // ---------------- stage the whole series --------------------------------
+    const int C = (n + L - 1) / L;
+    const int slots = C * L;
+    float* s_th = reinterpret_cast<float*>(smem);
+    float* s_tl = s_th + slots;
+    float* s_y = s_tl + slots;
+    float* s_s2 = s_y + slots;
+    int* s_in = reinterpret_cast<int*>(s_s2 + slots);
+    float* s_dt = reinterpret_cast<float*>(s_in + slots);
+    for (int idx = tid; idx < n; idx += NT) {
+        const int rr = idx / C;
+        const int kk = idx - rr * C;
+        const int pos = kk * L + ((rr + kk) & (L - 1));
+        s_th[pos] = A.d.t_hi[idx];
+        s_tl[pos] = A.d.t_lo[idx];
+        s_y[pos] = A.d.y32[idx];
+        s_s2[pos] = A.d.s2_32[idx];
+        s_in[pos] = A.d.inst[idx];
+#pragma unroll
+        for (int c = 0; c < Q; ++c) s_dt[c * slots + pos] = A.d.dt32[(size_t)c * n + idx];
+    }
+    __syncthreads();
+    const int nr = max(0, min(C, n - r * C));
+    auto posof = [&](int rr, int kk) { return kk * L + ((rr + kk) & (L - 1)); };
+    // MA coefficient a_{c,i} and its exp factor at a lane-chunk position
+    auto ma_coef = [&](int ps, int c, float& ef) -> float {
+        const float* ic = insc + s_in[ps] * INSW;
+        const float dt = s_dt[c * slots + ps];
+        ef = dt < INFINITY ? __expf(-dt / ic[3 + 2 * c]) : 0.f;
+        return ic[2 + 2 * c] * ef;
+    };
+
+    // ---------------- pass 1: mean model, b = y - model ---------------------
+    R xh[NQ], gh[NQ][NQ];
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) {
+        xh[m] = 0.f;
+#pragma unroll
+        for (int q2 = 0; q2 < NQ; ++q2) gh[m][q2] = m == q2 ? 1.f : 0.f;
+    }
+    if (valid) {
+        for (int k0 = 0; k0 < nr; k0 += NE) {
+            int pos[NE];
+            bool ok[NE];
+            float th[NE], tl[NE], model[NE];
+#pragma unroll
+            for (int e = 0; e < NE; ++e) {
+                const int kk = k0 + e < nr ? k0 + e : nr - 1;
+                ok[e] = k0 + e < nr;
+                pos[e] = posof(r, kk);
+                th[e] = s_th[pos[e]];
+                tl[e] = s_tl[pos[e]];
+                model[e] = 0.f;
+            }
+            for (int p = 0; p < n_planets; ++p) {
+                const float* pc = pcs + p * kGradPC;
+                float M[NE], sn[NE], cs[NE];
+#pragma unroll
+                for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e]);
+                kepler_f32_n<NE>(M, pc[4], sn, cs);
+#pragma unroll
+                for (int e = 0; e < NE; ++e) {
+                    const float ec = pc[4], D = 1.f - ec * cs[e];
+                    const float Nn = (cs[e] - ec) * pc[5] - pc[8] * sn[e] * pc[6];
+                    model[e] += pc[7] * (Nn / D + ec * pc[5]);
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < NE; ++e) {
+                if (!ok[e]) continue;
+                float mdl = model[e];
+                if (acc_order > 0) {
+                    const float x = (th[e] - (float)A.d.t0) + tl[e];
+                    float pv = 0.f;
+                    for (int j = 0; j < acc_order; ++j) pv = pv * x + (float)accc[j];
+                    mdl += pv * x;
+                }
+                const int ps = pos[e];
+                mdl += insc[s_in[ps] * INSW];
+                const float b = s_y[ps] - mdl;
+                rb[ps] = b;
+                if (Q > 0) {
+                    R x = b, gn[NQ];
+#pragma unroll
+                    for (int q2 = 0; q2 < NQ; ++q2) gn[q2] = 0.f;
+#pragma unroll
+                    for (int c = 0; c < Q; ++c) {
+                        float ef;
+                        const float a = ma_coef(ps, c, ef);
+                        x -= a * xh[c];
+#pragma unroll
+                        for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
+                    }
+#pragma unroll
+                    for (int m = NQ - 1; m > 0; --m) {
+                        xh[m] = xh[m - 1];
+#pragma unroll
+                        for (int q2 = 0; q2 < NQ; ++q2) gh[m][q2] = gh[m - 1][q2];
+                    }
+                    xh[0] = x;
+#pragma unroll
+                    for (int q2 = 0; q2 < NQ; ++q2) gh[0][q2] = gn[q2];
+                }
+            }
+        }
+    }
+
+    // ---------------- pass 2: MA join, r and logL ---------------------------
+    constexpr int MS = NQ + NQ * NQ;
+    constexpr int WL = L < 32 ? L : 32;
+    const int lw = r & (WL - 1);
+    R u[NQ];
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) u[m] = 0.f;
+    if (Q > 0) {
+        R mv[MS];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) {
+            mv[m] = xh[m];
+#pragma unroll
+            for (int q2 = 0; q2 < NQ; ++q2) mv[NQ + m * NQ + q2] = gh[m][q2];
+        }
+#pragma unroll
+        for (int off = 1; off < WL; off <<= 1) {
+            R pv[MS];
+#pragma unroll
+            for (int k = 0; k < MS; ++k) pv[k] = __shfl_up_sync(0xffffffffu, mv[k], off, WL);
+            if (lw >= off) map_compose<R, NQ>(mv, pv);
+        }
+        R ex[MS];
+#pragma unroll
+        for (int k = 0; k < MS; ++k) ex[k] = __shfl_up_sync(0xffffffffu, mv[k], 1, WL);
+        if (lw == 0) map_identity<R, NQ>(ex);
+        R wpre[MS];
+        map_identity<R, NQ>(wpre);
+        if (L > 32) {
+            if (lw == WL - 1) {
+#pragma unroll
+                for (int k = 0; k < MS; ++k) scan[(r >> 5) * MS + k] = mv[k];
+            }
+            __syncthreads();
+            for (int k = 0; k < (r >> 5); ++k) map_compose_left<R, NQ>(scan + k * MS, wpre);
+            __syncthreads();
+        }
+        R zero[NQ], cw_[NQ];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) zero[m] = 0.f;
+        map_apply<R, NQ>(wpre, zero, cw_);
+        map_apply<R, NQ>(ex, cw_, u);
+    }
+    LaneAcc<EMP_PREC_MIXED> lacc;
+    lacc.init();
+    if (valid) {
+        R hist[NQ];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) hist[m] = u[m];
+        for (int kk = 0; kk < nr; ++kk) {
+            const int ps = posof(r, kk);
+            float x = rb[ps];
+            if (Q > 0) {
+#pragma unroll
+                for (int c = 0; c < Q; ++c) {
+                    float ef;
+                    x -= ma_coef(ps, c, ef) * hist[c];
+                }
+#pragma unroll
+                for (int m = NQ - 1; m > 0; --m) hist[m] = hist[m - 1];
+                hist[0] = x;
+            }
+            rb[ps] = x;
+            const float J = insc[s_in[ps] * INSW + 1];
+            const float err2 = s_s2[ps] + J * J;
+            const float w = __frcp_rn(err2);
+            lacc.add(x * x * w + __log2f(err2) * 0.69314718055994531f);
+        }
+    }
+    const double sumL = lacc.group_sum<L>(red, r);
+    __syncthreads();
+
+    // ---------------- pass 3: backward map, reverse scan -------------------
+    R v[NQ];
+#pragma unroll
+    for (int m = 0; m < NQ; ++m) v[m] = 0.f;
+    // lambda_i = -w_i r_i - sum_c a_{c,i+1+c} lambda_{i+1+c}; state at chunk
+    // end = (lambda_e, ..., lambda_{e+Q-1}); a of epochs past n is 0
+    auto a_after = [&](int kk_abs_next, int c, float& ef) -> float {
+        // epoch (r, kk) + 1 + c in series order: lane-chunk index arithmetic
+        const int idx = r * C + kk_abs_next;
+        if (idx >= n) { ef = 0.f; return 0.f; }
+        const int rr = idx / C, k2 = idx - rr * C;
+        return ma_coef(posof(rr, k2), c, ef);
+    };
+    if (Q > 0) {
+        R lh[NQ], hh[NQ][NQ];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) {
+            lh[m] = 0.f;
+#pragma unroll
+            for (int q2 = 0; q2 < NQ; ++q2) hh[m][q2] = m == q2 ? 1.f : 0.f;
+        }
+        if (valid) {
+            for (int kk = nr - 1; kk >= 0; --kk) {
+                const int ps = posof(r, kk);
+                const float J = insc[s_in[ps] * INSW + 1];
+                const float w = __frcp_rn(s_s2[ps] + J * J);
+                float lam = -w * rb[ps];
+                float hn[NQ];
+#pragma unroll
+                for (int q2 = 0; q2 < NQ; ++q2) hn[q2] = 0.f;
+#pragma unroll
+                for (int c = 0; c < Q; ++c) {
+                    float ef;
+                    const float a = a_after(kk + 1 + c, c, ef);
+                    lam -= a * lh[c];
+#pragma unroll
+                    for (int q2 = 0; q2 < NQ; ++q2) hn[q2] -= a * hh[c][q2];
+                }
+#pragma unroll
+                for (int m = NQ - 1; m > 0; --m) {
+                    lh[m] = lh[m - 1];
+#pragma unroll
+                    for (int q2 = 0; q2 < NQ; ++q2) hh[m][q2] = hh[m - 1][q2];
+                }
+                lh[0] = lam;
+#pragma unroll
+                for (int q2 = 0; q2 < NQ; ++q2) hh[0][q2] = hn[q2];
+            }
+        }
+        R mv[MS];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) {
+            mv[m] = lh[m];
+#pragma unroll
+            for (int q2 = 0; q2 < NQ; ++q2) mv[NQ + m * NQ + q2] = hh[m][q2];
+        }
+        // inclusive suffix scan: S_r = map_r o S_{r+1}
+#pragma unroll
+        for (int off = 1; off < WL; off <<= 1) {
+            R pv[MS];
+#pragma unroll
+            for (int k = 0; k < MS; ++k) pv[k] = __shfl_down_sync(0xffffffffu, mv[k], off, WL);
+            if (lw + off < WL) map_compose<R, NQ>(mv, pv);
+        }
+        R ex[MS];
+#pragma unroll
+        for (int k = 0; k < MS; ++k) ex[k] = __shfl_down_sync(0xffffffffu, mv[k], 1, WL);
+        if (lw == WL - 1) map_identity<R, NQ>(ex);
+        R wsuf[MS];
+        map_identity<R, NQ>(wsuf);
+        if (L > 32) {
+            if (lw == 0) {
+#pragma unroll
+                for (int k = 0; k < MS; ++k) scan[(r >> 5) * MS + k] = mv[k];
+            }
+            __syncthreads();
+            for (int k = L / 32 - 1; k > (r >> 5); --k) map_compose_left<R, NQ>(scan + k * MS, wsuf);
+            __syncthreads();
+        }
+        R zero[NQ], cw_[NQ];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) zero[m] = 0.f;
+        map_apply<R, NQ>(wsuf, zero, cw_);
+        map_apply<R, NQ>(ex, cw_, v);
+    }
+
+    // ---------------- pass 4: lambda, noise-model gradients ---------------
+    float g_off[KI], g_jit[KI], g_phi[KI][NQ], g_tau[KI][NQ];
+#pragma unroll
+    for (int k = 0; k < KI; ++k) {
+        g_off[k] = 0.f; g_jit[k] = 0.f;
+#pragma unroll
+        for (int c = 0; c < NQ; ++c) { g_phi[k][c] = 0.f; g_tau[k][c] = 0.f; }
+    }
+    if (valid) {
+        float st[NQ];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) st[m] = v[m];
+        for (int kk = nr - 1; kk >= 0; --kk) {
+            const int ps = posof(r, kk);
+            const int ki = s_in[ps];
+            const float* ic = insc + ki * INSW;
+            const float J = ic[1];
+            const float w = __frcp_rn(s_s2[ps] + J * J);
+            const float ri = rb[ps];
+            float lam = -w * ri;
+            if (Q > 0) {
+#pragma unroll
+                for (int c = 0; c < Q; ++c) {
+                    float ef;
+                    lam -= a_after(kk + 1 + c, c, ef) * st[c];
+                }
+            }
+            lb[ps] = lam;
+            const float gj = (w * w * ri * ri - w) * J;
+            float gp[NQ], gt[NQ];
+#pragma unroll
+            for (int c = 0; c < NQ; ++c) { gp[c] = 0.f; gt[c] = 0.f; }
+#pragma unroll
+            for (int c = 0; c < Q; ++c) {
+                // r_{i-1-c} in series order
+                const int idx = r * C + kk - 1 - c;
+                float ef;
+                ma_coef(ps, c, ef);
+                if (idx >= 0 && ef > 0.f) {
+                    const int rr = idx / C, k2 = idx - rr * C;
+                    const float rp = rb[posof(rr, k2)];
+                    const float dt = s_dt[c * slots + ps];
+                    const float tau = ic[3 + 2 * c];
+                    gp[c] = -lam * rp * ef;
+                    gt[c] = -lam * rp * ic[2 + 2 * c] * ef * dt / (tau * tau);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < KI; ++k) {
+                if (k == ki) {
+                    g_off[k] -= lam;
+                    g_jit[k] += gj;
+#pragma unroll
+                    for (int c = 0; c < NQ; ++c) { g_phi[k][c] += gp[c]; g_tau[k][c] += gt[c]; }
+                }
+            }
+            if (Q > 0) {
+#pragma unroll
+                for (int m = NQ - 1; m > 0; --m) st[m] = st[m - 1];
+                st[0] = lam;
+            }
+        }
+    }
+    // reduce the noise gradients into gfull (lane 0 of the group)
+    for (int k = 0; k < min(n_ins, KI); ++k) {
+        LaneAcc<EMP_PREC_MIXED> a1; a1.init(); a1.add(g_off[k]);
+        const double s_off = a1.group_sum<L>(red, r);
+        LaneAcc<EMP_PREC_MIXED> a2; a2.init(); a2.add(g_jit[k]);
+        const double s_jit = a2.group_sum<L>(red, r);
+        if (r == 0 && valid) {
+            if (md->offset_slot >= 0) gfull[md->offset_slot + k] += s_off;
+            if (md->jitter_slot >= 0) gfull[md->jitter_slot + k] += s_jit;
+        }
+#pragma unroll
+        for (int c = 0; c < Q; ++c) {
+            LaneAcc<EMP_PREC_MIXED> a3; a3.init(); a3.add(g_phi[k][c]);
+            const double s_phi = a3.group_sum<L>(red, r);
+            LaneAcc<EMP_PREC_MIXED> a4; a4.init(); a4.add(g_tau[k][c]);
+            const double s_tau = a4.group_sum<L>(red, r);
+            if (r == 0 && valid) {
+                const int base = md->ma_global ? md->ma_slot + 2 * c : md->ma_slot + 2 * Q * k + 2 * c;
+                gfull[base] += s_phi;
+                gfull[base + 1] += s_tau;
+            }
+        }
+        __syncthreads();
+    }
+
+    // ---------------- pass 5: planets (E recomputed) and acceleration ------
+    for (int p = 0; p < n_planets; ++p) {
+        const float* pc = pcs + p * kGradPC;
+        float gP = 0.f, gK = 0.f, gF = 0.f, g3 = 0.f, g4 = 0.f;
+        if (valid) {
+            const float ec = pc[4], cwp = pc[5], swp = pc[6], K = pc[7], q = pc[8];
+            const float fh = pc[0];
+            for (int k0 = 0; k0 < nr; k0 += NE) {
+                int pos[NE];
+                bool ok[NE];
+                float th[NE], tl[NE], M[NE], sn[NE], cs[NE];
+#pragma unroll
+                for (int e = 0; e < NE; ++e) {
+                    const int kk = k0 + e < nr ? k0 + e : nr - 1;
+                    ok[e] = k0 + e < nr;
+                    pos[e] = posof(r, kk);
+                    th[e] = s_th[pos[e]];
+                    tl[e] = s_tl[pos[e]];
+                    M[e] = mean_anomaly_mixed(pc, th[e], tl[e]);
+                }
+                kepler_f32_n<NE>(M, ec, sn, cs);
+#pragma unroll
+                for (int e = 0; e < NE; ++e) {
+                    if (!ok[e]) continue;
+                    const float wgt = -lb[pos[e]];                   // dL/dmodel_i
+                    const float invD = __frcp_rn(1.f - ec * cs[e]);
+                    const float Nn = (cs[e] - ec) * cwp - q * sn[e] * swp;
+                    const float F = Nn * invD;
+                    const float dNdE = -sn[e] * cwp - q * cs[e] * swp;
+                    const float dFdE = (dNdE - F * ec * sn[e]) * invD;
+                    const float dRVdM = K * dFdE * invD;
+                    const float tf = (th[e] + tl[e]) * fh;           // t / P
+                    gF += wgt * dRVdM;
+                    gP += wgt * dRVdM * (-6.28318530717958647692f * tf * fh);
+                    gK += wgt * (F + ec * cwp);
+                    const float dNde = -cwp + (q > 0.f ? ec / q : 0.f) * sn[e] * swp;
+                    const float dFde = (dNde + F * cs[e]) * invD;
+                    const float dRVde = K * (dFde + dFdE * sn[e] * invD) + K * cwp;
+                    const float dRVdcw = K * ((cs[e] - ec) * invD + ec);
+                    const float dRVdsw = -K * q * sn[e] * invD;
+                    if (pc[12] == 0.f) {
+                        g3 += wgt * dRVde;                                     // e
+                        g4 += wgt * (-dRVdcw * swp + dRVdsw * cwp);            // omega
+                    } else {
+                        const float S = pc[9], Cc = pc[10], r3 = pc[11];
+                        g3 += wgt * (dRVde * 2.f * S + (dRVdcw * (-Cc * S) + dRVdsw * (Cc * Cc)) * r3);
+                        g4 += wgt * (dRVde * 2.f * Cc + (dRVdcw * (S * S) + dRVdsw * (-S * Cc)) * r3);
+                    }
+                }
+            }
+        }
+        float gv[5] = {gP, gK, gF, g3, g4};
+        for (int j = 0; j < 5; ++j) {
+            LaneAcc<EMP_PREC_MIXED> a; a.init(); a.add(gv[j]);
+            const double sj = a.group_sum<L>(red, r);
+            if (r == 0 && valid) gfull[md->kep_slot[p] + j] += sj;
+            __syncthreads();
+        }
+    }
+    for (int j = 0; j < acc_order; ++j) {
+        float ga = 0.f;
+        if (valid) {
+            for (int kk = 0; kk < nr; ++kk) {
+                const int ps = posof(r, kk);
+                const float x = (s_th[ps] - (float)A.d.t0) + s_tl[ps];
+                // d polyval / d coef_j = x^(acc_order - j)
+                float pw = 1.f;
+                for (int m = 0; m < acc_order - j; ++m) pw *= x;
+                ga += -lb[ps] * pw;
+            }
+        }
+        LaneAcc<EMP_PREC_MIXED> a; a.init(); a.add(ga);
+        const double sj = a.group_sum<L>(red, r);
+        if (r == 0 && valid) gfull[md->acc_slot + j] += sj;
+        __syncthreads();
+    }
+
+    // ---------------- outputs ---------------------------------------------
+    __syncthreads();
+    if (active) {
+        if (r == 0) {
+            A.logl[wk] = valid ? -0.5 * sumL + md->loglike_const : -INFINITY;
+            A.logprior[wk] = lp;
+        }
+        for (int d = r; d < n_free; d += L)
+            A.grad_logl[(size_t)wk * n_free + d] = valid ? gfull[md->prior_slot[d]] : 0.0;
+    }
+}
+
+}  // namespace emp

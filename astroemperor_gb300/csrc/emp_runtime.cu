@@ -18,11 +18,14 @@
 #include "emp_device.cuh"
 #include "emp_pt.cuh"
 #include "emp_model_eval.cuh"
+#include "emp_grad.cuh"
 
 namespace emp {
 using KFn = void (*)(KArgs);
 KFn get_kernel_fp64(int q, int lidx);
 KFn get_kernel_mixed(int q, int lidx);
+using GFn = void (*)(GArgs);
+GFn get_kernel_grad(int q, int lidx);
 }  // namespace emp
 
 using namespace emp;
@@ -548,6 +551,58 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, dou
         CUDA_TRY(cudaGetLastError());
     }
     return EMP_OK;
+}
+
+int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, double* logprior,
+                     double* grad_logl, double* grad_logprior, void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (B < 0) return fail(EMP_E_INVALID, "B=%d < 0", B);
+    if (B == 0) return EMP_OK;
+    if (!theta || !logl || !logprior || !grad_logl || !grad_logprior)
+        return fail(EMP_E_INVALID, "a NULL argument");
+    const emp_model_desc& m = h->md;
+    for (int p = 0; p < m.n_planets; ++p)
+        if (m.kep_param[p] != 0 && m.kep_param[p] != 1)
+            return fail(EMP_E_UNSUPPORTED, "gradient: parameterisation %d (0 and 1 are built)", m.kep_param[p]);
+    if (m.n_ins > kGradMaxIns)
+        return fail(EMP_E_UNSUPPORTED, "gradient: %d instruments (at most %d)", m.n_ins, kGradMaxIns);
+    if (h->q > 2) return fail(EMP_E_UNSUPPORTED, "gradient: MA order %d (at most 2)", h->q);
+    static const int kL[4] = {32, 64, 128, 256};
+    static bool attr[3][4] = {};
+    // prefer ~16-32 epochs per lane, then the largest shape that fits
+    int order[4] = {0, 1, 2, 3};
+    if (h->n >= 2048) { order[0] = 2; order[1] = 3; order[2] = 1; order[3] = 0; }
+    else if (h->n >= 512) { order[0] = 1; order[1] = 2; order[2] = 0; order[3] = 3; }
+    for (int oi = 0; oi < 4; ++oi) {
+        const int li = order[oi];
+        const int L = kL[li];
+        const int NT = L > 128 ? L : 128;
+        GSmem lay;
+        lay.build(h->q, L, NT / L, h->n, m.n_full, m.n_free, m.n_planets, m.n_ins, m.acc_order);
+        if (lay.total > 227 * 1024) continue;
+        GFn fn = get_kernel_grad(h->q, li);
+        if (!fn) return fail(EMP_E_UNSUPPORTED, "no gradient kernel for q=%d", h->q);
+        if (!attr[h->q][li]) {
+            CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          227 * 1024));
+            attr[h->q][li] = true;
+        }
+        GArgs a{};
+        a.md = h->md_dev;
+        a.d = h->dd;
+        a.nwalk = B;
+        a.theta = theta;
+        a.logl = logl;
+        a.logprior = logprior;
+        a.grad_logl = grad_logl;
+        a.grad_logprior = grad_logprior;
+        const int G = NT / L;
+        fn<<<(B + G - 1) / G, NT, lay.total, (cudaStream_t)stream>>>(a);
+        g_launches.fetch_add(1);
+        CUDA_TRY(cudaGetLastError());
+        return EMP_OK;
+    }
+    return fail(EMP_E_SIZE, "gradient: %d epochs do not fit in shared memory", h->n);
 }
 
 int64_t emp_pt_work_bytes(int ntemps, int nwalkers, int ndim) {

@@ -116,6 +116,19 @@ class Context:
         return logl, logprior
 
 
+    def logpost_grad(self, theta: torch.Tensor, stream=None):
+        """(logL, logprior, dlogL/dtheta, dlogprior/dtheta) of theta [B, ndim],
+        from the adjoint kernel (FP32 per epoch, FP64 sums)."""
+        theta = theta.contiguous()
+        B, D = theta.shape
+        f64 = dict(dtype=torch.float64, device=theta.device)
+        logl, logprior = torch.empty(B, **f64), torch.empty(B, **f64)
+        gl, gp = torch.empty(B, D, **f64), torch.empty(B, D, **f64)
+        s = stream if stream is not None else torch.cuda.current_stream(theta.device)
+        N.call('emp_logpost_grad', self.h, _ptr(theta), B, _ptr(logl), _ptr(logprior), _ptr(gl),
+               _ptr(gp), s.cuda_stream)
+        return logl, logprior, gl, gp
+
     def model_eval(self, theta: torch.Tensor, stream=None):
         """my_model(theta) on the device: (model0, err20), each [B, ndata], FP64."""
         theta = theta.contiguous()

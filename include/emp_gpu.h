@@ -144,6 +144,19 @@ int emp_logpost(emp_handle* h, const double* theta, int B,
                 double* logl, double* logprior, double* logp,
                 int precision, void* stream);
 
+/* Gradient of my_likelihood and my_prior (the reference has none; it is the
+   adjoint of support/likelihoods/00.like:3-5 through my_model,
+   emp_model.py:706-781) for a batch of B walkers: logl/logprior [B] and
+   grad_logl/grad_logprior [B][n_free] (device, FP64), with respect to the
+   free parameters.  FP32 forward and adjoint per epoch, float-float sums
+   finished in FP64.  Keplerian parameterisations 0 and 1, up to 4
+   instruments, MA order <= 2, whole series <= shared memory (~8000 epochs
+   with MA(1)); EMP_E_UNSUPPORTED / EMP_E_SIZE otherwise.  Walkers outside
+   the prior support get logl = -inf and a zero logl gradient. */
+int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl,
+                     double* logprior, double* grad_logl, double* grad_logprior,
+                     void* stream);
+
 /* Replaces: my_model(theta) -> (model0, err20) (emp_model.py:706-781) for a
    batch of B walkers; model/err2 are device [B][n] in the dataset's input
    (time) order, model including the moving-average terms.  FP64.  Meant

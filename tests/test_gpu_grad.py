@@ -1,0 +1,139 @@
+"""Adjoint kernel (d logL/d theta, d logprior/d theta) against an FP64 torch
+autograd reference and central finite differences; the autograd wrapper;
+multistart MAP.
+
+Tolerance for the gradient: per component, |g - g_ref| <= 1e-5 * max(|g_ref|,
+1e-3 * max_j |g_ref_j|) (relative, with a floor for components near zero).
+"""
+import numpy as np
+import pytest
+import torch
+
+from astroemperor_gb300 import _native as N
+from astroemperor_gb300 import synth
+from astroemperor_gb300.autograd import log_posterior
+from astroemperor_gb300.engine import Context
+from astroemperor_gb300.mapfit import multistart_map
+from oracle.grad_ref import TorchRV
+from oracle.rv import OracleRV
+from tests.golden.cases import kat_case_models, model_51peg
+
+pytestmark = pytest.mark.gpu
+
+GRAD_RTOL = 1e-5
+
+
+def _rel_err(g, ref):
+    floor = 1e-3 * np.max(np.abs(ref), axis=1, keepdims=True)
+    return np.abs(g - ref) / np.maximum(np.abs(ref), floor)
+
+
+def _prior_draws(model, o, n, rng, shrink_ecc=0.7):
+    lim = model.limits_free()
+    out = []
+    while len(out) < n:
+        th = rng.uniform(lim[:, 0], lim[:, 1])
+        for j, p in enumerate(model.free_parameters()):
+            if p.name.startswith(('Ecc_sin', 'Ecc_cos')):
+                th[j] *= shrink_ecc
+        if np.isfinite(o.my_prior(th)):
+            out.append(th)
+    return np.array(out)
+
+
+@pytest.mark.parametrize('name', ['51peg_k1_p1', '51peg_k1_p0', '51peg_fixed_acc', '51peg_gma2',
+                                  'c2_ma1', 'c2_ma1_quirk', '51peg_k0'])
+def test_gradient_matches_fp64_autograd(peg_arr, lib, cuda, name):
+    m, d, _ = kat_case_models(peg_arr)[name]
+    o = OracleRV(m.spec(), d.as_dict())
+    th = _prior_draws(m, o, 16, np.random.default_rng(3))
+    ctx = Context(m, 'cuda:0')
+    t = torch.as_tensor(th, dtype=torch.float64, device='cuda:0')
+    ll, lp, gl, gp = ctx.logpost_grad(t)
+    torch.cuda.synchronize()
+    ll, gl = ll.cpu().numpy(), gl.cpu().numpy()
+    want_ll = np.array([o.my_likelihood(x) for x in th])
+    assert np.max(np.abs(ll - want_ll) / np.abs(want_ll)) <= 1e-6
+    ref_ll, ref_g = TorchRV(m.spec(), d.as_dict()).grad(th)
+    err = _rel_err(gl, ref_g)
+    print(name, 'max rel gradient error', err.max(), 'median', np.median(err))
+    assert err.max() <= GRAD_RTOL, (name, err.max(), np.unravel_index(err.argmax(), err.shape))
+    np.testing.assert_allclose(lp.cpu().numpy(), [o.my_prior(x) for x in th], rtol=1e-13, atol=1e-13)
+
+
+def test_prior_gradient(peg_arr, lib, cuda):
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    o = OracleRV(m.spec(), d.as_dict())
+    th = _prior_draws(m, o, 8, np.random.default_rng(4))
+    ctx = Context(m, 'cuda:0')
+    _, _, _, gp = ctx.logpost_grad(torch.as_tensor(th, device='cuda:0'))
+    gp = gp.cpu().numpy()
+    for b, x in enumerate(th):
+        for j in range(len(x)):
+            h = 1e-6 * max(1.0, abs(x[j]))
+            a, c = x.copy(), x.copy()
+            a[j] += h
+            c[j] -= h
+            fd = (o.my_prior(a) - o.my_prior(c)) / (2 * h)
+            assert gp[b, j] == pytest.approx(fd, abs=1e-6, rel=1e-6)
+
+
+def test_c4_gradient_at_1000_prior_draws(lib, cuda):
+    """5 Keplerians, 3 instruments with offset, jitter, MA(1) each, N=4096."""
+    model, data, setup, truth = synth.build_model('c4', seed=11)
+    o = OracleRV(model.spec(), data.as_dict())
+    th = _prior_draws(model, o, 1000, np.random.default_rng(12), shrink_ecc=0.6)
+    ctx = Context(model, 'cuda:0')
+    ll, lp, gl, gp = ctx.logpost_grad(torch.as_tensor(th, device='cuda:0'))
+    torch.cuda.synchronize()
+    ref = TorchRV(model.spec(), data.as_dict(), device='cuda:0')
+    ref_ll, ref_g = ref.grad(th)
+    rel_ll = np.abs(ll.cpu().numpy() - ref_ll) / np.abs(ref_ll)
+    assert rel_ll.max() <= 1e-6
+    err = _rel_err(gl.cpu().numpy(), ref_g)
+    print('C4 gradient: max rel error', err.max(), 'median', np.median(err))
+    assert err.max() <= GRAD_RTOL
+    # central finite differences (h = 1e-6 relative) on the FP64 oracle for a
+    # few draws; period components excluded (their second derivative makes
+    # the 1e-6 step's truncation error larger than the tolerance)
+    g = gl.cpu().numpy()
+    names = [p.name for p in model.free_parameters()]
+    for b in range(3):
+        x = th[b]
+        for j in range(len(x)):
+            if names[j].startswith('Period'):
+                continue
+            h = 1e-6 * max(1.0, abs(x[j]))
+            a, c = x.copy(), x.copy()
+            a[j] += h
+            c[j] -= h
+            fd = (o.my_likelihood(a) - o.my_likelihood(c)) / (2 * h)
+            assert abs(g[b, j] - fd) <= 1e-3 * max(abs(fd), 1e-2 * np.max(np.abs(g[b]))), (names[j], g[b, j], fd)
+
+
+def test_autograd_function(peg_arr, lib, cuda):
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    o = OracleRV(m.spec(), d.as_dict())
+    th = torch.as_tensor(_prior_draws(m, o, 8, np.random.default_rng(5)), device='cuda:0')
+    ctx = Context(m, 'cuda:0')
+    x = th.clone().requires_grad_(True)
+    lp = log_posterior(x, ctx, N.EMP_PREC_MIXED)
+    lp.sum().backward()
+    _, _, gl, gp = ctx.logpost_grad(th)
+    torch.testing.assert_close(x.grad, gl + gp)
+
+
+def test_multistart_map_finds_the_51peg_fit(peg_arr, lib, cuda):
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    o = OracleRV(m.spec(), d.as_dict())
+    rng = np.random.default_rng(6)
+    starts = _prior_draws(m, o, 256, rng)
+    starts[:, 0] = rng.uniform(4.2, 4.26, size=256)        # a periodogram-like search box
+    ctx = Context(m, 'cuda:0')
+    res = multistart_map(ctx, m, torch.as_tensor(starts, device='cuda:0'), iters=300)
+    lp = res['logp'].cpu().numpy()
+    best = res['theta'][int(np.argmax(lp))].cpu().numpy()
+    # the oracle's maximum posterior with the current Normal normaliser
+    assert lp.max() == pytest.approx(o.my_likelihood(best) + o.my_prior(best), abs=1e-4)
+    assert lp.max() >= -881.52 - 0.02
+    assert best[0] == pytest.approx(4.2308, abs=5e-4)
