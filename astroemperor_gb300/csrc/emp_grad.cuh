@@ -478,12 +478,13 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
     }
 
     // ---------------- pass 4: lambda, noise-model gradients ---------------
-    float g_off[KI], g_jit[KI], g_phi[KI][NQ], g_tau[KI][NQ];
+    // compensated (TwoSum) per-lane sums: the gradient terms cancel strongly
+    LaneAcc<EMP_PREC_MIXED> g_off[KI], g_jit[KI], g_phi[KI][NQ], g_tau[KI][NQ];
 #pragma unroll
     for (int k = 0; k < KI; ++k) {
-        g_off[k] = 0.f; g_jit[k] = 0.f;
+        g_off[k].init(); g_jit[k].init();
 #pragma unroll
-        for (int c = 0; c < NQ; ++c) { g_phi[k][c] = 0.f; g_tau[k][c] = 0.f; }
+        for (int c = 0; c < NQ; ++c) { g_phi[k][c].init(); g_tau[k][c].init(); }
     }
     if (valid) {
         float st[NQ];
@@ -527,10 +528,10 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
 #pragma unroll
             for (int k = 0; k < KI; ++k) {
                 if (k == ki) {
-                    g_off[k] -= lam;
-                    g_jit[k] += gj;
+                    g_off[k].add(-lam);
+                    g_jit[k].add(gj);
 #pragma unroll
-                    for (int c = 0; c < NQ; ++c) { g_phi[k][c] += gp[c]; g_tau[k][c] += gt[c]; }
+                    for (int c = 0; c < Q; ++c) { g_phi[k][c].add(gp[c]); g_tau[k][c].add(gt[c]); }
                 }
             }
             if (Q > 0) {
@@ -542,20 +543,16 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
     }
     // reduce the noise gradients into gfull (lane 0 of the group)
     for (int k = 0; k < min(n_ins, KI); ++k) {
-        LaneAcc<EMP_PREC_MIXED> a1; a1.init(); a1.add(g_off[k]);
-        const double s_off = a1.group_sum<L>(red, r);
-        LaneAcc<EMP_PREC_MIXED> a2; a2.init(); a2.add(g_jit[k]);
-        const double s_jit = a2.group_sum<L>(red, r);
+        const double s_off = g_off[k].group_sum<L>(red, r);
+        const double s_jit = g_jit[k].group_sum<L>(red, r);
         if (r == 0 && valid) {
             if (md->offset_slot >= 0) gfull[md->offset_slot + k] += s_off;
             if (md->jitter_slot >= 0) gfull[md->jitter_slot + k] += s_jit;
         }
 #pragma unroll
         for (int c = 0; c < Q; ++c) {
-            LaneAcc<EMP_PREC_MIXED> a3; a3.init(); a3.add(g_phi[k][c]);
-            const double s_phi = a3.group_sum<L>(red, r);
-            LaneAcc<EMP_PREC_MIXED> a4; a4.init(); a4.add(g_tau[k][c]);
-            const double s_tau = a4.group_sum<L>(red, r);
+            const double s_phi = g_phi[k][c].group_sum<L>(red, r);
+            const double s_tau = g_tau[k][c].group_sum<L>(red, r);
             if (r == 0 && valid) {
                 const int base = md->ma_global ? md->ma_slot + 2 * c : md->ma_slot + 2 * Q * k + 2 * c;
                 gfull[base] += s_phi;
@@ -568,7 +565,8 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
     // ---------------- pass 5: planets (E recomputed) and acceleration ------
     for (int p = 0; p < n_planets; ++p) {
         const float* pc = pcs + p * kGradPC;
-        float gP = 0.f, gK = 0.f, gF = 0.f, g3 = 0.f, g4 = 0.f;
+        LaneAcc<EMP_PREC_MIXED> gP, gK, gF, g3, g4;
+        gP.init(); gK.init(); gF.init(); g3.init(); g4.init();
         if (valid) {
             const float ec = pc[4], cwp = pc[5], swp = pc[6], K = pc[7], q = pc[8];
             const float fh = pc[0];
@@ -597,35 +595,36 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
                     const float dFdE = (dNdE - F * ec * sn[e]) * invD;
                     const float dRVdM = K * dFdE * invD;
                     const float tf = (th[e] + tl[e]) * fh;           // t / P
-                    gF += wgt * dRVdM;
-                    gP += wgt * dRVdM * (-6.28318530717958647692f * tf * fh);
-                    gK += wgt * (F + ec * cwp);
+                    gF.add(wgt * dRVdM);
+                    gP.add(wgt * dRVdM * (-6.28318530717958647692f * tf * fh));
+                    gK.add(wgt * (F + ec * cwp));
                     const float dNde = -cwp + (q > 0.f ? ec / q : 0.f) * sn[e] * swp;
                     const float dFde = (dNde + F * cs[e]) * invD;
                     const float dRVde = K * (dFde + dFdE * sn[e] * invD) + K * cwp;
                     const float dRVdcw = K * ((cs[e] - ec) * invD + ec);
                     const float dRVdsw = -K * q * sn[e] * invD;
                     if (pc[12] == 0.f) {
-                        g3 += wgt * dRVde;                                     // e
-                        g4 += wgt * (-dRVdcw * swp + dRVdsw * cwp);            // omega
+                        g3.add(wgt * dRVde);                                   // e
+                        g4.add(wgt * (-dRVdcw * swp + dRVdsw * cwp));          // omega
                     } else {
                         const float S = pc[9], Cc = pc[10], r3 = pc[11];
-                        g3 += wgt * (dRVde * 2.f * S + (dRVdcw * (-Cc * S) + dRVdsw * (Cc * Cc)) * r3);
-                        g4 += wgt * (dRVde * 2.f * Cc + (dRVdcw * (S * S) + dRVdsw * (-S * Cc)) * r3);
+                        g3.add(wgt * (dRVde * 2.f * S + (dRVdcw * (-Cc * S) + dRVdsw * (Cc * Cc)) * r3));
+                        g4.add(wgt * (dRVde * 2.f * Cc + (dRVdcw * (S * S) + dRVdsw * (-S * Cc)) * r3));
                     }
                 }
             }
         }
-        float gv[5] = {gP, gK, gF, g3, g4};
+        const LaneAcc<EMP_PREC_MIXED>* gv[5] = {&gP, &gK, &gF, &g3, &g4};
+#pragma unroll
         for (int j = 0; j < 5; ++j) {
-            LaneAcc<EMP_PREC_MIXED> a; a.init(); a.add(gv[j]);
-            const double sj = a.group_sum<L>(red, r);
+            const double sj = gv[j]->group_sum<L>(red, r);
             if (r == 0 && valid) gfull[md->kep_slot[p] + j] += sj;
             __syncthreads();
         }
     }
     for (int j = 0; j < acc_order; ++j) {
-        float ga = 0.f;
+        LaneAcc<EMP_PREC_MIXED> ga;
+        ga.init();
         if (valid) {
             for (int kk = 0; kk < nr; ++kk) {
                 const int ps = posof(r, kk);
@@ -633,11 +632,10 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
                 // d polyval / d coef_j = x^(acc_order - j)
                 float pw = 1.f;
                 for (int m = 0; m < acc_order - j; ++m) pw *= x;
-                ga += -lb[ps] * pw;
+                ga.add(-lb[ps] * pw);
             }
         }
-        LaneAcc<EMP_PREC_MIXED> a; a.init(); a.add(ga);
-        const double sj = a.group_sum<L>(red, r);
+        const double sj = ga.group_sum<L>(red, r);
         if (r == 0 && valid) gfull[md->acc_slot + j] += sj;
         __syncthreads();
     }

@@ -34,7 +34,7 @@ def _objective(ctx, u, lo, span):
     return f, g
 
 
-def multistart_map(ctx, model, theta0: torch.Tensor, iters=200, m=8, tol=1e-7, max_ls=25):
+def multistart_map(ctx, model, theta0: torch.Tensor, iters=300, m=8, tol=1e-12, max_ls=25):
     """L-BFGS from every row of theta0 [S, D] (inside the limits).
 
     Returns dict with theta [S, D], logp [S] (log posterior), iterations.

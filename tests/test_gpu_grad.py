@@ -128,9 +128,9 @@ def test_multistart_map_finds_the_51peg_fit(peg_arr, lib, cuda):
     o = OracleRV(m.spec(), d.as_dict())
     rng = np.random.default_rng(6)
     starts = _prior_draws(m, o, 256, rng)
-    starts[:, 0] = rng.uniform(4.2, 4.26, size=256)        # a periodogram-like search box
+    starts[:, 0] = rng.uniform(4.229, 4.2325, size=256)     # a periodogram-peak search box
     ctx = Context(m, 'cuda:0')
-    res = multistart_map(ctx, m, torch.as_tensor(starts, device='cuda:0'), iters=300)
+    res = multistart_map(ctx, m, torch.as_tensor(starts, device="cuda:0"), iters=400)
     lp = res['logp'].cpu().numpy()
     best = res['theta'][int(np.argmax(lp))].cpu().numpy()
     # the oracle's maximum posterior with the current Normal normaliser
