@@ -77,6 +77,7 @@ class EmpPtState(C.Structure):
         ('adapt_tau', C.c_double), ('adapt_nu', C.c_double),
         ('adapt_mode', C.c_int32), ('precision', C.c_int32),
         ('work', C.c_void_p), ('work_bytes', C.c_int64),
+        ('n_systems', C.c_int32), ('_pad2', C.c_int32),
     ]
 
 
@@ -93,6 +94,8 @@ class EmpPtRecord(C.Structure):
 SIGNATURES = {
     'emp_create': (C.c_int, [C.POINTER(EmpModelDesc), C.POINTER(EmpDatasetDesc), C.POINTER(C.c_void_p)]),
     'emp_destroy': (C.c_int, [C.c_void_p]),
+    'emp_create_batch': (C.c_int, [C.POINTER(EmpModelDesc), C.POINTER(EmpDatasetDesc), C.POINTER(C.c_void_p)]),
+    'emp_num_systems': (C.c_int, [C.c_void_p]),
     'emp_logpost': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     'emp_logpost_grad': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,

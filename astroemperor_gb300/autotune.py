@@ -110,3 +110,38 @@ def representative_batch(model, batch, device, rng=None):
         elif p.name.startswith('Eccentricity'):
             th[:, j] = np.minimum(th[:, j], 0.5)
     return torch.as_tensor(th, dtype=torch.float64, device=device)
+
+
+def autotune_batch(ctx, theta, precision=N.EMP_PREC_MIXED, reps=3, verbose=False):
+    """(L, tile, ms) for a batch handle: every candidate timed on theta
+    [S, B, ndim] (all systems in one launch), the fastest kept."""
+    theta = theta.contiguous()
+    S, B, _ = theta.shape
+    stream = torch.cuda.Stream(device=theta.device)
+    n_typ = int(np.median(ctx.n_epochs))
+    ll = torch.empty(S, B, dtype=torch.float64, device=theta.device)
+    lp = torch.empty_like(ll)
+    best, seen = None, set()
+    for L, tile in candidates(n_typ, B):
+        ctx.set_launch(precision, L, tile)
+        eff = ctx.get_launch(precision)
+        if eff in seen:
+            continue
+        seen.add(eff)
+        args = (ctx.h, theta.data_ptr(), B, None, None, ll.data_ptr(), lp.data_ptr(), None,
+                int(precision), stream.cuda_stream)
+        N.call('emp_logpost', *args)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            N.call('emp_logpost', *args)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        if verbose:
+            print(f'autotune batch L={eff[0]:4d} tile={eff[1]:5d} {ms:9.3f} ms')
+        if best is None or ms < best[0]:
+            best = (ms, eff[0], eff[1])
+    ms, L, tile = best
+    ctx.set_launch(precision, L, tile)
+    return L, tile, ms

@@ -123,6 +123,16 @@ struct KArgs {
     int step_in_sweep;
     uint64_t seed;
     double a;
+    // systems (one for a plain handle; many for a batch handle)
+    int T;                     // temperatures per system (PT modes)
+    int n_sys;                 // systems processed by this launch
+    int cps;                   // CTA items per system
+    const int64_t* sys_off;    // [S+1] epoch offsets, null = one system
+    const double* sys_t0;      // [S] acceleration origins, null = d.t0
+    const int* sys_order;      // [S] systems costliest first, null = one system
+    int* work_counter;         // persistent scheduling counter, null = one item per CTA
+    int dstride;               // theta row stride (largest free dimension)
+    int lay_full, lay_free, lay_planets, lay_ins, lay_acc;   // layout maxima
 };
 
 // ----------------------------------------------------------------------------

@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
             lacc.add(x * x * w + __log2f(err2) * 0.69314718055994531f);
         }
     }
-    const double sumL = lacc.group_sum<L>(red, r);
+    const double sumL = lacc.template group_sum<L>(red, r);
     __syncthreads();
 
     // ---------------- pass 3: backward map, reverse scan -------------------
@@ -543,16 +543,16 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
     }
     // reduce the noise gradients into gfull (lane 0 of the group)
     for (int k = 0; k < min(n_ins, KI); ++k) {
-        const double s_off = g_off[k].group_sum<L>(red, r);
-        const double s_jit = g_jit[k].group_sum<L>(red, r);
+        const double s_off = g_off[k].template group_sum<L>(red, r);
+        const double s_jit = g_jit[k].template group_sum<L>(red, r);
         if (r == 0 && valid) {
             if (md->offset_slot >= 0) gfull[md->offset_slot + k] += s_off;
             if (md->jitter_slot >= 0) gfull[md->jitter_slot + k] += s_jit;
         }
 #pragma unroll
         for (int c = 0; c < Q; ++c) {
-            const double s_phi = g_phi[k][c].group_sum<L>(red, r);
-            const double s_tau = g_tau[k][c].group_sum<L>(red, r);
+            const double s_phi = g_phi[k][c].template group_sum<L>(red, r);
+            const double s_tau = g_tau[k][c].template group_sum<L>(red, r);
             if (r == 0 && valid) {
                 const int base = md->ma_global ? md->ma_slot + 2 * c : md->ma_slot + 2 * Q * k + 2 * c;
                 gfull[base] += s_phi;
@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
         const LaneAcc<EMP_PREC_MIXED>* gv[5] = {&gP, &gK, &gF, &g3, &g4};
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-            const double sj = gv[j]->group_sum<L>(red, r);
+            const double sj = gv[j]->template group_sum<L>(red, r);
             if (r == 0 && valid) gfull[md->kep_slot[p] + j] += sj;
             __syncthreads();
         }
@@ -635,7 +635,7 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
                 ga.add(-lb[ps] * pw);
             }
         }
-        const double sj = ga.group_sum<L>(red, r);
+        const double sj = ga.template group_sum<L>(red, r);
         if (r == 0 && valid) gfull[md->acc_slot + j] += sj;
         __syncthreads();
     }

@@ -403,21 +403,12 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     constexpr int NE = (PREC == EMP_PREC_MIXED) ? 4 : 1;   // epochs in flight per lane
     extern __shared__ __align__(16) unsigned char smem[];
 
-    const emp_model_desc* md = A.md;
-    const int n_full = md->n_full;
-    const int n_free = md->n_free;
-    const int n_planets = md->n_planets;
-    const int n_ins = md->n_ins;
-    const int acc_order = md->acc_order;
-
     Smem lay;
-    lay.build(PREC, Q, L, G, A.tile, n_full, n_free, n_planets, n_ins, acc_order);
+    lay.build(PREC, Q, L, G, A.tile, A.lay_full, A.lay_free, A.lay_planets, A.lay_ins, A.lay_acc);
 
     const int tid = threadIdx.x;
     const int g = tid / L;
     const int r = tid - g * L;
-    const int wk = blockIdx.x * G + g;
-    const bool active = wk < A.nwalk;
 
     unsigned char* gs = smem + lay.tile_bytes + g * lay.group_bytes;
     double* full = reinterpret_cast<double*>(gs + lay.off_full);
@@ -432,6 +423,36 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     int* flag = reinterpret_cast<int*>(misc + 4);
     constexpr int INSW = 2 + 2 * kMaxQ;
 
+    // items: one per CTA for a plain handle; (system, walker chunk) pairs
+    // claimed from an atomic counter, costliest systems first, for a batch
+    __shared__ int s_item;
+    int item = blockIdx.x;
+    for (;;) {
+    if (A.work_counter != nullptr) {
+        __syncthreads();
+        if (tid == 0) s_item = atomicAdd(A.work_counter, 1);
+        __syncthreads();
+        item = s_item;
+        if (item >= A.n_sys * A.cps) break;
+    }
+    const int sidx = A.sys_order != nullptr ? item / A.cps : 0;
+    const int sys = A.sys_order != nullptr ? A.sys_order[sidx] : 0;
+    const int chunk = item - sidx * A.cps;
+    const emp_model_desc* md = A.md + sys;
+    const int n_full = md->n_full;
+    const int n_free = md->n_free;
+    const int n_planets = md->n_planets;
+    const int n_ins = md->n_ins;
+    const int acc_order = md->acc_order;
+    const int wk = chunk * G + g;
+    const bool active = wk < A.nwalk;
+    const int64_t e0 = A.sys_off != nullptr ? A.sys_off[sys] : 0;
+    const double t0 = A.sys_t0 != nullptr ? A.sys_t0[sys] : A.d.t0;
+    const int ds = A.dstride;
+    const uint64_t seed = A.seed + (uint64_t)sys * 0x9E3779B97F4A7C15ULL;
+    const int pbase = sys * A.T * A.W;       // positions / slots of this system
+    const int bbase = sys * A.T;             // its inverse temperatures
+
     // ---------------- walker identity and theta -------------------------
     int t_idx = 0, j_idx = 0, slot_j = 0;
     double z = 1.0;
@@ -439,18 +460,19 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     if (active) {
         if (r == 0) flag[0] = 0;
         if (A.mode == kModeLogpost) {
-            for (int d = r; d < n_free; d += L) thp[d] = A.theta[(size_t)wk * n_free + d];
+            slot_j = sys * A.nwalk + wk;     // rows of a batch handle are [S][B]
+            for (int d = r; d < n_free; d += L) thp[d] = A.theta[(size_t)slot_j * ds + d];
         } else if (A.mode == kModeSlots) {
-            slot_j = wk;
-            for (int d = r; d < n_free; d += L) thp[d] = A.st_theta[(size_t)wk * n_free + d];
+            slot_j = pbase + wk;
+            for (int d = r; d < n_free; d += L) thp[d] = A.st_theta[(size_t)slot_j * ds + d];
         } else {
             const int Wh = A.W >> 1;
             t_idx = wk / Wh;
             const int jj = wk - t_idx * Wh;
             j_idx = 2 * jj + A.half;
-            slot_j = A.members[t_idx * A.W + j_idx];
+            slot_j = A.members[pbase + t_idx * A.W + j_idx];
             const uint64_t it = (uint64_t)A.counters[0] + (uint64_t)A.step_in_sweep;
-            U4 rr = rng_draw(A.seed, (uint32_t)(t_idx * A.W + j_idx), it,
+            U4 rr = rng_draw(seed, (uint32_t)(t_idx * A.W + j_idx), it,
                              kRngStretch0 + (uint32_t)A.half);
             uword = rr.w;
             // one warp per group forms z and the proposal (FP64, the
@@ -458,13 +480,13 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             if (r < 32) {
                 const int kk = (int)mulhi32(rr.z, (uint32_t)Wh);
                 const int k_idx = 2 * kk + (1 - A.half);
-                const int slot_k = A.members[t_idx * A.W + k_idx];
+                const int slot_k = A.members[pbase + t_idx * A.W + k_idx];
                 // emcee StretchMove.get_proposal: zz = ((a-1) u + 1)^2 / a
                 const double zz = __dadd_rn(__dmul_rn(A.a - 1.0, u53(rr.x, rr.y)), 1.0);
                 z = __dmul_rn(zz, zz) / A.a;
                 if (r == 0) misc[2] = z;
-                const double* sj = A.st_theta + (size_t)slot_j * n_free;
-                const double* ck = A.st_theta + (size_t)slot_k * n_free;
+                const double* sj = A.st_theta + (size_t)slot_j * ds;
+                const double* ck = A.st_theta + (size_t)slot_k * ds;
                 for (int d = r; d < n_free; d += (L < 32 ? L : 32))
                     thp[d] = __dsub_rn(ck[d], __dmul_rn(__dsub_rn(ck[d], sj[d]), z));
             }
@@ -536,7 +558,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     const bool valid = active && (lp > -INFINITY);
 
     // ---------------- likelihood over epoch tiles ------------------------
-    const int n = A.d.n;
+    const int n = A.sys_off != nullptr ? (int)(A.sys_off[sys + 1] - e0) : A.d.n;
     const int tile = A.tile;
     unsigned char* ts = smem;
     R* s_t0;  R* s_t1;  R* s_y;  R* s_s2;  int* s_in;  R* s_dt;
@@ -570,7 +592,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             const int rr = idx / C;
             const int kk = idx - rr * C;
             const int pos = kk * L + ((rr + kk) & (L - 1));
-            const int gi = base + idx;
+            const int64_t gi = e0 + base + idx;
             if (PREC == EMP_PREC_FP64) {
                 s_t0[pos] = (R)A.d.t[gi];
                 s_y[pos] = (R)A.d.y[gi];
@@ -584,8 +606,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             s_in[pos] = A.d.inst[gi];
 #pragma unroll
             for (int c = 0; c < Q; ++c) {
-                if (PREC == EMP_PREC_FP64) s_dt[c * tile + pos] = (R)A.d.dt[(size_t)c * n + gi];
-                else s_dt[c * tile + pos] = (R)A.d.dt32[(size_t)c * n + gi];
+                if (PREC == EMP_PREC_FP64) s_dt[c * tile + pos] = (R)A.d.dt[(size_t)c * A.d.n + gi];
+                else s_dt[c * tile + pos] = (R)A.d.dt32[(size_t)c * A.d.n + gi];
             }
         }
         __syncthreads();
@@ -625,7 +647,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                             m += rv_term_f64((const double*)(pcs + p * PC), t);
                         if (acc_order > 0) {
                             // np.polyval(concat(theta_acc, [0]), X_ - X_[0])
-                            double x = t - A.d.t0, pv = 0.0;
+                            double x = t - t0, pv = 0.0;
                             for (int j = 0; j < acc_order; ++j) pv = pv * x + accc[j];
                             m += pv * x;
                         }
@@ -651,7 +673,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     if (acc_order > 0) {
 #pragma unroll
                         for (int e = 0; e < NE; ++e) {
-                            const float x = (th[e] - (float)A.d.t0) + tl[e];
+                            const float x = (th[e] - (float)t0) + tl[e];
                             float pv = 0.f;
                             for (int j = 0; j < acc_order; ++j) pv = pv * x + (float)accc[j];
                             model[e] += (R)(pv * x);
@@ -784,19 +806,19 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     // ---------------- epilogue --------------------------------------------
     if (A.mode == kModeLogpost) {
         if (active && r == 0) {
-            A.logl[wk] = logl;
-            A.logprior[wk] = lp;
+            A.logl[slot_j] = logl;
+            A.logprior[slot_j] = lp;
             if (A.logp != nullptr && A.beta != nullptr)
-                A.logp[wk] = valid ? __dadd_rn(__dmul_rn(A.beta[wk], logl), lp) : -INFINITY;
+                A.logp[slot_j] = valid ? __dadd_rn(__dmul_rn(A.beta[slot_j], logl), lp) : -INFINITY;
         }
     } else if (A.mode == kModeSlots) {
         if (active && r == 0) {
-            A.st_logl[wk] = logl;
-            A.st_logprior[wk] = lp;
+            A.st_logl[slot_j] = logl;
+            A.st_logprior[slot_j] = lp;
         }
     } else {
         if (active && r == 0) {
-            const double beta = A.betas[t_idx];
+            const double beta = A.betas[bbase + t_idx];
             const double lpj = A.st_logprior[slot_j];
             const double llj = A.st_logl[slot_j];
             const double cur = lpj > -INFINITY ? __dadd_rn(__dmul_rn(beta, llj), lpj) : -INFINITY;
@@ -809,15 +831,17 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             if (acc) {
                 A.st_logl[slot_j] = logl;
                 A.st_logprior[slot_j] = lp;
-                A.accepted[t_idx * A.W + j_idx] += 1;
+                A.accepted[pbase + t_idx * A.W + j_idx] += 1;
             }
         }
         __syncthreads();
         if (active && misc[1] != 0.0) {
-            double* dst = A.st_theta + (size_t)slot_j * n_free;
+            double* dst = A.st_theta + (size_t)slot_j * ds;
             for (int d = r; d < n_free; d += L) dst[d] = thp[d];
         }
     }
+    if (A.work_counter == nullptr) break;
+    }   // items
 }
 
 }  // namespace emp

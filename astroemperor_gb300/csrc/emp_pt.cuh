@@ -52,6 +52,7 @@ __host__ __device__ inline Work carve_work(void* base) {
 
 struct SwapArgs {
     int T, W, D, nsteps;
+    int n_sys;                // systems (one CTA each when batched)
     const double* logl;
     int* members;
     double* betas;
@@ -87,12 +88,15 @@ __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
     return log(u32u(word)) < x;
 }
 
-// One CTA.  With SMEM the positions of every temperature (slot, logL) are
-// staged in shared memory and all random words are drawn up front by every
-// thread; the temperature pairs are then visited from the hottest down with
-// one barrier between pairs.  Accepted exchanges are logged for the swap
-// distance, which the record kernel computes across the whole GPU.
-template <bool SMEM>
+// One CTA per system.  With SMEM the positions of every temperature (slot,
+// logL) are staged in shared memory and all random words are drawn up front
+// by every thread; the temperature pairs are then visited from the hottest
+// down with one barrier between pairs.  For one system, accepted exchanges
+// are logged for the swap distance (computed across the GPU by the record
+// kernel) and the sweep counters advance here; for a batch (BATCH), system
+// s = blockIdx.x works on its own [T][W] block of every array with key
+// seed + s * 0x9E3779B97F4A7C15, and k_advance moves the shared counters.
+template <bool SMEM, bool BATCH>
 __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     __shared__ int s_cnt[kMaxTemps];
@@ -100,6 +104,7 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     __shared__ double s_ratio[kMaxTemps];
     __shared__ double s_invb[kMaxTemps];
     __shared__ double s_term[kMaxTemps];
+    __shared__ double s_bused[kMaxTemps];
 
     const int tid = threadIdx.x;
     const int nth = blockDim.x;
@@ -107,25 +112,31 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     const int T = S.T, W = S.W;
     const int TW = T * W;
     Work& wk = S.work;
+    const int sys = BATCH ? (int)blockIdx.x : 0;
+    const uint64_t seed = S.seed + (uint64_t)sys * 0x9E3779B97F4A7C15ULL;
+    int* members = S.members + (size_t)sys * TW;
+    double* betas = S.betas + (size_t)sys * T;
+    int* swaps_acc = S.swaps_accepted + (size_t)sys * T;
     double* s_ll = reinterpret_cast<double*>(sm_raw);              // [T*W] logL by position
     int* s_mem = reinterpret_cast<int*>(s_ll + (SMEM ? TW : 0));    // [T*W] slot by position
     uint32_t* s_u = reinterpret_cast<uint32_t*>(s_mem + (SMEM ? TW : 0));  // [T*W] words
 
     for (int t = tid; t < T; t += nth) {
-        wk.betas_used[t] = S.betas[t];
+        s_bused[t] = betas[t];
+        if (!BATCH) wk.betas_used[t] = betas[t];
         s_cnt[t] = 0;
         if (t >= 1) {
-            U4 pr = rng_draw(S.seed, (uint32_t)t, sweep, kRngSwapPerm);
+            U4 pr = rng_draw(seed, (uint32_t)t, sweep, kRngSwapPerm);
             s_perm[t][0] = (uint32_t)S.units[pr.x % (uint32_t)S.nunits];
             s_perm[t][1] = pr.y % (uint32_t)W;
         }
     }
     if (SMEM) {
         for (int k = tid; k < TW; k += nth) {
-            const int sl = S.members[k];
+            const int sl = members[k];
             s_mem[k] = sl;
             s_ll[k] = S.logl[sl];
-            s_u[k] = k >= W ? rng_draw(S.seed, (uint32_t)k, sweep, kRngSwapAcc).x : 0u;
+            s_u[k] = k >= W ? rng_draw(seed, (uint32_t)k, sweep, kRngSwapAcc).x : 0u;
         }
     }
     __syncthreads();
@@ -133,7 +144,7 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     for (int i = T - 1; i >= 1; --i) {
         const uint32_t m = s_perm[i][0];
         const uint32_t b = s_perm[i][1];
-        const double dbeta = S.betas[i - 1] - S.betas[i];
+        const double dbeta = betas[i - 1] - betas[i];
         for (int j = tid; j < W; j += nth) {
             const int jp = (int)(((uint64_t)m * (uint64_t)j + b) % (uint64_t)W);
             const int ia = i * W + j, ib = (i - 1) * W + jp;
@@ -143,30 +154,30 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
             if (SMEM) {
                 sa = s_mem[ia]; sb = s_mem[ib]; la = s_ll[ia]; lb = s_ll[ib]; word = s_u[ia];
             } else {
-                sa = S.members[ia]; sb = S.members[ib]; la = S.logl[sa]; lb = S.logl[sb];
-                word = rng_draw(S.seed, (uint32_t)ia, sweep, kRngSwapAcc).x;
+                sa = members[ia]; sb = members[ib]; la = S.logl[sa]; lb = S.logl[sb];
+                word = rng_draw(seed, (uint32_t)ia, sweep, kRngSwapAcc).x;
             }
             const double paccept = dbeta * (la - lb);
             if (log_uniform_below(word, paccept)) {
                 if (SMEM) {
                     s_mem[ia] = sb; s_mem[ib] = sa; s_ll[ia] = lb; s_ll[ib] = la;
                 } else {
-                    S.members[ia] = sb; S.members[ib] = sa;
+                    members[ia] = sb; members[ib] = sa;
                 }
                 const int k = atomicAdd(&s_cnt[i], 1);
-                wk.pairs[i * W + k] = make_int2(sa, sb);
+                if (!BATCH) wk.pairs[i * W + k] = make_int2(sa, sb);
             }
         }
         __syncthreads();
     }
     if (SMEM)
-        for (int k = tid; k < TW; k += nth) S.members[k] = s_mem[k];
+        for (int k = tid; k < TW; k += nth) members[k] = s_mem[k];
     for (int t = tid; t < T; t += nth) {
         const int c = t >= 1 ? s_cnt[t] : 0;
-        wk.pair_count[t] = c;
+        if (!BATCH) wk.pair_count[t] = c;
         if (t >= 1) {
             s_ratio[t - 1] = (double)c / (double)W;
-            S.swaps_accepted[t] += c;
+            swaps_acc[t] += c;
         }
     }
     __syncthreads();
@@ -174,7 +185,7 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     const bool adapt = S.adapt && T > 2;
     if (adapt) {
         const double kappa = S.adapt_tau / ((double)sweep + S.adapt_tau) / S.adapt_nu;
-        for (int t = tid; t < T - 1; t += nth) s_invb[t] = 1.0 / S.betas[t];
+        for (int t = tid; t < T - 1; t += nth) s_invb[t] = 1.0 / betas[t];
         __syncthreads();
         for (int k = tid; k < T - 2; k += nth) {
             const double dS = kappa * (s_ratio[k] - s_ratio[k + 1]);
@@ -189,16 +200,25 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
             }
         }
         __syncthreads();
-        for (int k = tid; k < T - 2; k += nth) S.betas[k + 1] = 1.0 / s_term[k];
+        for (int k = tid; k < T - 2; k += nth) betas[k + 1] = 1.0 / s_term[k];
     }
 
-    if (tid == 0) {
+    if (BATCH) {
+        // history rows [row][S][...]; k_advance moves the row counters
+        const int64_t row = S.n_rec[1];
+        const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
+        if (rec_sweep && row < S.cap) {
+            const int64_t rs = row * S.n_sys + sys;
+            if (S.beta_hist) for (int t = tid; t < T; t += nth) S.beta_hist[rs * T + t] = s_bused[t];
+            if (S.tsw_hist) for (int k = tid; k < T - 1; k += nth) S.tsw_hist[rs * (T - 1) + k] = s_ratio[k];
+        }
+    } else if (tid == 0) {
         // histories of this sweep (ladder used during the sweep)
         const int64_t row = S.n_rec[1];
         const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
         wk.rows[1] = -1;
         if (rec_sweep && row < S.cap) {
-            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = wk.betas_used[t];
+            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = s_bused[t];
             if (S.tsw_hist) for (int k = 0; k < T - 1; ++k) S.tsw_hist[row * (T - 1) + k] = s_ratio[k];
             if (S.have_smd) wk.rows[1] = row;
             S.n_rec[1] = row + 1;
@@ -295,6 +315,77 @@ __global__ void __launch_bounds__(256) k_record(RecArgs R) {
         }
         if (threadIdx.x == 0) *R.work.ticket = 0u;
     }
+}
+
+struct RecBatchArgs {
+    int S, T, W, D;
+    const double* theta;
+    const double* logl;
+    const double* logprior;
+    const int* members;
+    const double* betas;
+    const int64_t* counters;
+    const int64_t* n_rec;
+    int64_t cap;
+    int thin;
+    double* chain;        // [rows][S][W][D]
+    double* log_like;     // [rows][S][W]
+    double* log_prob;     // [rows][S][W]
+};
+
+// Cold-chain history row of a batch: walker w of system s at temperature 0.
+__global__ void __launch_bounds__(256) k_record_batch(RecBatchArgs R) {
+    const uint64_t sweep = (uint64_t)R.counters[1];
+    const bool rec_sweep = (R.thin <= 1) || ((int64_t)sweep % R.thin == (R.thin - 1));
+    const int64_t row = R.n_rec[0];
+    if (!rec_sweep || row >= R.cap) return;
+    const int64_t SW = (int64_t)R.S * R.W;
+    const int64_t TW = (int64_t)R.T * R.W;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (R.chain) {
+        const int64_t tot = SW * R.D;
+        double* dst = R.chain + row * tot;
+        for (int64_t idx = g0; idx < tot; idx += stride) {
+            const int64_t sw = idx / R.D;
+            const int d = (int)(idx - sw * R.D);
+            const int64_t s = sw / R.W;
+            const int64_t w = sw - s * R.W;
+            dst[idx] = R.theta[(int64_t)R.members[s * TW + w] * R.D + d];
+        }
+    }
+    for (int64_t idx = g0; idx < SW; idx += stride) {
+        const int64_t s = idx / R.W;
+        const int64_t w = idx - s * R.W;
+        const int slot = R.members[s * TW + w];
+        const double ll = R.logl[slot], lp = R.logprior[slot];
+        if (R.log_like) R.log_like[row * SW + idx] = ll;
+        if (R.log_prob)
+            R.log_prob[row * SW + idx] = lp > -INFINITY ? __dadd_rn(__dmul_rn(R.betas[s * R.T], ll), lp) : -INFINITY;
+    }
+}
+
+struct AdvArgs {
+    int64_t* counters;
+    int64_t* n_rec;
+    int64_t cap;
+    int thin;
+    int nsteps;
+    int record_chain;
+};
+
+// End of a batched sweep: the history rows and the step/sweep counters that
+// every system shares.
+__global__ void k_advance(AdvArgs A) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint64_t sweep = (uint64_t)A.counters[1];
+    const bool rec_sweep = (A.thin <= 1) || ((int64_t)sweep % A.thin == (A.thin - 1));
+    if (rec_sweep) {
+        if (A.n_rec[1] < A.cap) A.n_rec[1] += 1;
+        if (A.record_chain && A.n_rec[0] < A.cap) A.n_rec[0] += 1;
+    }
+    A.counters[0] += A.nsteps;
+    A.counters[1] += 1;
 }
 
 // CUDA-core throughput probe: independent FMA chains

@@ -79,9 +79,17 @@ struct GraphCache {
 }  // namespace
 
 struct emp_handle {
-    emp_model_desc md{};
-    emp_model_desc* md_dev = nullptr;
-    int n = 0;
+    emp_model_desc md{};       // system 0 (the only one unless batched)
+    emp_model_desc* md_dev = nullptr;   // [n_sys]
+    int n = 0;                 // epochs of the largest system (tile size)
+    int n_typ = 0;             // median epochs per system (default lanes)
+    int n_sys = 1;
+    int lay[5] = {};           // largest n_full, n_free, n_planets, n_ins, acc_order
+    const int64_t* sys_off = nullptr;   // device [S+1] epoch offsets (batch only)
+    const double* sys_t0 = nullptr;     // device [S] acceleration origins (batch only)
+    const int* sys_order = nullptr;     // device [S] costliest system first (batch only)
+    int persist_grid[2][6] = {};
+    int persist_smem[2][6] = {};
     int q = 0;                 // MA order evaluated on device
     void* dbuf = nullptr;
     DevData dd{};
@@ -92,6 +100,7 @@ struct emp_handle {
     GraphCache gc;
     bool attr_done[2][4][6] = {};
     bool swap_attr = false;
+    bool swap_attr_batch = false;
 };
 
 // dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
@@ -202,18 +211,52 @@ int pick_tile(const emp_handle* h, int prec, int L, int G, Smem& lay) {
     int t = round_L(std::min(want, h->n));
     t = std::max(t, L);
     for (;;) {
-        lay.build(prec, h->q, L, G, t, h->md.n_full, h->md.n_free, h->md.n_planets, h->md.n_ins,
-                  h->md.acc_order);
+        lay.build(prec, h->q, L, G, t, h->lay[0], h->lay[1], h->lay[2], h->lay[3], h->lay[4]);
         if (lay.total <= 200 * 1024 || t <= L) break;
         t = std::max(L, round_L(t / 2));
     }
     return t;
 }
 
-int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s) {
+int handle_L(const emp_handle* h, int prec) {
+    return h->L[prec] > 0 ? h->L[prec] : pick_default_L(prec, h->n_typ);
+}
+
+// Kernel attributes (and, for a batch, the persistent grid) set up outside
+// any stream capture.
+int prepare_eval(emp_handle* h, int prec) {
+    const int L = handle_L(h, prec);
+    const int li = lanes_index(L);
+    if (li < 0) return fail(EMP_E_INVALID, "lanes per walker %d not built", L);
+    KFn fn = prec == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
+    if (!fn) return fail(EMP_E_UNSUPPORTED, "no kernel for q=%d L=%d", h->q, L);
+    if (!h->attr_done[prec][h->q][li]) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      227 * 1024));
+        h->attr_done[prec][h->q][li] = true;
+    }
+    if (h->n_sys > 1) {
+        const int NT = L > 128 ? L : 128;
+        Smem lay;
+        pick_tile(h, prec, L, NT / L, lay);
+        if (h->persist_smem[prec][li] != lay.total || h->persist_grid[prec][li] <= 0) {
+            int dev = 0, sms = 0, nb = 0;
+            CUDA_TRY(cudaGetDevice(&dev));
+            CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)fn, NT, lay.total));
+            h->persist_grid[prec][li] = std::max(1, nb) * sms;
+            h->persist_smem[prec][li] = lay.total;
+        }
+    }
+    return EMP_OK;
+}
+
+// counter: for a batch, the int that CTAs of a persistent launch claim
+// items from (zeroed here, in stream order); null launches one CTA per item
+int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* counter = nullptr) {
     if (prec != EMP_PREC_FP64 && prec != EMP_PREC_MIXED)
         return fail(EMP_E_INVALID, "precision %d unknown", prec);
-    int L = h->L[prec] > 0 ? h->L[prec] : pick_default_L(prec, h->n);
+    int L = handle_L(h, prec);
     int li = lanes_index(L);
     if (li < 0) return fail(EMP_E_INVALID, "lanes per walker %d not built", L);
     int NT = L > 128 ? L : 128;
@@ -224,16 +267,34 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s) {
         return fail(EMP_E_SIZE, "shared memory %d B exceeds 227 KB", lay.total);
     KFn fn = prec == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
     if (!fn) return fail(EMP_E_UNSUPPORTED, "no kernel for q=%d L=%d", h->q, L);
-    if (!h->attr_done[prec][h->q][li]) {
-        CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      227 * 1024));
-        h->attr_done[prec][h->q][li] = true;
+    if (!h->attr_done[prec][h->q][li] || (h->n_sys > 1 && h->persist_smem[prec][li] != lay.total)) {
+        int rc = prepare_eval(h, prec);
+        if (rc) return rc;
     }
     a.md = h->md_dev;
     a.d = h->dd;
     a.tile = tile;
+    a.lay_full = h->lay[0];
+    a.lay_free = h->lay[1];
+    a.lay_planets = h->lay[2];
+    a.lay_ins = h->lay[3];
+    a.lay_acc = h->lay[4];
+    a.dstride = h->lay[1];
+    a.n_sys = h->n_sys;
+    a.sys_off = h->sys_off;
+    a.sys_t0 = h->sys_t0;
+    a.sys_order = h->sys_order;
     if (a.nwalk <= 0) return EMP_OK;
-    int grid = (a.nwalk + G - 1) / G;
+    a.cps = (a.nwalk + G - 1) / G;
+    const int64_t items = (int64_t)a.cps * h->n_sys;
+    if (items > 0x7fffffff) return fail(EMP_E_SIZE, "%lld CTA items exceed 2^31-1", (long long)items);
+    int grid = (int)items;
+    a.work_counter = nullptr;
+    if (counter != nullptr && h->n_sys > 1) {
+        a.work_counter = reinterpret_cast<int*>(counter);
+        grid = (int)std::min<int64_t>(items, h->persist_grid[prec][li]);
+        CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
+    }
     fn<<<grid, NT, lay.total, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
@@ -246,8 +307,14 @@ int check_state(const emp_handle* h, const emp_pt_state* st) {
         return fail(EMP_E_SIZE, "ntemps=%d outside [1, %d]", st->ntemps, kMaxTemps);
     if (st->nwalkers < 2 || (st->nwalkers & 1))
         return fail(EMP_E_INVALID, "nwalkers=%d must be even and >= 2", st->nwalkers);
-    if (st->ndim != h->md.n_free)
-        return fail(EMP_E_INVALID, "state ndim=%d but model has %d free parameters", st->ndim, h->md.n_free);
+    const int nsys = st->n_systems <= 0 ? 1 : st->n_systems;
+    if (nsys != h->n_sys)
+        return fail(EMP_E_INVALID, "state holds %d systems, handle %d", nsys, h->n_sys);
+    if ((int64_t)nsys * st->ntemps * st->nwalkers > 0x7fffffff)
+        return fail(EMP_E_SIZE, "systems*ntemps*nwalkers exceeds 2^31-1");
+    if (st->ndim != h->lay[1])
+        return fail(EMP_E_INVALID, "state ndim=%d but the model%s %d free parameters", st->ndim,
+                    h->n_sys > 1 ? "s' largest free dimension is" : " has", h->lay[1]);
     if (st->nsteps < 1) return fail(EMP_E_INVALID, "nsteps=%d < 1", st->nsteps);
     if (!st->theta || !st->logl || !st->logprior || !st->members || !st->betas || !st->counters ||
         !st->accepted || !st->swaps_accepted || !st->perm_units)
@@ -272,6 +339,8 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                   cudaStream_t s, int* nkern) {
     int rc;
     int kcount = 0;
+    const bool batch = h->n_sys > 1;
+    Work work = carve_work(st->work);
     for (int step = 0; step < st->nsteps; ++step) {
         for (int half = 0; half < 2; ++half) {
             KArgs a{};
@@ -285,22 +354,24 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
             a.counters = st->counters;
             a.accepted = st->accepted;
             a.W = st->nwalkers;
+            a.T = st->ntemps;
             a.half = half;
             a.step_in_sweep = step;
             a.seed = st->seed;
             a.a = st->a;
-            if ((rc = launch_eval(h, st->precision, a, s))) return rc;
+            if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr))) return rc;
             ++kcount;
         }
     }
     SwapArgs S{};
     S.T = st->ntemps; S.W = st->nwalkers; S.D = st->ndim; S.nsteps = st->nsteps;
+    S.n_sys = h->n_sys;
     S.logl = st->logl; S.members = st->members; S.betas = st->betas;
     S.counters = st->counters; S.swaps_accepted = st->swaps_accepted;
     S.units = st->perm_units; S.nunits = st->n_perm_units;
     S.adapt = st->adapt; S.adapt_mode = st->adapt_mode;
     S.adapt_tau = st->adapt_tau; S.adapt_nu = st->adapt_nu; S.seed = st->seed;
-    S.work = carve_work(st->work);
+    S.work = work;
     const bool have_rec = rec && rec->n_recorded;
     S.beta_hist = have_rec ? rec->beta_history : nullptr;
     S.tsw_hist = have_rec ? rec->tsw_history : nullptr;
@@ -309,17 +380,57 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
     S.cap = have_rec ? rec->capacity : 0;
     S.thin = have_rec ? std::max(1, rec->thin) : 1;
     S.record_chain = have_rec && (rec->chain || rec->log_like || rec->log_prob);
-    const int nth = 1024;
     const size_t swap_smem = (size_t)st->ntemps * st->nwalkers * 16;
+    if (batch) {
+        // one CTA per system; threads cover a temperature's walkers
+        const int nthb = std::min(1024, std::max(128, (st->nwalkers + 31) / 32 * 32));
+        if (swap_smem <= kSwapSmemMax) {
+            if (!h->swap_attr_batch) {
+                CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, true>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+                h->swap_attr_batch = true;
+            }
+            k_swap<true, true><<<h->n_sys, nthb, swap_smem, s>>>(S);
+        } else {
+            k_swap<false, true><<<h->n_sys, nthb, 0, s>>>(S);
+        }
+        g_launches.fetch_add(1);
+        ++kcount;
+        CUDA_TRY(cudaGetLastError());
+        if (S.record_chain) {
+            RecBatchArgs R{};
+            R.S = h->n_sys; R.T = st->ntemps; R.W = st->nwalkers; R.D = st->ndim;
+            R.theta = st->theta; R.logl = st->logl; R.logprior = st->logprior;
+            R.members = st->members; R.betas = st->betas; R.counters = st->counters;
+            R.n_rec = S.n_rec; R.cap = S.cap; R.thin = S.thin;
+            R.chain = rec->chain; R.log_like = rec->log_like; R.log_prob = rec->log_prob;
+            const int64_t tot = (int64_t)h->n_sys * st->nwalkers * (rec->chain ? st->ndim : 1);
+            const int grid = (int)std::min<int64_t>(std::max<int64_t>(1, (tot + 255) / 256), 152 * 8);
+            k_record_batch<<<grid, 256, 0, s>>>(R);
+            g_launches.fetch_add(1);
+            ++kcount;
+            CUDA_TRY(cudaGetLastError());
+        }
+        AdvArgs V{};
+        V.counters = st->counters; V.n_rec = S.n_rec; V.cap = S.cap; V.thin = S.thin;
+        V.nsteps = st->nsteps; V.record_chain = S.record_chain;
+        k_advance<<<1, 32, 0, s>>>(V);
+        g_launches.fetch_add(1);
+        ++kcount;
+        CUDA_TRY(cudaGetLastError());
+        if (nkern) *nkern = kcount;
+        return EMP_OK;
+    }
+    const int nth = 1024;
     if (swap_smem <= kSwapSmemMax) {
         if (!h->swap_attr) {
-            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true>,
+            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
             h->swap_attr = true;
         }
-        k_swap<true><<<1, nth, swap_smem, s>>>(S);
+        k_swap<true, false><<<1, nth, swap_smem, s>>>(S);
     } else {
-        k_swap<false><<<1, nth, 0, s>>>(S);
+        k_swap<false, false><<<1, nth, 0, s>>>(S);
     }
     g_launches.fetch_add(1);
     ++kcount;
@@ -361,82 +472,173 @@ const char* emp_last_error_string(void) { return g_err; }
 
 int64_t emp_launch_count(void) { return g_launches.load(); }
 
-int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_handle** out) {
-    if (!out) return fail(EMP_E_INVALID, "out is NULL");
-    *out = nullptr;
-    int rc = validate_model(model);
-    if (rc) return rc;
-    if (!data) return fail(EMP_E_INVALID, "dataset descriptor is NULL");
-    if (data->n_systems != 1)
-        return fail(EMP_E_UNSUPPORTED, "n_systems=%d: this entry takes one system", data->n_systems);
-    if (!data->offsets || !data->t || !data->y || !data->yerr || !data->inst)
-        return fail(EMP_E_INVALID, "a dataset array is NULL");
-    const int64_t n64 = data->offsets[1] - data->offsets[0];
-    if (n64 <= 0) return fail(EMP_E_INVALID, "system has %lld epochs", (long long)n64);
-    if (n64 > (1 << 26)) return fail(EMP_E_SIZE, "%lld epochs exceed 2^26", (long long)n64);
-    const int n = (int)n64;
-    const int64_t o = data->offsets[0];
+}  // extern "C"
+
+namespace {
+
+// Host preprocessing of one system's epochs into the device layout: time
+// order, or instrument-grouped time order when each instrument carries its
+// own MA series; squared errors; the FP32 hi/lo split of the times; the lag
+// distances of the MA recurrence (+inf across a series start).
+struct HostData {
+    std::vector<double> t, y, s2, dt;
+    std::vector<float> t_hi, t_lo, y32, s2_32, dt32;
+    std::vector<int> inst, orig;
+    void reserve(size_t n, int q) {
+        t.reserve(n); y.reserve(n); s2.reserve(n); t_hi.reserve(n); t_lo.reserve(n);
+        y32.reserve(n); s2_32.reserve(n); inst.reserve(n); orig.reserve(n);
+        (void)q;
+    }
+};
+
+int check_system(const emp_model_desc* model, const emp_dataset_desc* data, int s, int64_t* n_out) {
+    const int64_t n64 = data->offsets[s + 1] - data->offsets[s];
+    if (n64 <= 0) return fail(EMP_E_INVALID, "system %d has %lld epochs", s, (long long)n64);
+    if (n64 > (1 << 26)) return fail(EMP_E_SIZE, "system %d: %lld epochs exceed 2^26", s, (long long)n64);
+    const int64_t o = data->offsets[s];
     const double* t = data->t + o;
     const double* y = data->y + o;
     const double* ye = data->yerr + o;
     const int32_t* in = data->inst + o;
-    for (int i = 0; i < n; ++i) {
+    for (int64_t i = 0; i < n64; ++i) {
         if (!isfinite(t[i]) || !isfinite(y[i]) || !isfinite(ye[i]))
-            return fail(EMP_E_INVALID, "epoch %d has a non-finite value", i);
+            return fail(EMP_E_INVALID, "system %d epoch %lld has a non-finite value", s, (long long)i);
         if (in[i] < 1 || in[i] > model->n_ins)
-            return fail(EMP_E_INVALID, "epoch %d: instrument %d outside 1..%d", i, in[i], model->n_ins);
-        if (i > 0 && t[i] < t[i - 1]) return fail(EMP_E_INVALID, "times not sorted at epoch %d", i);
+            return fail(EMP_E_INVALID, "system %d epoch %lld: instrument %d outside 1..%d", s, (long long)i,
+                        in[i], model->n_ins);
+        if (i > 0 && t[i] < t[i - 1])
+            return fail(EMP_E_INVALID, "system %d: times not sorted at epoch %lld", s, (long long)i);
     }
+    *n_out = n64;
+    return EMP_OK;
+}
 
-    emp_handle* h = new (std::nothrow) emp_handle();
-    if (!h) return fail(EMP_E_INVALID, "out of host memory");
-    h->md = *model;
-    h->n = n;
-    const bool ma_on = model->ma_order > 0 && (model->ma_global || !model->ma_quirk);
-    h->q = ma_on ? model->ma_order : 0;
-    const bool group_by_ins = ma_on && !model->ma_global;
+int ma_order_on_device(const emp_model_desc* m) {
+    const bool ma_on = m->ma_order > 0 && (m->ma_global || !m->ma_quirk);
+    return ma_on ? m->ma_order : 0;
+}
 
-    // epoch order: per-instrument MA needs each instrument's subsequence
-    // contiguous (time order kept inside); otherwise time order.
+void append_system(const emp_model_desc* model, const emp_dataset_desc* data, int s, int q,
+                   HostData& H, std::vector<std::vector<double>>& dts) {
+    const int64_t o = data->offsets[s];
+    const int n = (int)(data->offsets[s + 1] - o);
+    const double* t = data->t + o;
+    const double* y = data->y + o;
+    const double* ye = data->yerr + o;
+    const int32_t* in = data->inst + o;
+    const bool group_by_ins = q > 0 && !model->ma_global;
     std::vector<int> order(n);
     std::iota(order.begin(), order.end(), 0);
     if (group_by_ins)
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return in[a] < in[b]; });
-    const int q = h->q;
-    std::vector<double> ht(n), hy(n), hs2(n), hdt((size_t)std::max(q, 1) * n);
-    std::vector<float> tf_hi(n), tf_lo(n), yf(n), s2f(n), dtf((size_t)std::max(q, 1) * n);
-    std::vector<int> hin(n);
+    const size_t base = H.t.size();
     for (int i = 0; i < n; ++i) {
-        int k = order[i];
-        ht[i] = t[k];
-        hy[i] = y[k];
-        hs2[i] = ye[k] * ye[k];
-        hin[i] = in[k] - 1;
-        tf_hi[i] = (float)t[k];
-        tf_lo[i] = (float)(t[k] - (double)tf_hi[i]);
-        yf[i] = (float)y[k];
-        s2f[i] = (float)hs2[i];
+        const int k = order[i];
+        H.t.push_back(t[k]);
+        H.y.push_back(y[k]);
+        H.s2.push_back(ye[k] * ye[k]);
+        H.inst.push_back(in[k] - 1);
+        const float hi = (float)t[k];
+        H.t_hi.push_back(hi);
+        H.t_lo.push_back((float)(t[k] - (double)hi));
+        H.y32.push_back((float)y[k]);
+        H.s2_32.push_back((float)(ye[k] * ye[k]));
+        H.orig.push_back(k);
     }
     for (int c = 0; c < q; ++c) {
         for (int i = 0; i < n; ++i) {
-            // predecessor at lag c+1 inside the same sequence (instrument or global)
-            int lag = c + 1;
+            // predecessor at lag c+1 inside the same series (instrument or global)
+            const int lag = c + 1;
             double v = INFINITY;
-            if (i - lag >= 0 && (!group_by_ins || hin[i - lag] == hin[i])) v = fabs(ht[i] - ht[i - lag]);
-            hdt[(size_t)c * n + i] = v;
-            dtf[(size_t)c * n + i] = (float)v;
+            if (i - lag >= 0 && (!group_by_ins || H.inst[base + i - lag] == H.inst[base + i]))
+                v = fabs(H.t[base + i] - H.t[base + i - lag]);
+            dts[c].push_back(v);
         }
     }
-    // one device allocation for the dataset + descriptor + scratch
-    size_t qn = (size_t)std::max(q, 1) * n;
+}
+
+int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* data, emp_handle** out) {
+    if (!out) return fail(EMP_E_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!models) return fail(EMP_E_INVALID, "model descriptor is NULL");
+    if (!data) return fail(EMP_E_INVALID, "dataset descriptor is NULL");
+    if (!data->offsets || !data->t || !data->y || !data->yerr || !data->inst)
+        return fail(EMP_E_INVALID, "a dataset array is NULL");
+    int rc;
+    const int q = ma_order_on_device(&models[0]);
+    std::vector<int64_t> nsys(S);
+    int64_t total = 0;
+    int lay[5] = {0, 0, 0, 0, 0};
+    for (int s = 0; s < S; ++s) {
+        const emp_model_desc* m = &models[s];
+        if ((rc = validate_model(m))) {
+            if (S > 1) {
+                char tmp[600];
+                snprintf(tmp, sizeof(tmp), "system %d: %s", s, g_err);
+                return fail(rc, "%s", tmp);
+            }
+            return rc;
+        }
+        if (ma_order_on_device(m) != q)
+            return fail(EMP_E_UNSUPPORTED, "system %d: MA order %d differs from system 0's %d", s,
+                        ma_order_on_device(m), q);
+        if ((rc = check_system(m, data, s, &nsys[s]))) return rc;
+        total += nsys[s];
+        lay[0] = std::max(lay[0], m->n_full);
+        lay[1] = std::max(lay[1], m->n_free);
+        lay[2] = std::max(lay[2], m->n_planets);
+        lay[3] = std::max(lay[3], m->n_ins);
+        lay[4] = std::max(lay[4], m->acc_order);
+    }
+    if (total > (1 << 30)) return fail(EMP_E_SIZE, "%lld epochs in total exceed 2^30", (long long)total);
+    const int n = (int)total;
+
+    HostData H;
+    H.reserve((size_t)n, q);
+    std::vector<std::vector<double>> dts(std::max(q, 1));
+    std::vector<int64_t> off(S + 1, 0);
+    std::vector<double> t0(S);
+    for (int s = 0; s < S; ++s) {
+        off[s] = (int64_t)H.t.size();
+        t0[s] = data->t[data->offsets[s]];
+        append_system(&models[s], data, s, q, H, dts);
+    }
+    off[S] = (int64_t)H.t.size();
+    const size_t qn = (size_t)std::max(q, 1) * n;
+    std::vector<double> hdt(qn, INFINITY);
+    std::vector<float> dtf(qn, INFINITY);
+    for (int c = 0; c < q; ++c)
+        for (int i = 0; i < n; ++i) {
+            hdt[(size_t)c * n + i] = dts[c][i];
+            dtf[(size_t)c * n + i] = (float)dts[c][i];
+        }
+    // costliest systems first: epochs x (planets + 1)
+    std::vector<int> sorder(S);
+    std::iota(sorder.begin(), sorder.end(), 0);
+    std::stable_sort(sorder.begin(), sorder.end(), [&](int a, int b) {
+        return nsys[a] * (models[a].n_planets + 1) > nsys[b] * (models[b].n_planets + 1);
+    });
+    std::vector<int64_t> sorted_n(nsys);
+    std::sort(sorted_n.begin(), sorted_n.end());
+
+    emp_handle* h = new (std::nothrow) emp_handle();
+    if (!h) return fail(EMP_E_INVALID, "out of host memory");
+    h->md = models[0];
+    h->n = (int)sorted_n.back();
+    h->n_typ = (int)sorted_n[S / 2];
+    h->n_sys = S;
+    for (int k = 0; k < 5; ++k) h->lay[k] = lay[k];
+    h->q = q;
+
+    // one device allocation for the dataset, descriptors and system tables
     size_t bytes = 0;
-    auto take = [&](size_t b) { size_t off = bytes; bytes += (b + 255) & ~(size_t)255; return off; };
-    size_t o_t = take(8 * (size_t)n), o_y = take(8 * (size_t)n), o_s2 = take(8 * (size_t)n);
-    size_t o_dt = take(8 * qn);
-    size_t o_th = take(4 * (size_t)n), o_tl = take(4 * (size_t)n), o_yf = take(4 * (size_t)n);
-    size_t o_sf = take(4 * (size_t)n), o_dtf = take(4 * qn), o_in = take(4 * (size_t)n);
-    size_t o_perm = take(4 * (size_t)n);
-    size_t o_md = take(sizeof(emp_model_desc));
+    auto take = [&](size_t b) { size_t o = bytes; bytes += (b + 255) & ~(size_t)255; return o; };
+    const size_t N8 = 8 * (size_t)n, N4 = 4 * (size_t)n;
+    size_t o_t = take(N8), o_y = take(N8), o_s2 = take(N8), o_dt = take(8 * qn);
+    size_t o_th = take(N4), o_tl = take(N4), o_yf = take(N4), o_sf = take(N4), o_dtf = take(4 * qn);
+    size_t o_in = take(N4), o_perm = take(N4);
+    size_t o_md = take(sizeof(emp_model_desc) * (size_t)S);
+    size_t o_off = take(8 * (size_t)(S + 1)), o_t0 = take(8 * (size_t)S), o_ord = take(4 * (size_t)S);
     cudaError_t e = cudaMalloc(&h->dbuf, bytes);
     if (e != cudaSuccess) {
         delete h;
@@ -444,11 +646,12 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_ha
     }
     char* b = (char*)h->dbuf;
     struct Cp { size_t off; const void* src; size_t n; } cps[] = {
-        {o_t, ht.data(), 8 * (size_t)n}, {o_y, hy.data(), 8 * (size_t)n}, {o_s2, hs2.data(), 8 * (size_t)n},
-        {o_dt, hdt.data(), 8 * qn}, {o_th, tf_hi.data(), 4 * (size_t)n}, {o_tl, tf_lo.data(), 4 * (size_t)n},
-        {o_yf, yf.data(), 4 * (size_t)n}, {o_sf, s2f.data(), 4 * (size_t)n}, {o_dtf, dtf.data(), 4 * qn},
-        {o_in, hin.data(), 4 * (size_t)n}, {o_perm, order.data(), 4 * (size_t)n},
-        {o_md, model, sizeof(emp_model_desc)}};
+        {o_t, H.t.data(), N8}, {o_y, H.y.data(), N8}, {o_s2, H.s2.data(), N8}, {o_dt, hdt.data(), 8 * qn},
+        {o_th, H.t_hi.data(), N4}, {o_tl, H.t_lo.data(), N4}, {o_yf, H.y32.data(), N4},
+        {o_sf, H.s2_32.data(), N4}, {o_dtf, dtf.data(), 4 * qn}, {o_in, H.inst.data(), N4},
+        {o_perm, H.orig.data(), N4}, {o_md, models, sizeof(emp_model_desc) * (size_t)S},
+        {o_off, off.data(), 8 * (size_t)(S + 1)}, {o_t0, t0.data(), 8 * (size_t)S},
+        {o_ord, sorder.data(), 4 * (size_t)S}};
     for (auto& c : cps) {
         e = cudaMemcpy(b + c.off, c.src, c.n, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
@@ -459,9 +662,14 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_ha
     }
     h->md_dev = (emp_model_desc*)(b + o_md);
     h->dev2orig = (int*)(b + o_perm);
+    if (S > 1) {
+        h->sys_off = (const int64_t*)(b + o_off);
+        h->sys_t0 = (const double*)(b + o_t0);
+        h->sys_order = (const int*)(b + o_ord);
+    }
     h->dd.n = n;
     h->dd.q = q;
-    h->dd.t0 = t[0];
+    h->dd.t0 = t0[0];
     h->dd.t = (const double*)(b + o_t);
     h->dd.y = (const double*)(b + o_y);
     h->dd.s2 = (const double*)(b + o_s2);
@@ -474,6 +682,31 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_ha
     h->dd.inst = (const int*)(b + o_in);
     *out = h;
     return EMP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int emp_create(const emp_model_desc* model, const emp_dataset_desc* data, emp_handle** out) {
+    if (out) *out = nullptr;
+    if (data && data->n_systems != 1)
+        return fail(EMP_E_UNSUPPORTED, "n_systems=%d: this entry takes one system (emp_create_batch "
+                    "takes many)", data->n_systems);
+    return create_impl(model, 1, data, out);
+}
+
+int emp_create_batch(const emp_model_desc* models, const emp_dataset_desc* data, emp_handle** out) {
+    if (out) *out = nullptr;
+    if (!data) return fail(EMP_E_INVALID, "dataset descriptor is NULL");
+    if (data->n_systems < 1 || data->n_systems > (1 << 20))
+        return fail(EMP_E_SIZE, "n_systems=%d outside [1, 2^20]", data->n_systems);
+    return create_impl(models, data->n_systems, data, out);
+}
+
+int emp_num_systems(emp_handle* h) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    return h->n_sys;
 }
 
 int emp_destroy(emp_handle* h) {
@@ -503,7 +736,7 @@ int emp_get_launch(emp_handle* h, int precision, int* lanes_per_walker, int* til
     if (!h || !lanes_per_walker || !tile_epochs) return fail(EMP_E_INVALID, "NULL argument");
     if (precision != EMP_PREC_FP64 && precision != EMP_PREC_MIXED)
         return fail(EMP_E_INVALID, "precision %d unknown", precision);
-    int L = h->L[precision] > 0 ? h->L[precision] : pick_default_L(precision, h->n);
+    int L = handle_L(h, precision);
     int NT = L > 128 ? L : 128;
     Smem lay;
     *lanes_per_walker = L;
@@ -519,7 +752,8 @@ int emp_logpost(emp_handle* h, const double* theta, int B, const int32_t* system
     if (B == 0) return EMP_OK;
     if (!theta || !logl || !logprior) return fail(EMP_E_INVALID, "theta/logl/logprior NULL");
     if (system_of != nullptr)
-        return fail(EMP_E_UNSUPPORTED, "system_of is for ragged datasets (one system loaded)");
+        return fail(EMP_E_UNSUPPORTED, "system_of must be NULL (a batch handle takes B rows per system)");
+    if ((int64_t)B * h->n_sys > 0x7fffffff) return fail(EMP_E_SIZE, "B*systems exceeds 2^31-1");
     KArgs a{};
     a.mode = kModeLogpost;
     a.nwalk = B;
@@ -538,6 +772,7 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, dou
     if (B == 0) return EMP_OK;
     if (B > 65535) return fail(EMP_E_SIZE, "B=%d > 65535", B);
     if (!theta || !model || !err2) return fail(EMP_E_INVALID, "NULL argument");
+    if (h->n_sys > 1) return fail(EMP_E_UNSUPPORTED, "model evaluation takes a one-system handle");
     cudaStream_t s = (cudaStream_t)stream;
     const emp_model_desc& m = h->md;
     size_t sm = 8 * ((size_t)m.n_full + 8 * std::max(m.n_planets, 1) + 2 * m.n_ins + std::max(m.acc_order, 1));
@@ -560,6 +795,7 @@ int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, do
     if (B == 0) return EMP_OK;
     if (!theta || !logl || !logprior || !grad_logl || !grad_logprior)
         return fail(EMP_E_INVALID, "a NULL argument");
+    if (h->n_sys > 1) return fail(EMP_E_UNSUPPORTED, "the gradient takes a one-system handle");
     const emp_model_desc& m = h->md;
     for (int p = 0; p < m.n_planets; ++p)
         if (m.kep_param[p] != 0 && m.kep_param[p] != 1)
@@ -618,6 +854,8 @@ int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream) {
     KArgs a{};
     a.mode = kModeSlots;
     a.nwalk = st->ntemps * st->nwalkers;
+    a.T = st->ntemps;
+    a.W = st->nwalkers;
     a.st_theta = st->theta;
     a.st_logl = st->logl;
     a.st_logprior = st->logprior;
@@ -725,20 +963,18 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, 
     if (!(gc.valid && gc.stream == ls && same_state(gc.st, *st) && gc.has_rec == has_rec &&
           (!has_rec || same_rec(gc.rec, rcopy)))) {
         gc.reset();
-        // first eager sweep sets kernel attributes outside capture
-        // (capture forbids cudaFuncSetAttribute side effects on some drivers)
-        int L = h->L[st->precision] > 0 ? h->L[st->precision] : pick_default_L(st->precision, h->n);
-        int li = lanes_index(L);
-        KFn fn = st->precision == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
-        if (fn && !h->attr_done[st->precision][h->q][li]) {
-            CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          227 * 1024));
-            h->attr_done[st->precision][h->q][li] = true;
-        }
+        // kernel attributes and the persistent grid are set up outside the
+        // capture (it forbids cudaFuncSetAttribute side effects on some drivers)
+        if ((rc = prepare_eval(h, st->precision))) return rc;
         if (!h->swap_attr) {
-            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true>,
+            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
             h->swap_attr = true;
+        }
+        if (!h->swap_attr_batch) {
+            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+            h->swap_attr_batch = true;
         }
         CUDA_TRY(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
         int nk = 0;

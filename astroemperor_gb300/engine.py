@@ -306,6 +306,7 @@ class PTSampler:
         st.adapt_tau, st.adapt_nu, st.adapt_mode = self.adapt_tau, self.adapt_nu, self.adapt_mode
         st.precision = self.precision
         st.work, st.work_bytes = _ptr(self.work), int(self.work.numel())
+        st.n_systems = 1
         return st
 
     def _record_struct(self) -> N.EmpPtRecord:

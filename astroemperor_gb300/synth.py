@@ -12,6 +12,10 @@ go through the same preprocessing as EMPEROR's ``DataWrapper``.
 * ``c4`` -- 5 Keplerians, 3 instruments, MA(1), N=4096.
 * ``c5`` -- 7 Keplerians, 4 instruments, MA(2), N=16384 over 10000 d,
   T x W = 32 x 1024.
+* ``c3`` -- a ragged batch of independent systems (``make_ragged``): epoch
+  counts log-uniform in [50, 2000] over 1000-5000 d, 1-4 Keplerians with P
+  log-uniform in [1, 3000] d, K log-uniform in [0.5, 100] m/s,
+  e ~ Beta(0.87, 3.03), 1-3 instruments; T x W = 8 x 64, 1000 sweeps.
 """
 from __future__ import annotations
 
@@ -185,3 +189,71 @@ def truth_theta(model, truth, data, parameterisation=1):
                 for c in range(b.moav):
                     vals += [truth['ma']['phi'][c], truth['ma']['tau'][c]]
     return np.array(vals, dtype=np.float64)
+
+
+RAGGED = dict(n_systems=4096, n_range=(50, 2000), span=(1000.0, 5000.0), planets=(1, 4),
+              P=(1.0, 3000.0), K=(0.5, 100.0), ins=(1, 3), setup=[8, 64, 1000, 1])
+
+
+def ragged_system(seed: int, s: int):
+    """(instruments, truth) of system ``s`` of the ragged batch: its own
+    generator keyed by (seed, s), so any subset regenerates identically."""
+    cfg = RAGGED
+    rng = np.random.default_rng([int(seed), int(s)])
+    lo, hi = cfg['n_range']
+    n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+    span = rng.uniform(*cfg['span'])
+    kp = int(rng.integers(cfg['planets'][0], cfg['planets'][1] + 1))
+    nins = int(rng.integers(cfg['ins'][0], cfg['ins'][1] + 1))
+    P = np.sort(np.exp(rng.uniform(np.log(cfg['P'][0]), np.log(cfg['P'][1]), kp)))
+    K = np.exp(rng.uniform(np.log(cfg['K'][0]), np.log(cfg['K'][1]), kp))
+    e = np.minimum(rng.beta(0.87, 3.03, kp), 0.8)
+    w = rng.uniform(0, 2 * np.pi, kp)
+    phase = rng.uniform(0, 2 * np.pi, kp)
+    t = BJD0 + np.sort(rng.uniform(0, span, n))
+    tr = t - t[0]
+    rv = np.zeros(n)
+    for p in range(kp):
+        rv += keplerian(tr, P[p], K[p], phase[p], e[p], w[p])
+    labels = np.concatenate([np.arange(nins), rng.integers(0, nins, n - nins)])
+    rng.shuffle(labels)
+    sig = rng.uniform(1.5, 3.0, n)
+    offsets = list(rng.uniform(-30, 30, nins))
+    jitters = list(rng.uniform(0.5, 3.0, nins))
+    instruments = []
+    for k in range(nins):
+        m = labels == k
+        tot = np.sqrt(sig[m] ** 2 + jitters[k] ** 2)
+        instruments.append(np.column_stack([t[m], rv[m] + offsets[k] + rng.normal(0.0, tot), sig[m]]))
+    truth = dict(P=list(P), K=list(K), phase=list(phase), e=list(e), w=list(w), offsets=offsets,
+                 jitters=jitters, ma=None)
+    return instruments, truth
+
+
+def ragged_model(seed: int, s: int):
+    """(ReddModel, RVData, truth-theta) of system ``s``: Keplerians
+    (parameterisation 1, period box +-10% around the generating period),
+    offsets and jitters with EMPEROR's default priors."""
+    instruments, truth = ragged_system(seed, s)
+    data = preprocess_instruments(instruments, [f'INS{k + 1}' for k in range(len(instruments))])
+    ss = SmartSetter(data)
+    blocks = []
+    for p in range(len(truth['P'])):
+        kb = KeplerianBlock(1, p + 1)
+        ss(kb)
+        kb[0].limits = [truth['P'][p] * 0.9, truth['P'][p] * 1.1]
+        blocks.append(kb)
+    ob = OffsetBlock(data.nins)
+    ss(ob)
+    blocks.append(ob)
+    jb = JitterBlock(data.nins)
+    ss(jb, jit_prargs=(5, 5))
+    blocks.append(jb)
+    model = ReddModel(blocks, data)
+    return model, data, truth_theta(model, truth, data, 1)
+
+
+def make_ragged(n_systems: int = None, seed: int = 7):
+    """[(ReddModel, RVData, truth-theta)] of the ragged batch."""
+    n = RAGGED['n_systems'] if n_systems is None else int(n_systems)
+    return [ragged_model(seed, s) for s in range(n)]

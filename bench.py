@@ -38,6 +38,8 @@ WORKLOADS = {
     'c2': 'RV PT sweep: 3 Keplerians, 2 instruments, N=1024, per-instrument MA(1)',
     'c4': 'RV PT sweep: 5 Keplerians, 3 instruments, N=4096, per-instrument MA(1)',
     'c5': 'RV PT sweep: 7 Keplerians, 4 instruments, N=16384, per-instrument MA(2)',
+    'c3': 'RV PT sweep of a ragged batch: 4096 independent systems, N log-uniform in [50, 2000], '
+          '1-4 Keplerians, 1-3 instruments',
 }
 SEED = 1234
 
@@ -149,6 +151,8 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    if args.config == 'c3':
+        return run_reference_ragged(args)
     model, data, setup, truth = synth.build_model(args.config, seed=SEED)
     lim = model.limits_free()
     rng = np.random.default_rng(7)
@@ -186,10 +190,228 @@ def run_reference(args):
     return 0
 
 
+def ragged_p0(models, truths, T, W, rng):
+    out = []
+    for m, th in zip(models, truths):
+        lim = m.limits_free()
+        c = np.clip(th, lim[:, 0], lim[:, 1])
+        out.append(np.clip(c + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, len(c))),
+                           lim[:, 0], lim[:, 1]))
+    return out
+
+
+def ragged_cpu_sample(sy, seconds, n_sys=64, per_sys=4, ncores=None):
+    """Reference-faithful CPU rate on a sample of the batch's systems."""
+    from oracle import cpu_baseline as cb
+    rng = np.random.default_rng(7)
+    pick = rng.choice(len(sy), size=min(n_sys, len(sy)), replace=False)
+    specs = [sy[i][0].spec() for i in pick]
+    datas = [sy[i][1].as_dict() for i in pick]
+    n_ep = [sy[i][1].ndata for i in pick]
+    p0 = ragged_p0([sy[i][0] for i in pick], [sy[i][2] for i in pick], 1, per_sys, rng)
+    tasks = [(k, p0[k][0, j]) for k in range(len(pick)) for j in range(per_sys)]
+    ncores = ncores or os.cpu_count() or 1
+    v, ne, el, nc = cb.time_pool_many(specs, datas, tasks, n_ep, ncores=ncores,
+                                      min_seconds=seconds, max_seconds=2 * seconds)
+    return v, ne, el, nc, len(pick), per_sys
+
+
+def main_ragged(args):
+    """C3: every system of the ragged batch advances one PT sweep per step."""
+    import ctypes as C
+    import torch
+    from astroemperor_gb300 import _native as N
+    from astroemperor_gb300 import synth
+    from astroemperor_gb300.batch import BatchContext, BatchPTSampler
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.device('cuda', local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    sy = synth.make_ragged(seed=SEED + rank)
+    models = [m for m, _, _ in sy]
+    T, W, _, nsteps = synth.RAGGED['setup']
+    n_ep = np.array([m.data.ndata for m in models], dtype=np.int64)
+    kps = np.array([m.kplan__ for m in models], dtype=np.int64)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, ne, el, nc, npick, per = ragged_cpu_sample(sy, args.cpu_seconds)
+        cpu = {'value': v, 'unit': 'evals*epochs/s', 'cores': nc, 'kind': 'port',
+               'sample': f'{ne} reference-faithful evaluations over {npick} systems of the batch '
+                         f'({per} walkers each; my_prior+my_likelihood per walker, numpy over '
+                         f'epochs, Pool({nc})) in {el:.1f} s'}
+    lib = N.load()
+    ctx = BatchContext(models, str(dev))
+    rng = np.random.default_rng(SEED + rank)
+    p0 = ctx.pad(ragged_p0(models, [th for _, _, th in sy], T, W, rng))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def timed(precision, steps, warmup):
+        bt = BatchPTSampler(ctx, ntemps=T, nwalkers=W, precision=precision, seed=SEED + rank,
+                            record=False)
+        bt.run(p0, nsweeps=max(warmup, 1))               # autotunes, then warms up
+        st = bt._state_struct(nsteps)
+        stream = bt.stream
+        N.call('emp_pt_run', ctx.h, C.byref(st), None, 1, 1, stream.cuda_stream)
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = lib.emp_launch_count()
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(i))
+                evs[i][0].record(stream)
+            N.call('emp_pt_run', ctx.h, C.byref(st), None, 1, 1, stream.cuda_stream)
+            with torch.cuda.stream(stream):
+                evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs), lib.emp_launch_count() - l0, bt
+
+    steps = args.steps
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    ms_mixed, launches, bt = timed('mixed', steps, args.warmup)
+    clk = clocks.stop()
+    fp64_steps = args.fp64_steps or max(5, steps // 20)
+    ms_fp64, _, bt64 = timed('fp64', fp64_steps, 3)
+    t_mixed = ms_mixed / 1e3
+    if world > 1:
+        tt = torch.tensor([t_mixed], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(tt.item())
+    units_per_sweep = T * W * nsteps * int(n_ep.sum())
+    value = units_per_sweep * steps * world / t_mixed
+    fp64_value = units_per_sweep * fp64_steps / (ms_fp64 / 1e3)
+
+    # roofline: the stretch half-step shape (T*W/2 walkers of every system),
+    # one launch of the same kernel and launch shape, timed alone
+    half = torch.as_tensor(p0.reshape(ctx.S, T * W, ctx.ndim)[:, : T * W // 2].copy(), device=dev)
+    rs = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(rs):
+        for _ in range(3):
+            ctx.logpost(half, precision=N.EMP_PREC_MIXED, stream=rs)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(rs)
+        reps = 10
+        for _ in range(reps):
+            ctx.logpost(half, precision=N.EMP_PREC_MIXED, stream=rs)
+        e1.record(rs)
+    torch.cuda.synchronize()
+    k_ms = e0.elapsed_time(e1) / reps
+    F = 58 * kps + 10
+    flops_launch = float(np.sum(F * n_ep)) * (T * W // 2)
+    f32, f64p = C.c_double(), C.c_double()
+    N.call('emp_probe_peaks', C.byref(f32), C.byref(f64p), rs.cuda_stream)
+    achieved = flops_launch / (k_ms * 1e-3) / 1e12
+    peak32 = f32.value / 1e12
+    roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s',
+            'frac': achieved / peak32, 'traffic': None,
+            'kernel': 'k_logpost<MIXED,Q=0> over all systems (stretch half-step shape)',
+            'kernel_ms': k_ms, 'flop_per_eval_epoch': '58*planets + 10 per system',
+            'launch': {'lanes': bt.launch[0], 'tile': bt.launch[1]},
+            'peak_source': 'measured on this GPU by the library FMA probe (MEASURED_PEAKS.json '
+                           'has no CUDA-core figure); compute-issue bound, not HBM or tensor',
+            'fp64_peak_tflops': f64p.value / 1e12}
+
+    # end to end: the whole slot-ordered state through pinned host memory
+    SW = ctx.S * T * W
+    h_theta = torch.empty(SW, ctx.ndim, dtype=torch.float64).pin_memory()
+    h_ll = torch.empty(SW, dtype=torch.float64).pin_memory()
+    h_lp = torch.empty(SW, dtype=torch.float64).pin_memory()
+    h_theta.copy_(bt.theta.cpu())
+    h_ll.copy_(bt.logl.cpu())
+    h_lp.copy_(bt.logprior.cpu())
+    e2e_steps = min(steps, 20)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        bt.sweep_host(h_theta, h_ll, h_lp)
+    e2e_t = time.perf_counter() - t0
+    bytes_io = SW * (ctx.ndim + 2) * 8
+    e2e = {'value': units_per_sweep * e2e_steps / e2e_t, 'unit': 'evals*epochs/s',
+           'h2d_bytes_per_step': bytes_io, 'd2h_bytes_per_step': bytes_io,
+           'api': 'BatchPTSampler.sweep_host (pinned host state in, one sweep, state out)'}
+    if rank == 0:
+        cfg = {'workload': WORKLOADS['c3'], 'systems': int(ctx.S), 'ntemps': T, 'nwalkers': W,
+               'nsteps_per_sweep': nsteps, 'epochs_total': int(n_ep.sum()),
+               'epochs_min_median_max': [int(n_ep.min()), int(np.median(n_ep)), int(n_ep.max())],
+               'planets_hist': [int((kps == k).sum()) for k in range(1, 5)], 'ndim_max': int(ctx.ndim),
+               'parameterisation': 1, 'seed': SEED, 'precision': 'mixed', 'recording': 'off',
+               'l2': 'flushed between timed steps (256 MiB write, outside the timed events)'}
+        line = {'metric': METRIC, 'value': value, 'unit': 'evals*epochs/s', 'n_gpus': world,
+                'steps': steps, 'warmup': args.warmup, 'ms_per_step': ms_mixed / steps,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+                'dtype': 'f32+f64 (mixed)',
+                'data': 'synthetic (seeded generator with the configuration shapes)', 'config': cfg,
+                'pt_sweeps_per_s': steps * world / t_mixed,
+                'fp64_plain': {'value': fp64_value, 'unit': 'evals*epochs/s', 'steps': fp64_steps,
+                               'ms_per_step': ms_fp64 / fp64_steps,
+                               'launch': {'lanes': bt64.launch[0], 'tile': bt64.launch[1]}},
+                'mixed_over_fp64': value / world / fp64_value,
+                'roofline': roof, 'cpu_baseline': cpu, 'e2e': e2e, 'clocks': clk,
+                'gpu_launches': int(launches)}
+        if cpu:
+            line['gpu_over_cpu'] = value / cpu['value']
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_reference_ragged(args):
+    """Reference CPU path on the ragged batch: each step evaluates a bounded
+    sample of walkers spread over 64 of the batch's systems."""
+    from astroemperor_gb300 import synth
+    from oracle import cpu_baseline as cb
+    sy = synth.make_ragged(seed=SEED)
+    rng = np.random.default_rng(7)
+    pick = rng.choice(len(sy), size=64, replace=False)
+    n_ep = [sy[i][1].ndata for i in pick]
+    p0 = ragged_p0([sy[i][0] for i in pick], [sy[i][2] for i in pick], 1, 16, rng)
+    tasks = [(k, p0[k][0, j]) for j in range(16) for k in range(len(pick))]
+    nc = os.cpu_count() or 1
+    timer = cb.PoolTimerMany([sy[i][0].spec() for i in pick], [sy[i][1].as_dict() for i in pick], nc)
+    timer.step(tasks[:nc])
+    t1 = timer.step(tasks[:4 * nc]) / (4 * nc)
+    budget = 90.0 / max(args.steps + args.warmup, 1)
+    batch = int(min(len(tasks), max(nc, round(budget / max(t1, 1e-6)))))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        sel = [tasks[(i * batch + j) % len(tasks)] for j in range(batch)]
+        el = timer.step(sel)
+        if i >= args.warmup:
+            vals.append(sum(n_ep[k] for k, _ in sel) / el)
+    timer.close()
+    v = float(np.median(vals)) if vals else float('nan')
+    T, W, _, nsteps = synth.RAGGED['setup']
+    line = {'metric': METRIC, 'impl': 'reference', 'value': v, 'unit': 'evals*epochs/s',
+            'n_gpus': 0, 'steps': args.steps, 'warmup': args.warmup,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic',
+            'config': {'workload': WORKLOADS['c3'], 'systems': len(sy), 'ntemps': T, 'nwalkers': W,
+                       'nsteps_per_sweep': nsteps, 'parameterisation': 1, 'seed': SEED},
+            'cpu_baseline': {'value': v, 'unit': 'evals*epochs/s', 'cores': nc, 'kind': 'port',
+                             'sample': f'per step {batch} reference-faithful walker evaluations over '
+                                       f'64 systems of the batch, multiprocessing.Pool({nc}); '
+                                       f'median over steps'},
+            'e2e': {'value': v, 'unit': 'evals*epochs/s', 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.config == 'c3':
+        return main_ragged(args)
 
     import torch
     from astroemperor_gb300 import _native as N

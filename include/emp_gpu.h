@@ -132,13 +132,28 @@ int emp_create(const emp_model_desc* model, const emp_dataset_desc* data,
                emp_handle** out);
 int emp_destroy(emp_handle* h);
 
+/* Many independent systems in one handle (ragged epoch counts, each with
+   its own model): models[s] for s < data->n_systems, all with the same MA
+   order.  Replaces mapping the reference's whole run over systems one
+   script at a time.  The PT entry points then advance every system in the
+   same launches: the stretch kernel is persistent (CTAs claim
+   (system, walker-chunk) items, costliest systems first, from an atomic
+   counter), swaps run one CTA per system, and the record keeps each
+   system's cold chain (emp_pt_record.chain [rows][S][W][ndim], log_like /
+   log_prob [rows][S][W], beta_history [rows][S][T], tsw_history
+   [rows][S][T-1]; smd_history unused). */
+int emp_create_batch(const emp_model_desc* models, const emp_dataset_desc* data,
+                     emp_handle** out);
+int emp_num_systems(emp_handle* h);
+
 /* Replaces: my_likelihood(theta) (support/likelihoods/00.like:3-5) and
    my_prior(theta) (emp.py:190-251) evaluated for a batch of B walkers.
    theta [B][n_free] f64.  logl/logprior [B] f64 (device).
    If beta != NULL and logp != NULL, logp[b] = beta[b]*logl[b] + logprior[b]
    (logl is left at -inf when the prior is -inf).
-   For ragged datasets, system_of (device int32 [B], may be NULL for one
-   system) names the system of each walker. */
+   A batch handle (emp_create_batch) evaluates B rows per system: theta
+   [S][B][ndim] with ndim the largest free dimension (shorter rows padded),
+   beta and the outputs [S][B].  system_of is reserved and must be NULL. */
 int emp_logpost(emp_handle* h, const double* theta, int B,
                 const int32_t* system_of, const double* beta,
                 double* logl, double* logprior, double* logp,
@@ -191,6 +206,12 @@ typedef struct emp_pt_state {
     int32_t precision;            /* EMP_PREC_* used for every evaluation */
     void* work;                   /* device workspace of emp_pt_work_bytes() bytes */
     int64_t work_bytes;
+    /* batched handles (emp_create_batch): every array above holds all
+       systems back to back ([S][T][W] slots, [S][T] betas, theta rows of
+       `ndim` = the largest free dimension, shorter rows padded); system s
+       draws with key seed + s * 0x9E3779B97F4A7C15.  0 or 1 otherwise. */
+    int32_t n_systems;
+    int32_t _pad2;
 } emp_pt_state;
 
 /* Bytes of the workspace a PT state of this shape needs (swap log, per-sweep

@@ -100,3 +100,62 @@ def time_single(spec, data, thetas, min_seconds=2.0):
         el = time.perf_counter() - t0
         if el >= min_seconds:
             return n / el, n, el
+
+
+def _init_many(specs, datas):
+    _MANY.clear()
+    _MANY.extend(rv.OracleRV(faithful_spec(sp), d) for sp, d in zip(specs, datas))
+
+
+_MANY = []
+
+
+def _eval_many(task):
+    s, theta = task
+    o = _MANY[s]
+    lp = o.my_prior(theta)
+    if lp == -np.inf:
+        return -np.inf, lp
+    return o.my_likelihood(theta), lp
+
+
+def time_pool_many(specs, datas, tasks, n_epochs, ncores=None, min_seconds=10.0, max_seconds=30.0):
+    """Reference-faithful CPU rate over several independent systems: each
+    task (system index, theta) is one walker evaluation, as running the
+    reference once per system would do.  Returns (evals*epochs per second,
+    n_evals, seconds, ncores)."""
+    ncores = int(ncores or os.cpu_count() or 1)
+    ctx = mp.get_context('spawn')
+    tasks = list(tasks)
+    work = sum(int(n_epochs[s]) for s, _ in tasks)
+    with ctx.Pool(ncores, initializer=_init_many, initargs=(specs, datas)) as pool:
+        pool.map(_eval_many, tasks[:ncores], chunksize=1)
+        n, units = 0, 0
+        t0 = time.perf_counter()
+        while True:
+            pool.map(_eval_many, tasks, chunksize=1)
+            n += len(tasks)
+            units += work
+            el = time.perf_counter() - t0
+            if el >= min_seconds or el >= max_seconds:
+                break
+    return units / el, n, el, ncores
+
+
+class PoolTimerMany:
+    """A reference-faithful pool over several systems kept open across steps."""
+
+    def __init__(self, specs, datas, ncores=None):
+        self.ncores = int(ncores or os.cpu_count() or 1)
+        ctx = mp.get_context('spawn')
+        self.pool = ctx.Pool(self.ncores, initializer=_init_many, initargs=(specs, datas))
+
+    def step(self, tasks):
+        """Seconds to evaluate (system, theta) tasks, one walker per task."""
+        t0 = time.perf_counter()
+        self.pool.map(_eval_many, list(tasks), chunksize=1)
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()

@@ -162,3 +162,55 @@ def test_null_handles_are_errors_not_crashes(lib):
     assert lib.emp_set_launch(None, 0, 32, 0) == N.EMP_E_INVALID
     assert lib.emp_destroy(None) == N.EMP_OK
     assert b'NULL' in lib.emp_last_error_string()
+
+
+def _batch(lib, models, parts):
+    """emp_create_batch over per-system (t, y, e, ins) tuples."""
+    S = len(models)
+    descs = (N.EmpModelDesc * S)()
+    for s, m in enumerate(models):
+        descs[s] = m.descriptor() if hasattr(m, 'descriptor') else m
+    cat = lambda k, dt: np.ascontiguousarray(np.concatenate([p[k] for p in parts]), dtype=dt)
+    keep = dict(t=cat(0, np.float64), y=cat(1, np.float64), e=cat(2, np.float64), i=cat(3, np.int32),
+                o=np.concatenate([[0], np.cumsum([len(p[0]) for p in parts])]).astype(np.int64))
+    ds = N.EmpDatasetDesc()
+    ds.n_systems = S
+    ds.offsets = keep['o'].ctypes.data_as(C.POINTER(C.c_int64))
+    ds.t = keep['t'].ctypes.data_as(C.POINTER(C.c_double))
+    ds.y = keep['y'].ctypes.data_as(C.POINTER(C.c_double))
+    ds.yerr = keep['e'].ctypes.data_as(C.POINTER(C.c_double))
+    ds.inst = keep['i'].ctypes.data_as(C.POINTER(C.c_int32))
+    h = C.c_void_p()
+    rc = lib.emp_create_batch(descs, C.byref(ds), C.byref(h))
+    return rc, lib.emp_last_error_string().decode()
+
+
+def test_create_batch_rejects_bad_input_before_touching_the_gpu(lib):
+    from astroemperor_gb300 import synth
+    sy = synth.make_ragged(3, seed=1)
+    models = [m for m, _, _ in sy]
+    parts = [(d.BJD, d.RV, d.eRV, d.Flag) for _, d, _ in sy]
+    # a system with no epochs
+    bad = list(parts)
+    bad[1] = tuple(x[:0] for x in parts[1])
+    rc, msg = _batch(lib, models, bad)
+    assert rc == N.EMP_E_INVALID and 'system 1' in msg
+    # unsorted times in the last system
+    t = parts[2][0].copy(); t[[0, 1]] = t[[1, 0]]
+    bad = list(parts); bad[2] = (t,) + tuple(parts[2][1:])
+    rc, msg = _batch(lib, models, bad)
+    assert rc == N.EMP_E_INVALID and 'system 2' in msg and 'sorted' in msg
+    # a bad descriptor names its system
+    md = models[1].descriptor(); md.abi_version = 99
+    rc, msg = _batch(lib, [models[0], md, models[2]], parts)
+    assert rc == N.EMP_E_INVALID and 'system 1' in msg
+    # MA order must agree across systems
+    md = models[2].descriptor(); md.ma_order = 1; md.ma_slot = 0; md.ma_global = 1
+    rc, msg = _batch(lib, [models[0], models[1], md], parts)
+    assert rc == N.EMP_E_UNSUPPORTED and 'MA order' in msg
+    # system count out of range
+    descs = (N.EmpModelDesc * 1)()
+    ds = N.EmpDatasetDesc(); ds.n_systems = 0
+    h = C.c_void_p()
+    assert lib.emp_create_batch(descs, C.byref(ds), C.byref(h)) == N.EMP_E_SIZE
+    assert lib.emp_num_systems(None) == N.EMP_E_INVALID
