@@ -257,6 +257,9 @@ class BatchPTSampler:
             raise RuntimeError('give p0 (or call set_positions) first')
         if self.autotune and self.launch is None:
             self.tune()
+            # stored values from the shape the sweeps use
+            st = self._state_struct(1)
+            N.call('emp_pt_evaluate', self.ctx.h, C.byref(st), self.stream.cuda_stream)
         if self.record:
             self._grow((int(nsweeps) + self.thin - 1) // self.thin + 1)
         st = self._state_struct(nsteps)

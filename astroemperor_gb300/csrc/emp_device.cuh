@@ -22,6 +22,9 @@ namespace emp {
 constexpr double kTwoPi = 6.283185307179586476925286766559;
 constexpr double kPi = 3.1415926535897932384626433832795;
 constexpr int kMaxQ = EMP_MAX_MA;
+// per-instrument constants of the log-posterior kernel: offset, jitter^2,
+// offset low part (mixed), then (Phi, -1/tau) per MA term
+constexpr int kInsW = 3 + 2 * kMaxQ;
 
 // ----------------------------------------------------------------------------
 // Philox4x32-10 counter-based generator (Salmon, Moraes, Dror & Shaw,
@@ -91,6 +94,7 @@ struct DevData {
     const float* t_hi;     // float-float split of t
     const float* t_lo;
     const float* y32;
+    const float* y_lo;     // y - (double)y32
     const float* s2_32;
     const float* dt32;     // [q][n]
     const int* inst;       // [n] 0-based instrument
@@ -150,13 +154,13 @@ struct Smem {
                                    int n_free, int n_planets, int n_ins, int acc_order) {
         int rs = prec == EMP_PREC_FP64 ? 8 : 4;          // real size
         int per_epoch = (prec == EMP_PREC_FP64) ? (8 * 3 + 4 + 8 * q)
-                                                : (4 * 4 + 4 + 4 * q);
+                                                : (4 * 5 + 4 + 4 * q);
         tile_bytes = align16(per_epoch * tile + 64);
         int o = 0;
         off_full = o; o += align16(8 * n_full);
         off_thp = o;  o += align16(8 * (n_free > 0 ? n_free : 1));
-        off_pc = o;   o += align16(rs * 8 * (n_planets > 0 ? n_planets : 1));
-        off_ins = o;  o += align16(rs * (2 + 2 * kMaxQ) * (n_ins > 0 ? n_ins : 1));
+        off_pc = o;   o += align16(rs * (prec == EMP_PREC_FP64 ? 8 : 12) * (n_planets > 0 ? n_planets : 1));
+        off_ins = o;  o += align16(rs * kInsW * (n_ins > 0 ? n_ins : 1));
         off_acc = o;  o += align16(8 * (acc_order > 0 ? acc_order : 1));
         off_red = o;  o += align16(8 * 4 * ((L + 31) / 32));
         off_scan = o; o += align16(rs * 2 * (kMaxQ + kMaxQ * kMaxQ) * L);
@@ -241,30 +245,6 @@ __device__ __forceinline__ void kepler_f64(double Mr, double e, double& s, doubl
     sincos(E, &s, &c);
 }
 
-// FP32: second-order series start, Halley until |dE| < 1e-3 (cubic
-// convergence leaves ~1e-9), final (sin E, cos E) rotated by the last step.
-__device__ __forceinline__ void kepler_f32(float M, float e, float& s, float& c) {
-    float sM, cM;
-    __sincosf(M, &sM, &cM);
-    float E = M + e * sM * (1.f + e * cM);
-    float d = 0.f;
-#pragma unroll 1
-    for (int it = 0; it < 16; ++it) {
-        __sincosf(E, &s, &c);
-        float f = E - e * s - M;
-        float f1 = 1.f - e * c;
-        float f2 = e * s;
-        d = __fdividef(f * f1, f1 * f1 - 0.5f * f * f2);
-        E -= d;
-        if (fabsf(d) < 1e-3f) break;
-    }
-    float d2 = d * d;
-    float cd = 1.f - 0.5f * d2;
-    float sd = d * (1.f - d2 * (1.f / 6.f));
-    float sn = s * cd - c * sd;
-    float cn = c * cd + s * sd;
-    s = sn; c = cn;
-}
 
 // ----------------------------------------------------------------------------
 // precision traits
@@ -278,8 +258,9 @@ template <> struct P<EMP_PREC_FP64> {
 };
 template <> struct P<EMP_PREC_MIXED> {
     using R = float;
-    // [0]=f_hi [1]=f_lo (cycles/day) [2]=ph_hi [3]=ph_lo (cycles) [4]=e [5]=A [6]=B [7]=C
-    static constexpr int kPC = 8;
+    // [0]=f_hi [1]=f_lo (cycles/day) [2]=ph_hi [3]=ph_lo (cycles) [4]=e [5]=A [6]=B [7]=C,
+    // [8..11] = the low parts of e, A, B, C (float-float constants)
+    static constexpr int kPC = 12;
 };
 
 // ----------------------------------------------------------------------------

@@ -76,7 +76,7 @@ __device__ __forceinline__ double prior_var_grad(const emp_prior& p, double x) {
 // [4]=e [5]=cw [6]=sw [7]=K [8]=q=sqrt(1-e^2) [9]=S or 0 [10]=C or 0
 // [11]=1/e^1.5 (0 below the omega threshold) [12]=parameterisation
 __device__ __forceinline__ void planet_grad_consts(int par, const double* v, float* pc) {
-    float tmp[8];
+    float tmp[12];
     planet_consts_mixed(par, v, tmp);
     pc[0] = tmp[0]; pc[1] = tmp[1]; pc[2] = tmp[2]; pc[3] = tmp[3];
     const float e = tmp[4];
@@ -268,10 +268,10 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
             }
             for (int p = 0; p < n_planets; ++p) {
                 const float* pc = pcs + p * kGradPC;
-                float M[NE], sn[NE], cs[NE];
+                float M[NE], ml[NE], sn[NE], cs[NE];
 #pragma unroll
-                for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e]);
-                kepler_f32_n<NE>(M, pc[4], sn, cs);
+                for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e], ml[e]);
+                kepler_f32_n<NE>(M, ml, pc[4], 0.f, sn, cs);
 #pragma unroll
                 for (int e = 0; e < NE; ++e) {
                     const float ec = pc[4], D = 1.f - ec * cs[e];
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
             for (int k0 = 0; k0 < nr; k0 += NE) {
                 int pos[NE];
                 bool ok[NE];
-                float th[NE], tl[NE], M[NE], sn[NE], cs[NE];
+                float th[NE], tl[NE], M[NE], ml[NE], sn[NE], cs[NE];
 #pragma unroll
                 for (int e = 0; e < NE; ++e) {
                     const int kk = k0 + e < nr ? k0 + e : nr - 1;
@@ -581,9 +581,9 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
                     pos[e] = posof(r, kk);
                     th[e] = s_th[pos[e]];
                     tl[e] = s_tl[pos[e]];
-                    M[e] = mean_anomaly_mixed(pc, th[e], tl[e]);
+                    M[e] = mean_anomaly_mixed(pc, th[e], tl[e], ml[e]);
                 }
-                kepler_f32_n<NE>(M, ec, sn, cs);
+                kepler_f32_n<NE>(M, ml, ec, 0.f, sn, cs);
 #pragma unroll
                 for (int e = 0; e < NE; ++e) {
                     if (!ok[e]) continue;

@@ -117,42 +117,64 @@ __device__ __forceinline__ void planet_consts_fp64(int par, const double* v, dou
     pc[7] = (double)el.use_tp;
 }
 
+// 1/sqrt(x) and sqrt(x) to ~1e-14: FP32 estimate, one FP64 Newton step
+// (two or three FP64 operations instead of a full FP64 square root)
+__device__ __forceinline__ double rsqrt_refined(double x) {
+    const double r0 = (double)rsqrtf((float)x);
+    return r0 * fma(-0.5 * x * r0, r0, 1.5);
+}
+__device__ __forceinline__ double sqrt_refined(double x) {
+    const float s0 = sqrtf((float)x);
+    if (!(s0 > 0.f)) return 0.0;
+    return fma(fma(-(double)s0, (double)s0, x), (double)(0.5f / s0), (double)s0);
+}
+
+__device__ __forceinline__ void split_ff(double x, float& hi, float& lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
 // mixed: [0]=f_hi [1]=f_lo (cycles/day) [2]=ph_hi [3]=ph_lo (cycles)
-//        [4]=e [5]=A=K cw [6]=B=K sqrt(1-e^2) sw [7]=C=K e cw
+//        [4]=e [5]=A=K cw [6]=B=K sqrt(1-e^2) sw [7]=C=K e cw, and [8..11]
+//        the low parts of e, A, B, C: the constants are formed in FP64 and
+//        kept as float-float pairs, so their rounding adds no systematic
+//        error to the model (a rounded constant shifts every epoch alike)
 __device__ __forceinline__ void planet_consts_mixed(int par, const double* v, float* pc) {
-    double per;
-    float K, e, cw, sw;
+    double per, K, e = 0.0, cw = 1.0, sw = 0.0;
     bool use_tp = false;
     double phase = 0.0, tp = 0.0;
     if (par == 0 || par == 3 || par == 6) {
         per = par == 6 ? exp(v[0]) : v[0];
-        K = (float)v[1];
-        e = (float)v[3];
-        sincosf((float)v[4], &sw, &cw);
+        K = v[1];
+        e = v[3];
+        float s32, c32;
+        sincosf((float)v[4], &s32, &c32);
+        sw = s32;
+        cw = c32;
         if (par == 3) { use_tp = true; tp = v[2]; } else { phase = v[2]; }
     } else if (par == 2) {
         per = exp(v[0]);
         const float As = (float)v[1], Ac = (float)v[2];
-        K = As * As + Ac * Ac;
-        float ph = acosf(Ac * rsqrtf(K));
+        const float K32 = As * As + Ac * Ac;
+        K = (double)K32;
+        float ph = acosf(Ac * rsqrtf(K32));
         if (As < 0.f) ph = 6.28318530717958647692f - ph;
         phase = (double)ph;
     } else {
         per = par == 7 ? exp(v[0]) : v[0];
-        K = (float)v[1];
+        K = v[1];
         if (par == 4) { use_tp = true; tp = v[2]; } else { phase = v[2]; }
     }
     if (par == 1 || par == 2 || par == 4 || par == 7) {
-        const double ed = v[3] * v[3] + v[4] * v[4];        // FP64 as the reference
+        e = v[3] * v[3] + v[4] * v[4];                      // FP64 as the reference
         const double thr = (par == 2 || par == 4) ? 1e-5 : 1e-6;
-        e = (float)ed;
-        if (ed < thr) { cw = 1.f; sw = 0.f; }
-        else {
-            const float rs = rsqrtf(e);
-            cw = (float)v[4] * rs;
-            sw = (float)v[3] * rs;
+        if (e >= thr) {
+            const double rs = rsqrt_refined(e);
+            cw = v[4] * rs;
+            sw = v[3] * rs;
         }
     }
+    const double sq = sqrt_refined(fma(-e, e, 1.0));
     const FF f = ff_recip(ff_split(per));
     FF ph;
     if (use_tp) {
@@ -167,10 +189,11 @@ __device__ __forceinline__ void planet_consts_mixed(int par, const double* v, fl
     pc[1] = f.lo;
     pc[2] = ph.hi;
     pc[3] = ph.lo;
-    pc[4] = e;
-    pc[5] = K * cw;
-    pc[6] = K * sqrtf((1.f - e) * (1.f + e)) * sw;
-    pc[7] = K * e * cw;
+    const double A = K * cw;
+    split_ff(e, pc[4], pc[8]);
+    split_ff(A, pc[5], pc[9]);
+    split_ff(K * sq * sw, pc[6], pc[10]);
+    split_ff(A * e, pc[7], pc[11]);
 }
 
 // one Keplerian term at one epoch (FP64)
@@ -191,8 +214,9 @@ __device__ __forceinline__ double rv_term_f64(const double* pc, double t) {
     return (pc[3] * (c - e) - pc[4] * s) * inv + pc[5];
 }
 
-// mean anomaly in [-pi, pi] from float-float time and planet constants
-__device__ __forceinline__ float mean_anomaly_mixed(const float* pc, float th, float tl) {
+// mean anomaly in [-pi, pi] from float-float time and planet constants;
+// mlo receives the part of (cycles mod 1) * 2 pi that the FP32 result drops
+__device__ __forceinline__ float mean_anomaly_mixed(const float* pc, float th, float tl, float& mlo) {
     // cycles = (th + tl) * (fh + fl) + (ph_hi + ph_lo), reduced mod 1; the
     // error-free transforms use _rn intrinsics so they are not contracted
     const float fh = pc[0], fl = pc[1];
@@ -203,49 +227,99 @@ __device__ __forceinline__ float mean_anomaly_mixed(const float* pc, float th, f
     const float xe = __fadd_rn(__fsub_rn(p, __fsub_rn(x, bv)), __fsub_rn(pc[2], bv));
     const float fr = __fsub_rn(x, rintf(x));             // exact
     const float lo = pe + xe + pc[3] + __fmaf_rn(th, fl, tl * fh);
-    float cyc = __fadd_rn(fr, lo);
-    cyc = __fsub_rn(cyc, rintf(cyc));
-    return cyc * 6.28318530717958647692f;
+    const float cyc0 = __fadd_rn(fr, lo);
+    const float cb = __fsub_rn(cyc0, fr);                // TwoSum(fr, lo) error
+    const float ce = __fadd_rn(__fsub_rn(fr, __fsub_rn(cyc0, cb)), __fsub_rn(lo, cb));
+    const float cyc = __fsub_rn(cyc0, rintf(cyc0));      // exact
+    const float M = __fmul_rn(cyc, 6.28318530717958647692f);
+    // 2 pi = 6.2831855f - 1.7484555e-07
+    mlo = __fadd_rn(__fmaf_rn(cyc, 6.28318530717958647692f, -M),
+                    __fmaf_rn(cyc, -1.7484555e-07f, __fmul_rn(ce, 6.28318530717958647692f)));
+    return M;
+}
+__device__ __forceinline__ float mean_anomaly_mixed(const float* pc, float th, float tl) {
+    float mlo;
+    return mean_anomaly_mixed(pc, th, tl, mlo);
 }
 
-// NE independent FP32 Kepler solves: second-order series start, joint
-// Halley iterations until every |dE| < 1e-3 (cubic convergence leaves
-// ~1e-9), final (sin E, cos E) rotated by the last step.
+// sin and cos of x (|x| <= ~8) to about 1 ulp without the special
+// function unit: Cody-Waite reduction by pi/2 (the first part of pi/2 has
+// 12 significant bits, so q * C1 and x - q * C1 are exact for |q| <= 4),
+// Taylor polynomials of degree 9 (sin) and 10 (cos) on |r| <= pi/4
+// (truncation below 2e-9), and the quadrant rotation.
+__device__ __forceinline__ void sincos_acc(float x, float& s, float& c) {
+    const float q = rintf(__fmul_rn(x, 0.636619772367581343f));
+    float r = __fmaf_rn(-q, 1.5703125f, x);
+    r = __fmaf_rn(-q, 4.83826794896619231e-04f, r);
+    r = __fmaf_rn(-q, 2.56328273e-12f, r);
+    const float r2 = __fmul_rn(r, r);
+    float ps = __fmaf_rn(r2, 2.75573192e-06f, -1.98412698e-04f);
+    ps = __fmaf_rn(r2, ps, 8.33333333e-03f);
+    ps = __fmaf_rn(r2, ps, -1.66666667e-01f);
+    const float sr = __fmaf_rn(__fmul_rn(r2, r), ps, r);
+    float pc = __fmaf_rn(r2, -2.75573192e-07f, 2.48015873e-05f);
+    pc = __fmaf_rn(r2, pc, -1.38888889e-03f);
+    pc = __fmaf_rn(r2, pc, 4.16666667e-02f);
+    pc = __fmaf_rn(r2, pc, -0.5f);
+    const float cr = __fmaf_rn(r2, pc, 1.f);
+    const int qi = (int)q;
+    const float ss = (qi & 1) ? cr : sr;
+    const float cc = (qi & 1) ? sr : cr;
+    s = (qi & 2) ? -ss : ss;
+    c = ((qi + 1) & 2) ? -cc : cc;
+}
+
+// NE independent FP32 Kepler solves of E - (e + elo) sin E = M + mlo:
+// second-order series start, joint Halley iterations with the special
+// function unit's sin/cos until every |dE| < 1e-3, then one Newton step
+// whose residual uses sincos_acc, an error-free E - M and the low parts of
+// M and e; (sin E, cos E) are rotated by that step.  The hardware sin/cos
+// (absolute error ~4e-7) only steer the iterations: the converged E is off
+// by at most ~2e-6, which the Newton step reduces below 1e-11.
 template <int NE>
-__device__ __forceinline__ void kepler_f32_n(const float (&M)[NE], float e, float (&s)[NE],
-                                             float (&c)[NE]) {
-    float E[NE], d[NE];
+__device__ __forceinline__ void kepler_f32_n(const float (&M)[NE], const float (&mlo)[NE], float e,
+                                             float elo, float (&s)[NE], float (&c)[NE]) {
+    float E[NE];
 #pragma unroll
     for (int k = 0; k < NE; ++k) {
         float sM, cM;
         __sincosf(M[k], &sM, &cM);
         E[k] = M[k] + e * sM * (1.f + e * cM);
-        d[k] = 0.f;
     }
 #pragma unroll 1
     for (int it = 0; it < 16; ++it) {
         bool more = false;
 #pragma unroll
         for (int k = 0; k < NE; ++k) {
-            __sincosf(E[k], &s[k], &c[k]);
-            const float f = E[k] - e * s[k] - M[k];
-            const float f1 = 1.f - e * c[k];
-            const float f2 = e * s[k];
-            d[k] = __fdividef(f * f1, f1 * f1 - 0.5f * f * f2);
-            E[k] -= d[k];
-            more |= fabsf(d[k]) >= 1e-3f;
+            float sk, ck;
+            __sincosf(E[k], &sk, &ck);
+            const float f = E[k] - e * sk - M[k];
+            const float f1 = 1.f - e * ck;
+            const float f2 = e * sk;
+            const float d = __fdividef(f * f1, f1 * f1 - 0.5f * f * f2);
+            E[k] -= d;
+            more |= fabsf(d) >= 1e-3f;
         }
         if (!more) break;
     }
 #pragma unroll
     for (int k = 0; k < NE; ++k) {
-        const float d2 = d[k] * d[k];
+        float sa, ca;
+        sincos_acc(E[k], sa, ca);
+        // E - M as an exact float pair (TwoSum)
+        const float dh = __fsub_rn(E[k], M[k]);
+        const float bv = __fsub_rn(dh, E[k]);
+        const float dl = __fadd_rn(__fsub_rn(E[k], __fsub_rn(dh, bv)), __fsub_rn(-M[k], bv));
+        // F = E - M - mlo - (e + elo) sin E; e sin E nearly cancels dh
+        float F = __fmaf_rn(-e, sa, dh);
+        F = __fadd_rn(F, __fmaf_rn(-elo, sa, __fsub_rn(dl, mlo[k])));
+        const float f1 = __fmaf_rn(-elo, ca, __fmaf_rn(-e, ca, 1.f));
+        const float d = __fdividef(F, f1);
+        const float d2 = d * d;
         const float cd = 1.f - 0.5f * d2;
-        const float sd = d[k] * (1.f - d2 * (1.f / 6.f));
-        const float sn = s[k] * cd - c[k] * sd;
-        const float cn = c[k] * cd + s[k] * sd;
-        s[k] = sn;
-        c[k] = cn;
+        const float sd = d * (1.f - d2 * (1.f / 6.f));
+        s[k] = __fmaf_rn(sa, cd, -ca * sd);
+        c[k] = __fmaf_rn(ca, cd, sa * sd);
     }
 }
 
@@ -421,7 +495,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     double* pterm = reinterpret_cast<double*>(gs + lay.off_pterm);
     double* misc = reinterpret_cast<double*>(gs + lay.off_misc);
     int* flag = reinterpret_cast<int*>(misc + 4);
-    constexpr int INSW = 2 + 2 * kMaxQ;
+    constexpr int INSW = kInsW;
 
     // items: one per CTA for a plain handle; (system, walker chunk) pairs
     // claimed from an atomic counter, costliest systems first, for a batch
@@ -530,15 +604,16 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             const double off = md->offset_slot >= 0 ? full[md->offset_slot + k] : 0.0;
             const double jit = md->jitter_slot >= 0 ? full[md->jitter_slot + k] : 0.0;
             ic[0] = (R)off;
+            ic[2] = (R)(off - (double)(R)off);              // 0 in FP64
             if (PREC == EMP_PREC_FP64) ic[1] = (R)(jit * jit);
             else { const float jf = (float)jit; ic[1] = (R)(jf * jf); }
 #pragma unroll
             for (int c = 0; c < Q; ++c) {
                 const int base = md->ma_global ? md->ma_slot + 2 * c : md->ma_slot + 2 * Q * k + 2 * c;
                 const double phi = full[base], tau = full[base + 1];
-                ic[2 + 2 * c] = (R)phi;
-                if (PREC == EMP_PREC_FP64) ic[3 + 2 * c] = (R)(-1.0 / tau);
-                else ic[3 + 2 * c] = (R)(-1.44269504f / (float)tau);   // exp2 scale
+                ic[3 + 2 * c] = (R)phi;
+                if (PREC == EMP_PREC_FP64) ic[4 + 2 * c] = (R)(-1.0 / tau);
+                else ic[4 + 2 * c] = (R)(-1.44269504f / (float)tau);   // exp2 scale
             }
         }
         for (int j = r; j < acc_order; j += L) accc[j] = full[md->acc_slot + j];
@@ -561,11 +636,12 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     const int n = A.sys_off != nullptr ? (int)(A.sys_off[sys + 1] - e0) : A.d.n;
     const int tile = A.tile;
     unsigned char* ts = smem;
-    R* s_t0;  R* s_t1;  R* s_y;  R* s_s2;  int* s_in;  R* s_dt;
+    R* s_t0;  R* s_t1;  R* s_y;  R* s_ylo;  R* s_s2;  int* s_in;  R* s_dt;
     if (PREC == EMP_PREC_FP64) {
         s_t0 = reinterpret_cast<R*>(ts);
         s_t1 = s_t0;                       // unused
         s_y = s_t0 + tile;
+        s_ylo = s_y;                       // unused
         s_s2 = s_y + tile;
         s_in = reinterpret_cast<int*>(s_s2 + tile);
         s_dt = reinterpret_cast<R*>(ts + Smem::align16((3 * tile) * (int)sizeof(R) + 4 * tile));
@@ -573,7 +649,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
         s_t0 = reinterpret_cast<R*>(ts);
         s_t1 = s_t0 + tile;
         s_y = s_t1 + tile;
-        s_s2 = s_y + tile;
+        s_ylo = s_y + tile;
+        s_s2 = s_ylo + tile;
         s_in = reinterpret_cast<int*>(s_s2 + tile);
         s_dt = reinterpret_cast<R*>(s_in + tile);
     }
@@ -601,6 +678,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                 s_t0[pos] = (R)A.d.t_hi[gi];
                 s_t1[pos] = (R)A.d.t_lo[gi];
                 s_y[pos] = (R)A.d.y32[gi];
+                s_ylo[pos] = (R)A.d.y_lo[gi];
                 s_s2[pos] = (R)A.d.s2_32[gi];
             }
             s_in[pos] = A.d.inst[gi];
@@ -659,15 +737,20 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     for (int e = 0; e < NE; ++e) { th[e] = (float)s_t0[pos[e]]; tl[e] = (float)s_t1[pos[e]]; }
                     for (int p = 0; p < n_planets; ++p) {
                         const float* pc = (const float*)(pcs + p * PC);
-                        float M[NE], sn[NE], cs[NE];
+                        float M[NE], ml[NE], sn[NE], cs[NE];
 #pragma unroll
-                        for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e]);
-                        const float ec = pc[4];
-                        kepler_f32_n<NE>(M, ec, sn, cs);
+                        for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e], ml[e]);
+                        const float ec = pc[4], el = pc[8];
+                        kepler_f32_n<NE>(M, ml, ec, el, sn, cs);
 #pragma unroll
                         for (int e = 0; e < NE; ++e) {
-                            const float inv = __frcp_rn(1.f - ec * cs[e]);
-                            model[e] += (R)__fmaf_rn(__fmaf_rn(pc[5], cs[e] - ec, -pc[6] * sn[e]), inv, pc[7]);
+                            // (A (cos E - e) - B sin E) / (1 - e cos E) + C with
+                            // float-float A, B, C, e
+                            const float cme = __fsub_rn(__fsub_rn(cs[e], ec), el);
+                            const float inv = __frcp_rn(__fmaf_rn(-el, cs[e], __fmaf_rn(-ec, cs[e], 1.f)));
+                            const float hi = __fmaf_rn(__fmaf_rn(pc[5], cme, -pc[6] * sn[e]), inv, pc[7]);
+                            const float lo = __fmaf_rn(__fmaf_rn(pc[9], cme, -pc[10] * sn[e]), inv, pc[11]);
+                            model[e] += (R)__fadd_rn(hi, lo);
                         }
                     }
                     if (acc_order > 0) {
@@ -686,9 +769,11 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     const int ps = pos[e];
                     const int ki = s_in[ps];
                     const R* ic = insc + ki * INSW;
-                    const R mod = model[e] + ic[0];
                     const R err2 = s_s2[ps] + ic[1];
-                    const R b = s_y[ps] - mod;
+                    R b;
+                    if (PREC == EMP_PREC_FP64) b = s_y[ps] - (model[e] + ic[0]);
+                    else b = (R)__fadd_rn(__fsub_rn(__fsub_rn((float)s_y[ps], (float)ic[0]), (float)model[e]),
+                                          __fsub_rn((float)s_ylo[ps], (float)ic[2]));
                     R w, lt;
                     if (PREC == EMP_PREC_FP64) { w = R(1) / err2; lt = (R)log((double)err2); }
                     else { w = (R)__frcp_rn((float)err2); lt = (R)(__log2f((float)err2) * 0.69314718055994531f); }
@@ -703,8 +788,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                         for (int c = 0; c < Q; ++c) {
                             const R dtc = s_dt[c * tile + ps];
                             R a;
-                            if (PREC == EMP_PREC_FP64) a = ic[2 + 2 * c] * (R)exp((double)(dtc * ic[3 + 2 * c]));
-                            else a = ic[2 + 2 * c] * (R)exp2f((float)(dtc * ic[3 + 2 * c]));
+                            if (PREC == EMP_PREC_FP64) a = ic[3 + 2 * c] * (R)exp((double)(dtc * ic[4 + 2 * c]));
+                            else a = ic[3 + 2 * c] * (R)exp2f((float)(dtc * ic[4 + 2 * c]));
                             x -= a * xh[c];
 #pragma unroll
                             for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];

@@ -231,8 +231,11 @@ int prepare_eval(emp_handle* h, int prec) {
     KFn fn = prec == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
     if (!fn) return fail(EMP_E_UNSUPPORTED, "no kernel for q=%d L=%d", h->q, L);
     if (!h->attr_done[prec][h->q][li]) {
+        // 227 KB per block covers the static shared memory too
+        cudaFuncAttributes fa;
+        CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)fn));
         CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      227 * 1024));
+                                      227 * 1024 - (int)fa.sharedSizeBytes));
         h->attr_done[prec][h->q][li] = true;
     }
     if (h->n_sys > 1) {
@@ -263,7 +266,7 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     int G = NT / L;
     Smem lay;
     int tile = pick_tile(h, prec, L, G, lay);
-    if (lay.total > 227 * 1024)
+    if (lay.total > 227 * 1024 - 64)
         return fail(EMP_E_SIZE, "shared memory %d B exceeds 227 KB", lay.total);
     KFn fn = prec == EMP_PREC_FP64 ? get_kernel_fp64(h->q, li) : get_kernel_mixed(h->q, li);
     if (!fn) return fail(EMP_E_UNSUPPORTED, "no kernel for q=%d L=%d", h->q, L);
@@ -482,11 +485,11 @@ namespace {
 // distances of the MA recurrence (+inf across a series start).
 struct HostData {
     std::vector<double> t, y, s2, dt;
-    std::vector<float> t_hi, t_lo, y32, s2_32, dt32;
+    std::vector<float> t_hi, t_lo, y32, y_lo, s2_32, dt32;
     std::vector<int> inst, orig;
     void reserve(size_t n, int q) {
         t.reserve(n); y.reserve(n); s2.reserve(n); t_hi.reserve(n); t_lo.reserve(n);
-        y32.reserve(n); s2_32.reserve(n); inst.reserve(n); orig.reserve(n);
+        y32.reserve(n); y_lo.reserve(n); s2_32.reserve(n); inst.reserve(n); orig.reserve(n);
         (void)q;
     }
 };
@@ -542,6 +545,7 @@ void append_system(const emp_model_desc* model, const emp_dataset_desc* data, in
         H.t_hi.push_back(hi);
         H.t_lo.push_back((float)(t[k] - (double)hi));
         H.y32.push_back((float)y[k]);
+        H.y_lo.push_back((float)(y[k] - (double)(float)y[k]));
         H.s2_32.push_back((float)(ye[k] * ye[k]));
         H.orig.push_back(k);
     }
@@ -635,7 +639,8 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
     auto take = [&](size_t b) { size_t o = bytes; bytes += (b + 255) & ~(size_t)255; return o; };
     const size_t N8 = 8 * (size_t)n, N4 = 4 * (size_t)n;
     size_t o_t = take(N8), o_y = take(N8), o_s2 = take(N8), o_dt = take(8 * qn);
-    size_t o_th = take(N4), o_tl = take(N4), o_yf = take(N4), o_sf = take(N4), o_dtf = take(4 * qn);
+    size_t o_th = take(N4), o_tl = take(N4), o_yf = take(N4), o_yl = take(N4), o_sf = take(N4);
+    size_t o_dtf = take(4 * qn);
     size_t o_in = take(N4), o_perm = take(N4);
     size_t o_md = take(sizeof(emp_model_desc) * (size_t)S);
     size_t o_off = take(8 * (size_t)(S + 1)), o_t0 = take(8 * (size_t)S), o_ord = take(4 * (size_t)S);
@@ -648,6 +653,7 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
     struct Cp { size_t off; const void* src; size_t n; } cps[] = {
         {o_t, H.t.data(), N8}, {o_y, H.y.data(), N8}, {o_s2, H.s2.data(), N8}, {o_dt, hdt.data(), 8 * qn},
         {o_th, H.t_hi.data(), N4}, {o_tl, H.t_lo.data(), N4}, {o_yf, H.y32.data(), N4},
+        {o_yl, H.y_lo.data(), N4},
         {o_sf, H.s2_32.data(), N4}, {o_dtf, dtf.data(), 4 * qn}, {o_in, H.inst.data(), N4},
         {o_perm, H.orig.data(), N4}, {o_md, models, sizeof(emp_model_desc) * (size_t)S},
         {o_off, off.data(), 8 * (size_t)(S + 1)}, {o_t0, t0.data(), 8 * (size_t)S},
@@ -677,6 +683,7 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
     h->dd.t_hi = (const float*)(b + o_th);
     h->dd.t_lo = (const float*)(b + o_tl);
     h->dd.y32 = (const float*)(b + o_yf);
+    h->dd.y_lo = (const float*)(b + o_yl);
     h->dd.s2_32 = (const float*)(b + o_sf);
     h->dd.dt32 = (const float*)(b + o_dtf);
     h->dd.inst = (const int*)(b + o_in);

@@ -364,6 +364,9 @@ class PTSampler:
             self.stream.synchronize()
             half = self.theta[: self.ntemps * (self.nwalkers // 2)]
             self.launch = autotune(self.ctx, half, self.precision)
+            # stored values from the shape the sweeps use
+            st = self._state_struct(1)
+            N.call('emp_pt_evaluate', self.ctx.h, C.byref(st), self.stream.cuda_stream)
         self._grow(nsweeps)
         st = self._state_struct(nsteps)
         rec = self._record_struct()
