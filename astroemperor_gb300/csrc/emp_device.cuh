@@ -159,7 +159,7 @@ struct Smem {
         int o = 0;
         off_full = o; o += align16(8 * n_full);
         off_thp = o;  o += align16(8 * (n_free > 0 ? n_free : 1));
-        off_pc = o;   o += align16(rs * (prec == EMP_PREC_FP64 ? 8 : 12) * (n_planets > 0 ? n_planets : 1));
+        off_pc = o;   o += align16(rs * (prec == EMP_PREC_FP64 ? 8 : 16) * (n_planets > 0 ? n_planets : 1));
         off_ins = o;  o += align16(rs * kInsW * (n_ins > 0 ? n_ins : 1));
         off_acc = o;  o += align16(8 * (acc_order > 0 ? acc_order : 1));
         off_red = o;  o += align16(8 * 4 * ((L + 31) / 32));
@@ -259,8 +259,9 @@ template <> struct P<EMP_PREC_FP64> {
 template <> struct P<EMP_PREC_MIXED> {
     using R = float;
     // [0]=f_hi [1]=f_lo (cycles/day) [2]=ph_hi [3]=ph_lo (cycles) [4]=e [5]=A [6]=B [7]=C,
-    // [8..11] = the low parts of e, A, B, C (float-float constants)
-    static constexpr int kPC = 12;
+    // [8..11] = the low parts of e, A, B, C (float-float constants),
+    // [12..15] = Kepler starter constants of e (a, a^3, 0.5 / (4 e + 0.5), 0.078 / (1 + e))
+    static constexpr int kPC = 16;
 };
 
 // ----------------------------------------------------------------------------

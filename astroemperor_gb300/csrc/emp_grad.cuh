@@ -76,7 +76,7 @@ __device__ __forceinline__ double prior_var_grad(const emp_prior& p, double x) {
 // [4]=e [5]=cw [6]=sw [7]=K [8]=q=sqrt(1-e^2) [9]=S or 0 [10]=C or 0
 // [11]=1/e^1.5 (0 below the omega threshold) [12]=parameterisation
 __device__ __forceinline__ void planet_grad_consts(int par, const double* v, float* pc) {
-    float tmp[12];
+    float tmp[16];
     planet_consts_mixed(par, v, tmp);
     pc[0] = tmp[0]; pc[1] = tmp[1]; pc[2] = tmp[2]; pc[3] = tmp[3];
     const float e = tmp[4];

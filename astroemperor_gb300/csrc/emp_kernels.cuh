@@ -194,6 +194,14 @@ __device__ __forceinline__ void planet_consts_mixed(int par, const double* v, fl
     split_ff(A, pc[5], pc[9]);
     split_ff(K * sq * sw, pc[6], pc[10]);
     split_ff(A * e, pc[7], pc[11]);
+    // starter of the Kepler solve (Mikkola 1987, Celest. Mech. 40, 329)
+    const float ef = pc[4];
+    const float den = __fdividef(1.f, 4.f * ef + 0.5f);
+    const float a = (1.f - ef) * den;
+    pc[12] = a;
+    pc[13] = a * a * a;
+    pc[14] = 0.5f * den;
+    pc[15] = __fdividef(0.078f, 1.f + ef);
 }
 
 // one Keplerian term at one epoch (FP64)
@@ -320,6 +328,118 @@ __device__ __forceinline__ void kepler_f32_n(const float (&M)[NE], const float (
         const float sd = d * (1.f - d2 * (1.f / 6.f));
         s[k] = __fmaf_rn(sa, cd, -ca * sd);
         c[k] = __fmaf_rn(ca, cd, sa * sd);
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Two epochs per instruction: the same mixed-precision steps on float2 pairs
+// with the packed FP32 instructions of sm_100+ (__ffma2_rn, __fadd2_rn,
+// __fmul2_rn).  Each element is rounded exactly as the scalar operation
+// would be; only the special-function and rounding-to-integer steps stay
+// per element.
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// a - b with one rounding (the product b * -1 is exact)
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.f), a); }
+__device__ __forceinline__ float2 rint2(float2 a) { return make_float2(rintf(a.x), rintf(a.y)); }
+__device__ __forceinline__ float2 rcp_approx2(float2 a) {
+    return make_float2(__fdividef(1.f, a.x), __fdividef(1.f, a.y));
+}
+__device__ __forceinline__ float2 rcp_rn2(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+
+// mean_anomaly_mixed on a pair of epochs
+__device__ __forceinline__ float2 mean_anomaly_pair(const float* pc, float2 th, float2 tl, float2& mlo) {
+    const float2 fh = bc2(pc[0]), ph = bc2(pc[2]);
+    const float2 p = mul2(th, fh);
+    const float2 pe = fma2(th, fh, make_float2(-p.x, -p.y));
+    const float2 x = add2(p, ph);
+    const float2 bv = sub2(x, p);
+    const float2 xe = add2(sub2(p, sub2(x, bv)), sub2(ph, bv));
+    const float2 fr = sub2(x, rint2(x));
+    const float2 lo = add2(add2(add2(pe, xe), bc2(pc[3])), fma2(th, bc2(pc[1]), mul2(tl, fh)));
+    const float2 cyc0 = add2(fr, lo);
+    const float2 cb = sub2(cyc0, fr);
+    const float2 ce = add2(sub2(fr, sub2(cyc0, cb)), sub2(lo, cb));
+    const float2 cyc = sub2(cyc0, rint2(cyc0));
+    const float2 tp = bc2(6.28318530717958647692f);
+    const float2 M = mul2(cyc, tp);
+    mlo = add2(fma2(cyc, tp, make_float2(-M.x, -M.y)), fma2(cyc, bc2(-1.7484555e-07f), mul2(ce, tp)));
+    return M;
+}
+
+// sincos_acc on a pair
+__device__ __forceinline__ void sincos_acc_pair(float2 x, float2& s, float2& c) {
+    const float2 q = rint2(mul2(x, bc2(0.636619772367581343f)));
+    float2 r = fma2(q, bc2(-1.5703125f), x);
+    r = fma2(q, bc2(-4.83826794896619231e-04f), r);
+    r = fma2(q, bc2(-2.56328273e-12f), r);
+    const float2 r2 = mul2(r, r);
+    float2 ps = fma2(r2, bc2(2.75573192e-06f), bc2(-1.98412698e-04f));
+    ps = fma2(r2, ps, bc2(8.33333333e-03f));
+    ps = fma2(r2, ps, bc2(-1.66666667e-01f));
+    const float2 sr = fma2(mul2(r2, r), ps, r);
+    float2 pc = fma2(r2, bc2(-2.75573192e-07f), bc2(2.48015873e-05f));
+    pc = fma2(r2, pc, bc2(-1.38888889e-03f));
+    pc = fma2(r2, pc, bc2(4.16666667e-02f));
+    pc = fma2(r2, pc, bc2(-0.5f));
+    const float2 cr = fma2(r2, pc, bc2(1.f));
+    const int qx = (int)q.x, qy = (int)q.y;
+    float ssx = (qx & 1) ? cr.x : sr.x, ccx = (qx & 1) ? sr.x : cr.x;
+    float ssy = (qy & 1) ? cr.y : sr.y, ccy = (qy & 1) ? sr.y : cr.y;
+    s = make_float2((qx & 2) ? -ssx : ssx, (qy & 2) ? -ssy : ssy);
+    c = make_float2(((qx + 1) & 2) ? -ccx : ccx, ((qy + 1) & 2) ? -ccy : ccy);
+}
+
+// Kepler's equation E - (e + elo) sin E = M + mlo on NP pairs of epochs,
+// without iteration.  Start: Mikkola's cubic approximation (Mikkola 1987,
+// Celest. Mech. 40, 329: with a = (1 - e)/(4 e + 1/2), b = M/2/(4 e + 1/2),
+// z = cbrt(b + sign(b) sqrt(b^2 + a^3)), s = z - a/z corrected by
+// -0.078 s^5/(1 + e), E0 = M + e (3 s - 4 s^3)); its error is below 4e-3
+// for e < 0.99.  One Halley step on a residual that uses sincos_acc, an
+// error-free E0 - M and the low parts of M and e then leaves an error
+// below 5e-9 (cubic convergence); (sin E, cos E) are the accurate values at
+// E0 rotated by the step.  kc = the planet's [a, a^3, 1/2/(4e+1/2),
+// 0.078/(1+e)].
+template <int NP>
+__device__ __forceinline__ void kepler_pairs(const float2 (&M)[NP], const float2 (&mlo)[NP], float e,
+                                             float elo, const float* kc, float2 (&s)[NP],
+                                             float2 (&c)[NP]) {
+    const float2 ev = bc2(e), nev = bc2(-e), one = bc2(1.f), nelo = bc2(-elo);
+    const float ka = kc[0];
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const float2 b = mul2(M[k], bc2(kc[2]));
+        const float2 x = fma2(b, b, bc2(kc[1]));                   // > 0: a > 0 for e < 1
+        float2 t, z;
+        t.x = b.x + copysignf(x.x * rsqrtf(x.x), b.x);
+        t.y = b.y + copysignf(x.y * rsqrtf(x.y), b.y);
+        z.x = copysignf(exp2f(__log2f(fabsf(t.x)) * (1.f / 3.f)), t.x);
+        z.y = copysignf(exp2f(__log2f(fabsf(t.y)) * (1.f / 3.f)), t.y);
+        float2 sm = sub2(z, make_float2(__fdividef(ka, z.x), __fdividef(ka, z.y)));
+        float2 s2 = mul2(sm, sm);
+        sm = fma2(mul2(mul2(bc2(-kc[3]), s2), s2), sm, sm);
+        s2 = mul2(sm, sm);
+        const float2 E0 = fma2(mul2(ev, sm), fma2(bc2(-4.f), s2, bc2(3.f)), M[k]);
+        float2 sa, ca;
+        sincos_acc_pair(E0, sa, ca);
+        // residual E0 - M - mlo - (e + elo) sin E0 with E0 - M exact
+        const float2 dh = sub2(E0, M[k]);
+        const float2 bv = sub2(dh, E0);
+        const float2 dl = sub2(sub2(E0, sub2(dh, bv)), add2(M[k], bv));
+        float2 f = fma2(nev, sa, dh);
+        f = add2(f, fma2(nelo, sa, sub2(dl, mlo[k])));
+        const float2 f1 = fma2(nelo, ca, fma2(nev, ca, one));
+        const float2 f2 = mul2(ev, sa);
+        const float2 den = fma2(mul2(bc2(-0.5f), f), f2, mul2(f1, f1));
+        const float2 d = mul2(mul2(f, f1), rcp_approx2(den));
+        const float2 d2 = mul2(d, d);
+        const float2 cd = fma2(bc2(-0.5f), d2, one);
+        const float2 sd = mul2(d, fma2(d2, bc2(-1.f / 6.f), one));
+        s[k] = fma2(mul2(ca, sd), bc2(-1.f), mul2(sa, cd));
+        c[k] = fma2(sa, sd, mul2(ca, cd));
     }
 }
 
@@ -716,7 +836,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     pos[e] = kk * L + ((r + kk) & (L - 1));
                     model[e] = R(0);
                 }
-                if (PREC == EMP_PREC_FP64) {
+                if constexpr (PREC == EMP_PREC_FP64) {
 #pragma unroll
                     for (int e = 0; e < NE; ++e) {
                         const double t = (double)s_t0[pos[e]];
@@ -732,26 +852,39 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                         model[e] = (R)m;
                     }
                 } else {
+                    constexpr int NP = NE / 2;
                     float th[NE], tl[NE];
 #pragma unroll
                     for (int e = 0; e < NE; ++e) { th[e] = (float)s_t0[pos[e]]; tl[e] = (float)s_t1[pos[e]]; }
+                    float2 th2[NP], tl2[NP], mod2[NP];
+#pragma unroll
+                    for (int j = 0; j < NP; ++j) {
+                        th2[j] = make_float2(th[2 * j], th[2 * j + 1]);
+                        tl2[j] = make_float2(tl[2 * j], tl[2 * j + 1]);
+                        mod2[j] = bc2(0.f);
+                    }
                     for (int p = 0; p < n_planets; ++p) {
                         const float* pc = (const float*)(pcs + p * PC);
-                        float M[NE], ml[NE], sn[NE], cs[NE];
+                        float2 M[NP], ml[NP], sn[NP], cs[NP];
 #pragma unroll
-                        for (int e = 0; e < NE; ++e) M[e] = mean_anomaly_mixed(pc, th[e], tl[e], ml[e]);
+                        for (int j = 0; j < NP; ++j) M[j] = mean_anomaly_pair(pc, th2[j], tl2[j], ml[j]);
                         const float ec = pc[4], el = pc[8];
-                        kepler_f32_n<NE>(M, ml, ec, el, sn, cs);
+                        kepler_pairs<NP>(M, ml, ec, el, pc + 12, sn, cs);
 #pragma unroll
-                        for (int e = 0; e < NE; ++e) {
+                        for (int j = 0; j < NP; ++j) {
                             // (A (cos E - e) - B sin E) / (1 - e cos E) + C with
                             // float-float A, B, C, e
-                            const float cme = __fsub_rn(__fsub_rn(cs[e], ec), el);
-                            const float inv = __frcp_rn(__fmaf_rn(-el, cs[e], __fmaf_rn(-ec, cs[e], 1.f)));
-                            const float hi = __fmaf_rn(__fmaf_rn(pc[5], cme, -pc[6] * sn[e]), inv, pc[7]);
-                            const float lo = __fmaf_rn(__fmaf_rn(pc[9], cme, -pc[10] * sn[e]), inv, pc[11]);
-                            model[e] += (R)__fadd_rn(hi, lo);
+                            const float2 cme = sub2(sub2(cs[j], bc2(ec)), bc2(el));
+                            const float2 inv = rcp_rn2(fma2(bc2(-el), cs[j], fma2(bc2(-ec), cs[j], bc2(1.f))));
+                            const float2 hi = fma2(fma2(bc2(pc[5]), cme, mul2(bc2(-pc[6]), sn[j])), inv, bc2(pc[7]));
+                            const float2 lo = fma2(fma2(bc2(pc[9]), cme, mul2(bc2(-pc[10]), sn[j])), inv, bc2(pc[11]));
+                            mod2[j] = add2(mod2[j], add2(hi, lo));
                         }
+                    }
+#pragma unroll
+                    for (int j = 0; j < NP; ++j) {
+                        model[2 * j] = (R)mod2[j].x;
+                        model[2 * j + 1] = (R)mod2[j].y;
                     }
                     if (acc_order > 0) {
 #pragma unroll

@@ -75,11 +75,17 @@ struct SwapArgs {
     int record_chain;
 };
 
+// uniform of a 32-bit word in FP32 (within 1e-7 of u32u; used only where a
+// guard band absorbs the difference)
+__device__ __forceinline__ float u32f(uint32_t w) {
+    return __fmaf_rn(__uint2float_rn(w), 2.3283064365386963e-10f, 1.1641532182693481e-10f);
+}
+
 // log(u) < x decided with an FP32 logarithm; inside a guard band around
 // the boundary the FP64 logarithm decides, so every decision equals the
 // FP64 test (the FP32 log of a 32-bit uniform is within 2e-5 of the FP64 one)
 __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
-    const float lf = __logf((float)u32u(word));
+    const float lf = __logf(u32f(word));
     const float xf = (float)x;
     const float d = xf - lf;
     const float guard = 1e-4f * (1.f + fabsf(lf)) + 1e-6f * fabsf(xf);
@@ -105,6 +111,7 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     __shared__ double s_invb[kMaxTemps];
     __shared__ double s_term[kMaxTemps];
     __shared__ double s_bused[kMaxTemps];
+    __shared__ float s_dbf[kMaxTemps];
 
     const int tid = threadIdx.x;
     const int nth = blockDim.x;
@@ -117,15 +124,20 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     int* members = S.members + (size_t)sys * TW;
     double* betas = S.betas + (size_t)sys * T;
     int* swaps_acc = S.swaps_accepted + (size_t)sys * T;
-    double* s_ll = reinterpret_cast<double*>(sm_raw);              // [T*W] logL by position
-    int* s_mem = reinterpret_cast<int*>(s_ll + (SMEM ? TW : 0));    // [T*W] slot by position
-    uint32_t* s_u = reinterpret_cast<uint32_t*>(s_mem + (SMEM ? TW : 0));  // [T*W] words
+    // staged by position: logL (FP64 and FP32), slot, random word, FP32 log
+    // of the word's uniform
+    double* s_ll = reinterpret_cast<double*>(sm_raw);
+    int* s_mem = reinterpret_cast<int*>(s_ll + (SMEM ? TW : 0));
+    float* s_lf = reinterpret_cast<float*>(s_mem + (SMEM ? TW : 0));
+    uint32_t* s_u = reinterpret_cast<uint32_t*>(s_lf + (SMEM ? TW : 0));
+    float* s_lu = reinterpret_cast<float*>(s_u + (SMEM ? TW : 0));
 
     for (int t = tid; t < T; t += nth) {
         s_bused[t] = betas[t];
         if (!BATCH) wk.betas_used[t] = betas[t];
         s_cnt[t] = 0;
         if (t >= 1) {
+            s_dbf[t] = (float)(betas[t - 1] - betas[t]);
             U4 pr = rng_draw(seed, (uint32_t)t, sweep, kRngSwapPerm);
             s_perm[t][0] = (uint32_t)S.units[pr.x % (uint32_t)S.nunits];
             s_perm[t][1] = pr.y % (uint32_t)W;
@@ -135,8 +147,12 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
         for (int k = tid; k < TW; k += nth) {
             const int sl = members[k];
             s_mem[k] = sl;
-            s_ll[k] = S.logl[sl];
-            s_u[k] = k >= W ? rng_draw(seed, (uint32_t)k, sweep, kRngSwapAcc).x : 0u;
+            const double l = S.logl[sl];
+            s_ll[k] = l;
+            s_lf[k] = (float)l;
+            const uint32_t word = k >= W ? rng_draw(seed, (uint32_t)k, sweep, kRngSwapAcc).x : 0u;
+            s_u[k] = word;
+            s_lu[k] = __logf(u32f(word));
         }
     }
     __syncthreads();
@@ -144,28 +160,53 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     for (int i = T - 1; i >= 1; --i) {
         const uint32_t m = s_perm[i][0];
         const uint32_t b = s_perm[i][1];
-        const double dbeta = betas[i - 1] - betas[i];
+        const float dbf = s_dbf[i];
         for (int j = tid; j < W; j += nth) {
-            const int jp = (int)(((uint64_t)m * (uint64_t)j + b) % (uint64_t)W);
+            // W <= 65535, so m * j + b < 2^32
+            const int jp = (int)(((uint32_t)m * (uint32_t)j + b) % (uint32_t)W);
             const int ia = i * W + j, ib = (i - 1) * W + jp;
             int sa, sb;
-            double la, lb;
-            uint32_t word;
+            bool acc;
             if (SMEM) {
-                sa = s_mem[ia]; sb = s_mem[ib]; la = s_ll[ia]; lb = s_ll[ib]; word = s_u[ia];
+                sa = s_mem[ia]; sb = s_mem[ib];
+                // log u < dbeta (la - lb), decided in FP32 outside a guard
+                // band that bounds the FP32 errors, else in FP64
+                const float lfa = s_lf[ia], lfb = s_lf[ib], lu = s_lu[ia];
+                const float xf = dbf * (lfa - lfb);
+                const float dd = xf - lu;
+                const float guard = 1e-4f * (1.f + fabsf(lu)) +
+                                    2.5e-7f * fabsf(dbf) * (fabsf(lfa) + fabsf(lfb)) + 1e-6f * fabsf(xf);
+                if (dd > guard) acc = true;
+                else if (dd < -guard) acc = false;
+                else acc = log(u32u(s_u[ia])) < (s_bused[i - 1] - s_bused[i]) * (s_ll[ia] - s_ll[ib]);
             } else {
-                sa = members[ia]; sb = members[ib]; la = S.logl[sa]; lb = S.logl[sb];
-                word = rng_draw(seed, (uint32_t)ia, sweep, kRngSwapAcc).x;
+                sa = members[ia]; sb = members[ib];
+                const double paccept = (s_bused[i - 1] - s_bused[i]) * (S.logl[sa] - S.logl[sb]);
+                acc = log_uniform_below(rng_draw(seed, (uint32_t)ia, sweep, kRngSwapAcc).x, paccept);
             }
-            const double paccept = dbeta * (la - lb);
-            if (log_uniform_below(word, paccept)) {
+            if (acc) {
                 if (SMEM) {
-                    s_mem[ia] = sb; s_mem[ib] = sa; s_ll[ia] = lb; s_ll[ib] = la;
+                    s_mem[ia] = sb; s_mem[ib] = sa;
+                    const double la = s_ll[ia];
+                    s_ll[ia] = s_ll[ib]; s_ll[ib] = la;
+                    const float lf = s_lf[ia];
+                    s_lf[ia] = s_lf[ib]; s_lf[ib] = lf;
                 } else {
                     members[ia] = sb; members[ib] = sa;
                 }
-                const int k = atomicAdd(&s_cnt[i], 1);
-                if (!BATCH) wk.pairs[i * W + k] = make_int2(sa, sb);
+            }
+            // one shared-memory atomic per warp: the warp's accepted
+            // exchanges take consecutive slots of the pair log
+            const unsigned act = __activemask();
+            const unsigned am = __ballot_sync(act, acc);
+            const int lane = tid & 31;
+            const int leader = __ffs(act) - 1;
+            int base = 0;
+            if (lane == leader && am != 0u) base = atomicAdd(&s_cnt[i], __popc(am));
+            base = __shfl_sync(act, base, leader);
+            if (acc && !BATCH) {
+                const int k = base + __popc(am & ((1u << lane) - 1u));
+                wk.pairs[i * W + k] = make_int2(sa, sb);
             }
         }
         __syncthreads();

@@ -310,6 +310,7 @@ int check_state(const emp_handle* h, const emp_pt_state* st) {
         return fail(EMP_E_SIZE, "ntemps=%d outside [1, %d]", st->ntemps, kMaxTemps);
     if (st->nwalkers < 2 || (st->nwalkers & 1))
         return fail(EMP_E_INVALID, "nwalkers=%d must be even and >= 2", st->nwalkers);
+    if (st->nwalkers > 65534) return fail(EMP_E_SIZE, "nwalkers=%d exceeds 65534", st->nwalkers);
     const int nsys = st->n_systems <= 0 ? 1 : st->n_systems;
     if (nsys != h->n_sys)
         return fail(EMP_E_INVALID, "state holds %d systems, handle %d", nsys, h->n_sys);
@@ -383,7 +384,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
     S.cap = have_rec ? rec->capacity : 0;
     S.thin = have_rec ? std::max(1, rec->thin) : 1;
     S.record_chain = have_rec && (rec->chain || rec->log_like || rec->log_prob);
-    const size_t swap_smem = (size_t)st->ntemps * st->nwalkers * 16;
+    const size_t swap_smem = (size_t)st->ntemps * st->nwalkers * 24;
     if (batch) {
         // one CTA per system; threads cover a temperature's walkers
         const int nthb = std::min(1024, std::max(128, (st->nwalkers + 31) / 32 * 32));
