@@ -146,6 +146,7 @@ struct Smem {
     int tile_bytes;        // staged epochs
     int group_bytes;       // per walker group
     int off_full, off_thp, off_pc, off_ins, off_acc, off_red, off_scan, off_pterm, off_misc;
+    int off_fullf, n_fullf;    // float-float copy of the full vector (mixed): hi [n], lo [n]
     int total;
 
     __host__ __device__ static int align16(int x) { return (x + 15) & ~15; }
@@ -158,6 +159,8 @@ struct Smem {
         tile_bytes = align16(per_epoch * tile + 64);
         int o = 0;
         off_full = o; o += align16(8 * n_full);
+        n_fullf = prec == EMP_PREC_FP64 ? 0 : n_full;
+        off_fullf = o; o += align16(8 * n_fullf);
         off_thp = o;  o += align16(8 * (n_free > 0 ? n_free : 1));
         off_pc = o;   o += align16(rs * (prec == EMP_PREC_FP64 ? 8 : 16) * (n_planets > 0 ? n_planets : 1));
         off_ins = o;  o += align16(rs * kInsW * (n_ins > 0 ? n_ins : 1));

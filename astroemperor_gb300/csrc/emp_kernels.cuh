@@ -100,6 +100,40 @@ __device__ __forceinline__ FF ff_recip(FF x) {
     return o;
 }
 
+// fast two-sum: hi + lo renormalised (|hi| >= |lo| or hi == 0)
+__device__ __forceinline__ FF ff_norm(float hi, float lo) {
+    const float sum = __fadd_rn(hi, lo);
+    FF r;
+    r.hi = sum;
+    r.lo = __fsub_rn(lo, __fsub_rn(sum, hi));
+    return r;
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const float sum = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(sum, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(sum, bb)), __fsub_rn(b.hi, bb));
+    return ff_norm(sum, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+// 1/sqrt(x), x > 0: hardware estimate and one Newton step on the exact
+// residual 1 - x r0^2 (relative error ~1e-14)
+__device__ __forceinline__ FF ff_rsqrt(FF x) {
+    const float r0 = rsqrtf(x.hi);
+    const float t = __fmul_rn(r0, r0);
+    const float te = __fmaf_rn(r0, r0, -t);
+    FF q = ff_mul(x, FF{t, te});
+    const float h = __fsub_rn(__fsub_rn(1.f, q.hi), q.lo);
+    return ff_norm(r0, __fmul_rn(__fmul_rn(0.5f, r0), h));
+}
+// sqrt(x), x >= 0, the same way
+__device__ __forceinline__ FF ff_sqrt(FF x) {
+    if (!(x.hi > 0.f)) return FF{0.f, 0.f};
+    const float s0 = x.hi * rsqrtf(x.hi);
+    const float t = __fmul_rn(s0, s0);
+    const float te = __fmaf_rn(s0, s0, -t);
+    const float d = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, t), te), x.lo);
+    return ff_norm(s0, __fmul_rn(d, __fdividef(0.5f, s0)));
+}
+
 // ----------------------------------------------------------------------------
 // per-planet constants
 // ----------------------------------------------------------------------------
@@ -115,6 +149,64 @@ __device__ __forceinline__ void planet_consts_fp64(int par, const double* v, dou
     pc[5] = el.K * el.e * el.cw;
     pc[6] = el.tp;
     pc[7] = (double)el.use_tp;
+}
+
+// planet_consts_mixed for parameterisations 0, 1, 3 and 4 from float-float
+// copies of the planet's slots (vh + vl = the FP64 values to ~2^-48): the
+// same constants in FP32 float-float arithmetic, without FP64 operations
+__device__ __forceinline__ void planet_consts_mixed_ff(int par, const float* vh, const float* vl, float* pc) {
+    const FF per{vh[0], vl[0]}, K{vh[1], vl[1]}, x2{vh[2], vl[2]};
+    FF e, cw{1.f, 0.f}, sw{0.f, 0.f};
+    if (par == 0 || par == 3) {
+        e = FF{vh[3], vl[3]};
+        float s32, c32;
+        sincosf(vh[4], &s32, &c32);
+        sw.hi = s32;
+        cw.hi = c32;
+    } else {
+        const FF S{vh[3], vl[3]}, C{vh[4], vl[4]};
+        e = ff_add(ff_mul(S, S), ff_mul(C, C));
+        // e >= 1e-6 (1e-5 for parameterisation 4) against the float-float
+        // split of the FP64 threshold
+        const float th = par == 4 ? 9.999999747378752e-06f : 9.999999974752427e-07f;
+        const float tl = par == 4 ? 2.526212474884132e-13f : 2.5247572468697606e-15f;
+        if (e.hi > th || (e.hi == th && e.lo >= tl)) {
+            const FF rs = ff_rsqrt(e);
+            cw = ff_mul(C, rs);
+            sw = ff_mul(S, rs);
+        }
+    }
+    const FF sq = ff_sqrt(ff_add(FF{1.f, 0.f}, ff_mul(FF{-e.hi, -e.lo}, e)));
+    const FF f = ff_recip(per);
+    FF ph;
+    if (par == 3 || par == 4) {
+        FF q = ff_mul(x2, f);
+        q.hi = -q.hi; q.lo = -q.lo;
+        ph = ff_frac(q);
+    } else {
+        const FF inv2pi = {0.15915493667125702f, 6.4206382432985265e-09f};   // 1/(2 pi) as float-float
+        ph = ff_frac(ff_mul(x2, inv2pi));
+    }
+    pc[0] = f.hi;
+    pc[1] = f.lo;
+    pc[2] = ph.hi;
+    pc[3] = ph.lo;
+    const FF en = ff_norm(e.hi, e.lo);
+    const FF A = ff_mul(K, cw);
+    const FF An = ff_norm(A.hi, A.lo);
+    const FF Bn = [&] { const FF b = ff_mul(ff_mul(K, sq), sw); return ff_norm(b.hi, b.lo); }();
+    const FF Cn = [&] { const FF c = ff_mul(A, en); return ff_norm(c.hi, c.lo); }();
+    pc[4] = en.hi;  pc[8] = en.lo;
+    pc[5] = An.hi;  pc[9] = An.lo;
+    pc[6] = Bn.hi;  pc[10] = Bn.lo;
+    pc[7] = Cn.hi;  pc[11] = Cn.lo;
+    const float ef = pc[4];
+    const float den = __fdividef(1.f, 4.f * ef + 0.5f);
+    const float a = (1.f - ef) * den;
+    pc[12] = a;
+    pc[13] = a * a * a;
+    pc[14] = 0.5f * den;
+    pc[15] = __fdividef(0.078f, 1.f + ef);
 }
 
 // 1/sqrt(x) and sqrt(x) to ~1e-14: FP32 estimate, one FP64 Newton step
@@ -606,6 +698,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
 
     unsigned char* gs = smem + lay.tile_bytes + g * lay.group_bytes;
     double* full = reinterpret_cast<double*>(gs + lay.off_full);
+    float* fullh = reinterpret_cast<float*>(gs + lay.off_fullf);
+    float* fulll = fullh + lay.n_fullf;
     double* thp = reinterpret_cast<double*>(gs + lay.off_thp);
     R* pcs = reinterpret_cast<R*>(gs + lay.off_pc);
     R* insc = reinterpret_cast<R*>(gs + lay.off_ins);
@@ -691,7 +785,13 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     if (active) {
         for (int s = r; s < n_full; s += L) {
             const int src = md->full_src[s];
-            full[s] = src >= 0 ? thp[src] : md->full_fixed[s];
+            const double v = src >= 0 ? thp[src] : md->full_fixed[s];
+            full[s] = v;
+            if (PREC == EMP_PREC_MIXED) {
+                const float h = (float)v;
+                fullh[s] = h;
+                fulll[s] = (float)(v - (double)h);
+            }
         }
     }
     __syncthreads();
@@ -716,8 +816,13 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
         for (int p = r; p < n_planets; p += L) {
             if (PREC == EMP_PREC_FP64)
                 planet_consts_fp64(md->kep_param[p], full + md->kep_slot[p], (double*)(pcs + p * PC));
-            else
-                planet_consts_mixed(md->kep_param[p], full + md->kep_slot[p], (float*)(pcs + p * PC));
+            else {
+                const int par = md->kep_param[p], ks = md->kep_slot[p];
+                if (par == 0 || par == 1 || par == 3 || par == 4)
+                    planet_consts_mixed_ff(par, fullh + ks, fulll + ks, (float*)(pcs + p * PC));
+                else
+                    planet_consts_mixed(par, full + ks, (float*)(pcs + p * PC));
+            }
         }
         for (int k = r; k < n_ins; k += L) {
             R* ic = insc + k * INSW;

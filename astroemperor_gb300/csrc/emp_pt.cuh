@@ -109,9 +109,9 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     __shared__ uint32_t s_perm[kMaxTemps][2];
     __shared__ double s_ratio[kMaxTemps];
     __shared__ double s_invb[kMaxTemps];
-    __shared__ double s_term[kMaxTemps];
     __shared__ double s_bused[kMaxTemps];
     __shared__ float s_dbf[kMaxTemps];
+    __shared__ double s_kappa;
 
     const int tid = threadIdx.x;
     const int nth = blockDim.x;
@@ -132,8 +132,13 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     uint32_t* s_u = reinterpret_cast<uint32_t*>(s_lf + (SMEM ? TW : 0));
     float* s_lu = reinterpret_cast<float*>(s_u + (SMEM ? TW : 0));
 
+    const bool adapt = S.adapt && T > 2;
+    // adaptation inputs that do not depend on this sweep's swaps, computed
+    // while the positions are staged
+    if (adapt && tid == nth - 1) s_kappa = S.adapt_tau / ((double)sweep + S.adapt_tau) / S.adapt_nu;
     for (int t = tid; t < T; t += nth) {
         s_bused[t] = betas[t];
+        if (adapt && t < T - 1) s_invb[t] = 1.0 / betas[t];
         if (!BATCH) wk.betas_used[t] = betas[t];
         s_cnt[t] = 0;
         if (t >= 1) {
@@ -213,57 +218,59 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     }
     if (SMEM)
         for (int k = tid; k < TW; k += nth) members[k] = s_mem[k];
-    for (int t = tid; t < T; t += nth) {
-        const int c = t >= 1 ? s_cnt[t] : 0;
+    if (tid >= 32) return;
+    // one warp: acceptance ratios, ladder adaptation (exponentials and
+    // reciprocals across lanes, the cumulative sum as a warp scan) and the
+    // histories
+    const int lane = tid;
+    for (int t = 1 + lane; t < T; t += 32) {
+        const int c = s_cnt[t];
         if (!BATCH) wk.pair_count[t] = c;
-        if (t >= 1) {
-            s_ratio[t - 1] = (double)c / (double)W;
-            swaps_acc[t] += c;
-        }
+        s_ratio[t - 1] = (double)c / (double)W;
+        swaps_acc[t] += c;
     }
-    __syncthreads();
-    // ladder adaptation, the exponentials and reciprocals in parallel
-    const bool adapt = S.adapt && T > 2;
+    if (!BATCH && lane == 0) wk.pair_count[0] = 0;
+    __syncwarp();
     if (adapt) {
-        const double kappa = S.adapt_tau / ((double)sweep + S.adapt_tau) / S.adapt_nu;
-        for (int t = tid; t < T - 1; t += nth) s_invb[t] = 1.0 / betas[t];
-        __syncthreads();
-        for (int k = tid; k < T - 2; k += nth) {
-            const double dS = kappa * (s_ratio[k] - s_ratio[k + 1]);
-            s_term[k] = __dmul_rn(s_invb[k + 1] - s_invb[k], exp(dS));
-        }
-        __syncthreads();
-        if (tid == 0) {
-            double cum = s_invb[0];
-            for (int k = 0; k < T - 2; ++k) {
-                cum = __dadd_rn(cum, s_term[k]);
-                s_term[k] = cum;
+        // 1/beta_{k+1} = 1/beta_0 + sum_{j<=k} (1/beta_{j+1} - 1/beta_j) exp(kappa (A_j - A_{j+1}))
+        const double kappa = s_kappa;
+        double carry = s_invb[0];
+        for (int k0 = 0; k0 < T - 2; k0 += 32) {
+            const int k = k0 + lane;
+            double v = 0.0;
+            if (k < T - 2)
+                v = __dmul_rn(s_invb[k + 1] - s_invb[k], exp(kappa * (s_ratio[k] - s_ratio[k + 1])));
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double u = __shfl_up_sync(0xffffffffu, v, o);
+                if (lane >= o) v = __dadd_rn(v, u);
             }
+            const double cum = __dadd_rn(carry, v);
+            if (k < T - 2) betas[k + 1] = 1.0 / cum;
+            carry = __shfl_sync(0xffffffffu, cum, 31);
         }
-        __syncthreads();
-        for (int k = tid; k < T - 2; k += nth) betas[k + 1] = 1.0 / s_term[k];
     }
 
+    const int64_t row = S.n_rec[1];
+    const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
     if (BATCH) {
         // history rows [row][S][...]; k_advance moves the row counters
-        const int64_t row = S.n_rec[1];
-        const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
         if (rec_sweep && row < S.cap) {
             const int64_t rs = row * S.n_sys + sys;
-            if (S.beta_hist) for (int t = tid; t < T; t += nth) S.beta_hist[rs * T + t] = s_bused[t];
-            if (S.tsw_hist) for (int k = tid; k < T - 1; k += nth) S.tsw_hist[rs * (T - 1) + k] = s_ratio[k];
+            if (S.beta_hist) for (int t = lane; t < T; t += 32) S.beta_hist[rs * T + t] = s_bused[t];
+            if (S.tsw_hist) for (int k = lane; k < T - 1; k += 32) S.tsw_hist[rs * (T - 1) + k] = s_ratio[k];
         }
-    } else if (tid == 0) {
-        // histories of this sweep (ladder used during the sweep)
-        const int64_t row = S.n_rec[1];
-        const bool rec_sweep = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
-        wk.rows[1] = -1;
-        if (rec_sweep && row < S.cap) {
-            if (S.beta_hist) for (int t = 0; t < T; ++t) S.beta_hist[row * T + t] = s_bused[t];
-            if (S.tsw_hist) for (int k = 0; k < T - 1; ++k) S.tsw_hist[row * (T - 1) + k] = s_ratio[k];
-            if (S.have_smd) wk.rows[1] = row;
-            S.n_rec[1] = row + 1;
-        }
+        return;
+    }
+    // histories of this sweep (ladder used during the sweep)
+    const bool hist = rec_sweep && row < S.cap;
+    if (hist) {
+        if (S.beta_hist) for (int t = lane; t < T; t += 32) S.beta_hist[row * T + t] = s_bused[t];
+        if (S.tsw_hist) for (int k = lane; k < T - 1; k += 32) S.tsw_hist[row * (T - 1) + k] = s_ratio[k];
+    }
+    if (lane == 0) {
+        wk.rows[1] = (hist && S.have_smd) ? row : -1;
+        if (hist) S.n_rec[1] = row + 1;
         const int64_t crow = S.n_rec[0];
         if (S.record_chain && rec_sweep && crow < S.cap) {
             wk.rows[0] = crow;
