@@ -6,8 +6,8 @@ the epoch tile staged in shared memory.  The best pair depends on the batch
 (walkers per launch), the number of epochs and the model (planets, MA
 order): few walkers want many lanes each, long series want the largest
 tile that still leaves room for several CTAs per SM.  ``autotune`` times
-every candidate on a representative batch with CUDA events on its own
-stream, keeps the fastest, sets it on the handle and caches the choice per
+every candidate on a representative batch (launches captured in a CUDA
+graph, timed with events on its own stream), keeps the fastest, sets it on the handle and caches the choice per
 (model shape, batch, precision).
 """
 from __future__ import annotations
@@ -45,20 +45,39 @@ def candidates(n_epochs, batch):
     return out
 
 
+def graph_time(args, reps, stream):
+    """Device milliseconds per ``emp_logpost(*args)`` launch: ``reps``
+    launches (fewer for launches above ~5 ms) captured in one CUDA graph and
+    replayed between two events, so that host-side call overhead does not
+    enter the measurement."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        N.call('emp_logpost', *args)                               # warm, sets attributes
+        e1.record(stream)
+    e1.synchronize()
+    reps = int(max(1, min(reps, round(20.0 / max(e0.elapsed_time(e1), 1e-3)))))
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        for _ in range(reps):
+            N.call('emp_logpost', *args)
+    g.replay()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        g.replay()
+        e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def time_launch(ctx, theta, precision, reps, stream):
     B = theta.shape[0]
     ll = torch.empty(B, dtype=torch.float64, device=theta.device)
     lp = torch.empty_like(ll)
     args = (ctx.h, theta.data_ptr(), B, None, None, ll.data_ptr(), lp.data_ptr(), None,
             int(precision), stream.cuda_stream)
-    N.call('emp_logpost', *args)                                   # warm
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        N.call('emp_logpost', *args)
-    e1.record(stream)
-    e1.synchronize()
-    return e0.elapsed_time(e1) / reps
+    return graph_time(args, reps, stream)
 
 
 def autotune(ctx, theta, precision=N.EMP_PREC_MIXED, reps=None, use_cache=True, verbose=False):
@@ -76,8 +95,7 @@ def autotune(ctx, theta, precision=N.EMP_PREC_MIXED, reps=None, use_cache=True, 
     stream = torch.cuda.Stream(device=theta.device)
     n = len(ctx._t)
     if reps is None:
-        # aim for ~2 ms of timing per candidate, at least 2 repetitions
-        reps = 3
+        reps = 8
     best = None
     results = []
     seen = set()
@@ -130,14 +148,7 @@ def autotune_batch(ctx, theta, precision=N.EMP_PREC_MIXED, reps=3, verbose=False
         seen.add(eff)
         args = (ctx.h, theta.data_ptr(), B, None, None, ll.data_ptr(), lp.data_ptr(), None,
                 int(precision), stream.cuda_stream)
-        N.call('emp_logpost', *args)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            N.call('emp_logpost', *args)
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1) / reps
+        ms = graph_time(args, reps, stream)
         if verbose:
             print(f'autotune batch L={eff[0]:4d} tile={eff[1]:5d} {ms:9.3f} ms')
         if best is None or ms < best[0]:

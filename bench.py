@@ -293,17 +293,11 @@ def main_ragged(args):
     # one launch of the same kernel and launch shape, timed alone
     half = torch.as_tensor(p0.reshape(ctx.S, T * W, ctx.ndim)[:, : T * W // 2].copy(), device=dev)
     rs = torch.cuda.Stream(device=dev)
-    with torch.cuda.stream(rs):
-        for _ in range(3):
-            ctx.logpost(half, precision=N.EMP_PREC_MIXED, stream=rs)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(rs)
-        reps = 10
-        for _ in range(reps):
-            ctx.logpost(half, precision=N.EMP_PREC_MIXED, stream=rs)
-        e1.record(rs)
-    torch.cuda.synchronize()
-    k_ms = e0.elapsed_time(e1) / reps
+    from astroemperor_gb300.autotune import graph_time
+    hll = torch.empty(ctx.S, T * W // 2, dtype=torch.float64, device=dev)
+    hlp = torch.empty_like(hll)
+    k_ms = graph_time((ctx.h, half.data_ptr(), T * W // 2, None, None, hll.data_ptr(), hlp.data_ptr(),
+                       None, N.EMP_PREC_MIXED, rs.cuda_stream), 10, rs)
     F = 58 * kps + 10
     flops_launch = float(np.sum(F * n_ep)) * (T * W // 2)
     f32, f64p = C.c_double(), C.c_double()
@@ -493,26 +487,15 @@ def main():
     fp64_value = units_per_sweep * fp64_steps / (ms_fp64 / 1e3)
 
     # ---- roofline of the dominant kernel: one half-step of the stretch move
-    # (T*W/2 walkers x N epochs), timed alone with events on its stream
+    # (T*W/2 walkers x N epochs), launches captured in a CUDA graph and timed
+    # with events on their stream
     th_half = torch.as_tensor(p0.reshape(-1, D)[: T * W // 2], dtype=torch.float64, device=dev)
     ll = torch.empty(th_half.shape[0], dtype=torch.float64, device=dev)
     lp = torch.empty_like(ll)
     rs = torch.cuda.Stream(device=dev)
-    reps = 50
-    for prec in (N.EMP_PREC_MIXED,):
-        for _ in range(5):
-            N.call('emp_logpost', ctx.h, th_half.data_ptr(), th_half.shape[0], None, None,
-                   ll.data_ptr(), lp.data_ptr(), None, prec, rs.cuda_stream)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(rs):
-            e0.record(rs)
-        for _ in range(reps):
-            N.call('emp_logpost', ctx.h, th_half.data_ptr(), th_half.shape[0], None, None,
-                   ll.data_ptr(), lp.data_ptr(), None, prec, rs.cuda_stream)
-        with torch.cuda.stream(rs):
-            e1.record(rs)
-        torch.cuda.synchronize()
-        k_ms = e0.elapsed_time(e1) / reps
+    from astroemperor_gb300.autotune import graph_time
+    k_ms = graph_time((ctx.h, th_half.data_ptr(), th_half.shape[0], None, None, ll.data_ptr(),
+                       lp.data_ptr(), None, N.EMP_PREC_MIXED, rs.cuda_stream), 50, rs)
     kp, q = model.kplan__, ma_order(model)
     F = 58 * kp + 10 + 7 * q                                   # FLOP per eval*epoch
     flops_launch = F * (T * W // 2) * n
