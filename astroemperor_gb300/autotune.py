@@ -61,9 +61,11 @@ def graph_time(args, reps, stream):
     with torch.cuda.graph(g, stream=stream):
         for _ in range(reps):
             N.call('emp_logpost', *args)
-    g.replay()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # replay() launches on the current stream: keep the warm-up and the
+    # timed replay on the same stream so that they cannot overlap
     with torch.cuda.stream(stream):
+        g.replay()
         e0.record(stream)
         g.replay()
         e1.record(stream)

@@ -54,6 +54,8 @@ def parse():
     p.add_argument('--no-cpu-baseline', action='store_true')
     p.add_argument('--cpu-seconds', type=float, default=15.0)
     p.add_argument('--config', default=CONFIG, choices=sorted(WORKLOADS))
+    p.add_argument('--launch', default=None,
+                   help='lanes,tile for the mixed kernel instead of the autotuner (e.g. 64,1024)')
     return p.parse_args()
 
 
@@ -249,9 +251,14 @@ def main_ragged(args):
     p0 = ctx.pad(ragged_p0(models, [th for _, _, th in sy], T, W, rng))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
+    fixed = tuple(int(x) for x in args.launch.split(',')) if args.launch else None
+
     def timed(precision, steps, warmup):
         bt = BatchPTSampler(ctx, ntemps=T, nwalkers=W, precision=precision, seed=SEED + rank,
-                            record=False)
+                            record=False, autotune=not (fixed and precision == 'mixed'))
+        if fixed and precision == 'mixed':
+            ctx.set_launch(N.EMP_PREC_MIXED, *fixed)
+            bt.launch = ctx.get_launch(N.EMP_PREC_MIXED) + (None,)
         bt.run(p0, nsweeps=max(warmup, 1))               # autotunes, then warms up
         st = bt._state_struct(nsteps)
         stream = bt.stream
@@ -440,8 +447,14 @@ def main():
                  lim[:, 0], lim[:, 1])
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
+    fixed = tuple(int(x) for x in args.launch.split(',')) if args.launch else None
+
     def timed_sweeps(precision, steps, warmup):
-        s = PTSampler(W, D, model, ntemps=T, precision=precision, seed=SEED + rank, context=ctx)
+        s = PTSampler(W, D, model, ntemps=T, precision=precision, seed=SEED + rank, context=ctx,
+                      autotune=not (fixed and precision == 'mixed'))
+        if fixed and precision == 'mixed':
+            ctx.set_launch(N.EMP_PREC_MIXED, *fixed)
+            s.launch = ctx.get_launch(N.EMP_PREC_MIXED) + (None,)
         s.run_mcmc(p0, nsweeps=max(warmup, 1))          # warms up
         s._grow(steps + 2)
         st = s._state_struct(nsteps)
@@ -508,6 +521,7 @@ def main():
             'frac': achieved / peak32, 'traffic': None,
             'kernel': 'k_logpost<MIXED,Q=1> (stretch half-step shape)',
             'kernel_ms': k_ms, 'flop_per_eval_epoch': F,
+            'launch': {'lanes': s_mixed.launch[0], 'tile': s_mixed.launch[1]} if s_mixed.launch else None,
             'peak_source': 'measured on this GPU by the library FMA probe (MEASURED_PEAKS.json '
                            'has no CUDA-core figure); compute-issue bound, not HBM or tensor',
             'fp64_peak_tflops': f64p.value / 1e12}
