@@ -166,7 +166,8 @@ struct Smem {
         off_ins = o;  o += align16(rs * kInsW * (n_ins > 0 ? n_ins : 1));
         off_acc = o;  o += align16(8 * (acc_order > 0 ? acc_order : 1));
         off_red = o;  o += align16(8 * 4 * ((L + 31) / 32));
-        off_scan = o; o += align16(rs * 2 * (kMaxQ + kMaxQ * kMaxQ) * L);
+        // MA scan: warp totals [L/32][q + q^2] when a walker spans several warps
+        off_scan = o; o += align16((L > 32 && q > 0) ? rs * (L / 32) * (q + q * q) : 0);
         off_pterm = o; o += align16(8 * (n_free + 2 * n_planets + 1));
         off_misc = o; o += 64;
         group_bytes = align16(o);
