@@ -25,6 +25,10 @@ EMP_E_UNSUPPORTED = -3
 EMP_E_SIZE = -4
 EMP_E_STATE = -5
 
+EMP_TERM_SINUSOID = 8
+EMP_TERM_CYCLE_1 = 9
+EMP_TERM_CYCLE_2 = 10
+
 EMP_PREC_FP64 = 0
 EMP_PREC_MIXED = 1
 

@@ -193,6 +193,14 @@ static __device__ Elements planet_elements(int par, const double* v) {
     Elements el;
     el.use_tp = 0; el.tp = 0.0;
     switch (par) {
+        case EMP_TERM_SINUSOID: case EMP_TERM_CYCLE_1: case EMP_TERM_CYCLE_2: {
+            // A cos(2 pi t / per' + phase) as an e = 0 Keplerian; the first
+            // magnetic-cycle term runs at pi / per, i.e. per' = 2 per (exact)
+            el.per = par == EMP_TERM_CYCLE_1 ? 2.0 * v[0] : v[0];
+            el.K = par == EMP_TERM_CYCLE_2 ? v[2] : v[1];
+            el.phase = par == EMP_TERM_SINUSOID ? v[2] : (par == EMP_TERM_CYCLE_1 ? v[3] : v[4]);
+            el.e = 0.0; el.cw = 1.0; el.sw = 0.0;
+        } break;
         case 0: case 6: {
             el.per = par == 6 ? exp(v[0]) : v[0];
             el.K = v[1]; el.phase = v[2]; el.e = v[3];

@@ -155,9 +155,16 @@ __device__ __forceinline__ void planet_consts_fp64(int par, const double* v, dou
 // copies of the planet's slots (vh + vl = the FP64 values to ~2^-48): the
 // same constants in FP32 float-float arithmetic, without FP64 operations
 __device__ __forceinline__ void planet_consts_mixed_ff(int par, const float* vh, const float* vl, float* pc) {
-    const FF per{vh[0], vl[0]}, K{vh[1], vl[1]}, x2{vh[2], vl[2]};
-    FF e, cw{1.f, 0.f}, sw{0.f, 0.f};
-    if (par == 0 || par == 3) {
+    FF per{vh[0], vl[0]}, K{vh[1], vl[1]}, x2{vh[2], vl[2]};
+    FF e{0.f, 0.f}, cw{1.f, 0.f}, sw{0.f, 0.f};
+    if (par >= EMP_TERM_SINUSOID) {
+        // cosine terms: e = 0 Keplerians (period doubled exactly for the
+        // first magnetic-cycle term)
+        if (par == EMP_TERM_CYCLE_1) { per.hi *= 2.f; per.lo *= 2.f; }
+        if (par == EMP_TERM_CYCLE_2) K = FF{vh[2], vl[2]};
+        if (par == EMP_TERM_CYCLE_1) x2 = FF{vh[3], vl[3]};
+        if (par == EMP_TERM_CYCLE_2) x2 = FF{vh[4], vl[4]};
+    } else if (par == 0 || par == 3) {
         e = FF{vh[3], vl[3]};
         float s32, c32;
         sincosf(vh[4], &s32, &c32);
@@ -818,7 +825,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                 planet_consts_fp64(md->kep_param[p], full + md->kep_slot[p], (double*)(pcs + p * PC));
             else {
                 const int par = md->kep_param[p], ks = md->kep_slot[p];
-                if (par == 0 || par == 1 || par == 3 || par == 4)
+                if (par == 0 || par == 1 || par == 3 || par == 4 || par >= EMP_TERM_SINUSOID)
                     planet_consts_mixed_ff(par, fullh + ks, fulll + ks, (float*)(pcs + p * PC));
                 else
                     planet_consts_mixed(par, full + ks, (float*)(pcs + p * PC));

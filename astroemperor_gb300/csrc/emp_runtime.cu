@@ -136,12 +136,20 @@ int validate_model(const emp_model_desc* m) {
         return fail(EMP_E_SIZE, "acceleration order %d outside [0, 8]", m->acc_order);
     for (int p = 0; p < m->n_planets; ++p) {
         int par = m->kep_param[p];
-        if (!(par == 0 || par == 1 || par == 2 || par == 3 || par == 4 || par == 6 || par == 7))
+        if (!(par == 0 || par == 1 || par == 2 || par == 3 || par == 4 || par == 6 || par == 7 ||
+              par == EMP_TERM_SINUSOID || par == EMP_TERM_CYCLE_1 || par == EMP_TERM_CYCLE_2))
             return fail(EMP_E_UNSUPPORTED, "planet %d: parameterisation %d not built", p, par);
-        if (m->kep_slot[p] < 0 || m->kep_slot[p] + 5 > m->n_full)
+        const int nslot = par == EMP_TERM_SINUSOID ? 3 : 5;
+        if (m->kep_slot[p] < 0 || m->kep_slot[p] + nslot > m->n_full)
             return fail(EMP_E_INVALID, "planet %d: slot %d out of range", p, m->kep_slot[p]);
-        if (p > 0 && m->kep_slot[p] < m->kep_slot[p - 1] + 5)
-            return fail(EMP_E_INVALID, "planet %d: slots overlap", p);
+        if (p > 0) {
+            const int pp = m->kep_param[p - 1];
+            // the two terms of a magnetic-cycle block share its slots
+            const bool shared = par == EMP_TERM_CYCLE_2 && pp == EMP_TERM_CYCLE_1 &&
+                                m->kep_slot[p] == m->kep_slot[p - 1];
+            if (!shared && m->kep_slot[p] < m->kep_slot[p - 1] + (pp == EMP_TERM_SINUSOID ? 3 : 5))
+                return fail(EMP_E_INVALID, "planet %d: slots overlap", p);
+        }
         for (int k = 0; k < 2; ++k) {
             int rc = validate_prior(m->derived[p][k], "derived prior of planet", p);
             if (rc) return rc;

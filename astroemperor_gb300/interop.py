@@ -12,8 +12,8 @@ from __future__ import annotations
 import numpy as np
 
 from .data import RVData
-from .model import (AccelerationBlock, JitterBlock, KeplerianBlock, MOAVBlock, OffsetBlock,
-                    Parameter, ReddModel)
+from .model import (AccelerationBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock, MOAVBlock,
+                    OffsetBlock, Parameter, ReddModel, SinusoidBlock)
 
 
 def data_from_frame(df, labels=None, common_t=0.0) -> RVData:
@@ -67,7 +67,21 @@ def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False) -> ReddM
             nb = MOAVBlock(int(b.number_), {'order': int(b.moav), 'global': bool(b.is_global)})
         elif t == 'Acceleration':
             nb = AccelerationBlock(len(b))
+        elif t == 'Sinusoid':
+            nb = SinusoidBlock(int(b.number_))
+        elif t == 'MagneticCycle':
+            nb = MagneticCycleBlock(int(b.number_))
         else:
             raise ValueError(f'block type {t!r} is not on the GPU hot path')
         out.append(_copy_params(b, nb))
+    # the reference appends sinusoid and magnetic-cycle blocks after the MOAV
+    # block (emp.py:2633-2650).  Its per-instrument MOAV is a no-op, so with
+    # the reference quirk the order does not matter and the cosine blocks move
+    # ahead of it; with a live MA the model is rejected by ReddModel.
+    ma = [i for i, b in enumerate(out) if b.type_ == 'MOAV']
+    if ma and moav_reference_quirk and not out[ma[0]].is_global:
+        cos = [b for b in out[ma[0]:] if b.type_ in ('Sinusoid', 'MagneticCycle')]
+        rest = [b for b in out if b not in cos]
+        k = next(i for i, b in enumerate(rest) if b.type_ == 'MOAV')
+        out = rest[:k] + cos + rest[k:]
     return ReddModel(out, data, moav_reference_quirk=moav_reference_quirk)

@@ -184,6 +184,26 @@ def AccelerationBlock(order: int) -> Parameter_Block:
                            class_='Data', number_=order)
 
 
+def SinusoidBlock(number: int) -> Parameter_Block:
+    """block_repo.py:75-100: A cos(2 pi t / P + phase)."""
+    ps = [Parameter(k) for k in ('dPeriod', 'dAmplitude', 'dPhase')]
+    if number:
+        for p in ps:
+            p.name += f' {number}'
+    return Parameter_Block(ps, name_='SinusoidBlock', type_='Sinusoid', class_='Model',
+                           number_=number)
+
+
+def MagneticCycleBlock(number: int) -> Parameter_Block:
+    """block_repo.py:275-315: A1 cos(pi t / P + phase1) + A2 cos(2 pi t / P + phase2);
+    parameter names carry the reference's S1/S2 suffixes."""
+    ps = [Parameter(k) for k in ('dPeriod', 'dAmplitude', 'dAmplitude', 'dPhase', 'dPhase')]
+    for p, suf in zip(ps, ('S1', 'S1', 'S2', 'S1', 'S2')):
+        p.name += f' {suf}'
+    return Parameter_Block(ps, name_='MagneticCycleBlock', type_='MagneticCycle', class_='Model',
+                           number_=number)
+
+
 class SmartSetter:
     """Data-derived default limits and priors (block_repo.py:505-868)."""
 
@@ -272,6 +292,18 @@ class SmartSetter:
                 prargs += [None, None]
         return lims, priors, prargs
 
+    def set_Sinusoid(self, b, **kw):
+        """block_repo.py:805-817."""
+        amp, per = self._amp_per()
+        lims = [[1.5, per], [1e-6, amp], list(self.angular)]
+        return lims, ['Uniform'] * 3, [None] * 3
+
+    def set_MagneticCycle(self, b, **kw):
+        """block_repo.py:819-833."""
+        amp, per = self._amp_per()
+        lims = [[1.5, per], [1e-6, amp], [1e-6, amp], list(self.angular), list(self.angular)]
+        return lims, ['Uniform'] * 5, [None] * 5
+
     def set_Acceleration(self, b, **kw):
         return [[-1, 1]] * b.number_, ['Uniform'] * b.number_, [None] * b.number_
 
@@ -318,7 +350,7 @@ class ReddModel:
     free (``C_``) and fixed (``A_``) index maps, ``ndim__``.
     """
 
-    HOT_TYPES = ('Keplerian', 'Acceleration', 'Offset', 'Jitter', 'MOAV')
+    HOT_TYPES = ('Keplerian', 'Acceleration', 'Offset', 'Jitter', 'MOAV', 'Sinusoid', 'MagneticCycle')
 
     def __init__(self, blocks, data, moav_reference_quirk=False):
         self.blocks = list(blocks)
@@ -352,8 +384,10 @@ class ReddModel:
         for b in self.blocks:
             if b.type_ == 'MOAV':
                 seen_moav = True
-            elif seen_moav and b.type_ in ('Keplerian', 'Acceleration', 'Offset'):
-                raise ValueError('MOAV block must follow the Keplerian, acceleration and offset blocks')
+            elif seen_moav and b.type_ in ('Keplerian', 'Acceleration', 'Offset', 'Sinusoid',
+                                           'MagneticCycle'):
+                raise ValueError('MOAV block must follow the Keplerian, sinusoid, magnetic-cycle, '
+                                 'acceleration and offset blocks')
 
     # plain dict spec (used by the CPU oracle in tests)
     def spec(self) -> dict:
@@ -405,6 +439,17 @@ class ReddModel:
                     elif ap.name[:3] == 'Amp':
                         md.derived[planet][1] = prior_struct(ap.prior, ap.limits, ap.prargs)
                 planet += 1
+            elif b.type_ in ('Sinusoid', 'MagneticCycle'):
+                # cosine terms: e = 0 Keplerian terms of the kernel (kinds 8, 9, 10)
+                kinds = (N.EMP_TERM_SINUSOID,) if b.type_ == 'Sinusoid' else (N.EMP_TERM_CYCLE_1, N.EMP_TERM_CYCLE_2)
+                for kind in kinds:
+                    if planet >= N.EMP_MAX_PLANETS:
+                        raise ValueError('too many Keplerian and cosine terms')
+                    md.kep_param[planet] = kind
+                    md.kep_slot[planet] = s0
+                    md.derived[planet][0] = prior_struct('None', None, None)
+                    md.derived[planet][1] = prior_struct('None', None, None)
+                    planet += 1
             elif b.type_ == 'Offset':
                 md.offset_slot = s0
             elif b.type_ == 'Jitter':

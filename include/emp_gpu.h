@@ -43,6 +43,16 @@ extern "C" {
 #define EMP_E_SIZE        -4   /* a size is beyond a documented limit */
 #define EMP_E_STATE       -5   /* call order / handle state */
 
+/* Cosine terms carried in kep_param next to the Keplerian parameterisations
+   0-4, 6, 7 (support/models/kep0*.model): sinusoid00.model (slots: period,
+   amplitude, phase) and the two terms of magneticcycle00.model (slots:
+   period, amplitude 1, amplitude 2, phase 1, phase 2; term 1 at half the
+   frequency).  Both terms of a magnetic-cycle block use the block's first
+   slot as kep_slot. */
+#define EMP_TERM_SINUSOID 8
+#define EMP_TERM_CYCLE_1 9
+#define EMP_TERM_CYCLE_2 10
+
 /* precision of the log-posterior */
 #define EMP_PREC_FP64   0  /* plain FP64 everywhere */
 #define EMP_PREC_MIXED  1  /* FP32 Kepler solve + RV sum; float-float phase;
@@ -85,7 +95,7 @@ typedef struct emp_model_desc {
     int32_t ma_slot;
     int32_t acc_slot;
     int32_t _pad0;
-    int32_t kep_param[EMP_MAX_PLANETS];   /* parameterisation 0,1,2,3,4,6,7 */
+    int32_t kep_param[EMP_MAX_PLANETS];   /* parameterisation 0,1,2,3,4,6,7 or EMP_TERM_* */
     int32_t kep_slot[EMP_MAX_PLANETS];    /* first full-theta index of planet */
     int32_t full_src[EMP_MAX_PARAMS];     /* free index feeding slot, -1 = fixed */
     double  full_fixed[EMP_MAX_PARAMS];   /* value of fixed slots */

@@ -331,6 +331,18 @@ class OracleRV:
                     model0 += A * (np.cos(f + w) + ecc * np.cos(w))
                 else:
                     model0 += kepler_rv(X_, per, A, phase, ecc, w)
+            elif t == 'Sinusoid':                              # sinusoid00.model:2-7
+                per, A, phase = theta[sl]
+                freq = 2. * np.pi / per
+                M = freq * X_ + phase
+                model0 += A * np.cos(M)
+            elif t == 'MagneticCycle':                         # magneticcycle00.model:2-11
+                per, A1, A2, phase1, phase2 = theta[sl]
+                freq2 = 2. * np.pi / per
+                freq1 = np.pi / per
+                M1 = freq1 * X_ + phase1
+                M2 = freq2 * X_ + phase2
+                model0 += A1 * np.cos(M1) + A2 * np.cos(M2)
             elif t == 'Acceleration':                          # acc.model:2
                 model0 += np.polyval(np.concatenate([theta[sl], [0]]), (X_ - X_[0]))
             elif t == 'Offset':                                # offset00.model:3

@@ -11,8 +11,9 @@ from __future__ import annotations
 import numpy as np
 
 from astroemperor_gb300.data import preprocess_instruments
-from astroemperor_gb300.model import (AccelerationBlock, JitterBlock, KeplerianBlock, MOAVBlock,
-                                      OffsetBlock, ReddModel, SmartSetter)
+from astroemperor_gb300.model import (AccelerationBlock, JitterBlock, KeplerianBlock,
+                                      MagneticCycleBlock, MOAVBlock, OffsetBlock, ReddModel,
+                                      SinusoidBlock, SmartSetter)
 from astroemperor_gb300 import synth
 
 # the 51 Peg fit recorded by the reference (tests/01_51peg_basic.ipynb:548-562)
@@ -31,7 +32,8 @@ def _kep(ss, par, number, **lims):
     return kb
 
 
-def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=None, quirk=False):
+def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=None, quirk=False,
+                sinusoid=False, cycle=False):
     data = peg_data(arr)
     ss = SmartSetter(data)
     blocks = []
@@ -51,6 +53,14 @@ def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=N
             kb[3].fixed = 0.0
             kb[4].fixed = 0.0
         blocks.append(kb)
+    if sinusoid:
+        sb = SinusoidBlock(1)
+        ss(sb)
+        blocks.append(sb)
+    if cycle:
+        cb = MagneticCycleBlock(1)
+        ss(cb)
+        blocks.append(cb)
     if acc:
         ab = AccelerationBlock(acc)
         ss(ab)
@@ -116,4 +126,9 @@ def kat_case_models(arr):
     for name, quirk in (('c2_ma1', False), ('c2_ma1_quirk', True)):
         m, d, setup, truth = synth.build_model('c2', seed=7, moav_reference_quirk=quirk)
         add(name, m, d, center=truth)
+    # trend blocks: sinusoid00.model and magneticcycle00.model
+    m, d = model_51peg(arr, k=1, par=1, sinusoid=True)
+    add('51peg_k1_sin', m, d, center=PEG_MAP_P1[:5] + [800.0, 3.0, 1.0] + PEG_MAP_P1[5:])
+    m, d = model_51peg(arr, k=1, par=0, cycle=True, moav={'order': 1, 'global': True})
+    add('51peg_k1_cycle_gma1', m, d)
     return cases

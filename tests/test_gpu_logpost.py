@@ -99,7 +99,8 @@ def test_nan_theta_gives_minus_inf(models, contexts):
 
 
 def test_model_eval_matches_oracle(models, contexts):
-    for name in ('51peg_k1_p1', 'c2_ma1', 'c2_ma1_quirk', '51peg_gma2', '51peg_fixed_acc', '51peg_k1_p3'):
+    for name in ('51peg_k1_p1', 'c2_ma1', 'c2_ma1_quirk', '51peg_gma2', '51peg_fixed_acc', '51peg_k1_p3',
+                 '51peg_k1_sin', '51peg_k1_cycle_gma1'):
         m, d, th = models[name]
         o = OracleRV(m.spec(), d.as_dict())
         good = np.array([t for t in th if np.isfinite(o.my_prior(t))][:5])

@@ -6,7 +6,7 @@ from astroemperor_gb300 import _native as N
 from astroemperor_gb300.model import MOAVBlock, ReddModel, SmartSetter, full_theta
 from astroemperor_gb300 import synth
 from oracle.rv import OracleRV
-from tests.golden.cases import model_51peg
+from tests.golden.cases import PEG_MAP_P1, model_51peg
 
 
 def test_smartsetter_defaults_51peg(peg_arr):
@@ -92,3 +92,40 @@ def test_synthetic_configs_shapes():
     model, data, setup, truth = synth.build_model('c2')
     assert model.ndim__ == 3 * 5 + 2 + 2 + 2 * 2      # 23: two (Phi, tau) pairs
     assert setup == [10, 256, 2000, 1]
+
+
+def test_trend_blocks_descriptor_and_oracle(peg_arr):
+    """sinusoid00 / magneticcycle00 compile to cosine terms; the oracle's
+    model equals the templates' formulas."""
+    from astroemperor_gb300 import _native as N
+    from oracle.rv import OracleRV
+    from tests.golden.cases import model_51peg
+    m, d = model_51peg(peg_arr, k=1, par=1, sinusoid=True, cycle=True)
+    md = m.descriptor()
+    assert md.n_planets == 4
+    assert list(md.kep_param[:4]) == [1, N.EMP_TERM_SINUSOID, N.EMP_TERM_CYCLE_1, N.EMP_TERM_CYCLE_2]
+    assert list(md.kep_slot[:4]) == [0, 5, 8, 8]
+    names = [p.name for p in m.free_parameters()]
+    assert names[5:13] == ['Period 1', 'Amplitude 1', 'Phase 1', 'Period S1', 'Amplitude S1',
+                           'Amplitude S2', 'Phase S1', 'Phase S2']
+    span = d.BJD.max() - d.BJD.min()
+    assert m.blocks[1][0].limits == [1.5, span]
+    o = OracleRV(m.spec(), d.as_dict())
+    th = np.array(PEG_MAP_P1[:5] + [700.0, 2.0, 0.5, 1100.0, 1.5, 0.7, 2.0, 4.0] + PEG_MAP_P1[5:])
+    model, _ = o.my_model(th)
+    m0, _ = OracleRV(model_51peg(peg_arr, k=1, par=1)[0].spec(), d.as_dict()).my_model(
+        np.array(PEG_MAP_P1))
+    X = d.BJD
+    want = (m0 + 2.0 * np.cos(2 * np.pi / 700.0 * X + 0.5)
+            + 1.5 * np.cos(np.pi / 1100.0 * X + 2.0) + 0.7 * np.cos(2 * np.pi / 1100.0 * X + 4.0))
+    np.testing.assert_allclose(model, want, rtol=1e-13, atol=1e-12)
+
+
+def test_trend_blocks_must_precede_moav(peg_arr):
+    from astroemperor_gb300.model import MOAVBlock, ReddModel, SinusoidBlock, SmartSetter
+    from tests.golden.cases import model_51peg
+    m, d = model_51peg(peg_arr, k=1, par=1, moav={'order': 1, 'global': True})
+    sb = SinusoidBlock(1)
+    SmartSetter(d)(sb)
+    with pytest.raises(ValueError, match='MOAV block must follow'):
+        ReddModel(m.blocks + [sb], d)
