@@ -4,12 +4,13 @@ multistart MAP.
 
 Gradient error measure: per walker, the relative error of the gradient with
 respect to the prior-width-scaled parameters (theta_j - lo_j)/(hi_j - lo_j),
-e = ||(g - g_ref) w|| / ||g_ref w|| with w = hi - lo.  Asserted: median
-e <= 1e-6, 99th percentile <= 1e-5, maximum <= 1e-4.  The forward pass is
-FP32: components whose per-epoch terms cancel strongly (period and phase,
-whose terms oscillate over hundreds of orbital cycles) inherit the ~1e-7
-precision of the FP32 mean anomaly amplified by the cancellation, so the
-worst walkers reach a few 1e-5 (printed, with the component-wise errors).
+e = ||(g - g_ref) w|| / ||g_ref w|| with w = hi - lo.  Asserted on the C4
+model at 1000 prior draws: median e <= 1e-6, 99th percentile and maximum
+<= 1e-5 (measured: 1.6e-7, 1.7e-6, 3.0e-6).  The forward pass is FP32:
+components whose per-epoch terms cancel strongly (period and phase, whose
+terms oscillate over hundreds of orbital cycles) inherit the ~1e-7
+precision of the FP32 mean anomaly amplified by the cancellation; their
+component-wise errors are printed.
 """
 import numpy as np
 import pytest
@@ -73,7 +74,7 @@ def test_gradient_matches_fp64_autograd(peg_arr, lib, cuda, name):
     serr = _scaled_err(gl, ref_g, m)
     print(name, 'scaled norm error max', serr.max(), '| component error max', err.max(),
           'median', np.median(err))
-    assert np.median(serr) <= 1e-6 and serr.max() <= 1e-4, (name, np.median(serr), serr.max())
+    assert np.median(serr) <= 1e-6 and serr.max() <= 2e-5, (name, np.median(serr), serr.max())
     np.testing.assert_allclose(lp.cpu().numpy(), [o.my_prior(x) for x in th], rtol=1e-13, atol=1e-13)
 
 
@@ -113,7 +114,7 @@ def test_c4_gradient_at_1000_prior_draws(lib, cuda):
     print('C4 gradient: 99th percentile', np.percentile(serr, 99))
     assert np.median(serr) <= 1e-6
     assert np.percentile(serr, 99) <= GRAD_RTOL
-    assert serr.max() <= 1e-4
+    assert serr.max() <= GRAD_RTOL
     # central finite differences (h = 1e-6 relative) on the FP64 oracle for a
     # few draws; period components excluded (their second derivative makes
     # the 1e-6 step's truncation error larger than the tolerance)
