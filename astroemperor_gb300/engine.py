@@ -497,8 +497,13 @@ class PTSampler:
         ll = self.get_log_like(discard=discard)
         return thermodynamic_integration(self.betas, ll, pchip=pchip)
 
+    def get_evidence_ss(self, discard=0):
+        """Stepping-stone log-evidence and its error (``stats.stepping_stone``)."""
+        from .stats import stepping_stone
+        return stepping_stone(self.betas, self.get_log_like(discard=discard))
+
+    # reddemcee's hybrid estimator is not reproduced: thermodynamic integration
     get_evidence_hybrid = get_evidence_ti
-    get_evidence_ss = get_evidence_ti
 
     def get_func(self, name, kwargs=None):
         return getattr(self, name)(**(kwargs or {}))

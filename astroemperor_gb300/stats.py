@@ -6,6 +6,10 @@
 * ``thermodynamic_integration`` -- log-evidence by integrating the mean
   log-likelihood over the inverse-temperature ladder, which EMPEROR reads
   through ``sampler.get_evidence_ti`` (``emp.py:1432-1447``).
+* ``stepping_stone`` -- log-evidence by the stepping-stone estimator of
+  Xie, Lewis, Fan, Kuo & Chen (2011, Syst. Biol. 60, 150), read through
+  ``sampler.get_evidence_ss`` when EMPEROR's ``evidence_method`` is 'ss'
+  (``emp.py:1431-1441``).
 * ``model_stats`` -- chi2, AIC, BIC, HQIC, RMSE of a fit (``emp.py:1187-1210``).
 """
 from __future__ import annotations
@@ -95,6 +99,42 @@ def thermodynamic_integration(betas, log_like, pchip=True):
     else:
         err = np.inf
     return z, err
+
+
+def stepping_stone(betas, log_like):
+    """(logZ, error) by stepping stones between adjacent inverse temperatures.
+
+    With the ladder sorted 0 <= b_0 < ... < b_K = 1 and samples L_i of the
+    log-likelihood drawn at b_{k-1}, each stone is
+    r_k = mean_i exp((b_k - b_{k-1}) L_i), and log Z = sum_k log r_k (each
+    mean taken with a log-sum-exp shift).  A ladder that stops above zero is
+    closed by thermodynamic integration of the hottest chain's mean over
+    [0, b_0].  The error is the delta-method standard deviation of the
+    summed log r_k, treating the samples of each rung as independent.
+    """
+    betas = np.asarray(betas, dtype=np.float64)
+    ll = np.asarray(log_like, dtype=np.float64).reshape(len(betas), -1)
+    order = np.argsort(betas)
+    b, rows = betas[order], ll[order]
+    logz, var = 0.0, 0.0
+    hot = rows[0][np.isfinite(rows[0])]
+    if b[0] > 0:
+        if hot.size == 0:
+            return -np.inf, np.inf
+        logz += b[0] * float(np.mean(hot))
+    for k in range(1, len(b)):
+        x = rows[k - 1]
+        x = x[np.isfinite(x)]
+        if x.size == 0:
+            return -np.inf, np.inf
+        a = (b[k] - b[k - 1]) * x
+        m = float(np.max(a))
+        w = np.exp(a - m)
+        mw = float(np.mean(w))
+        logz += m + np.log(mw)
+        if x.size > 1:
+            var += float(np.var(w, ddof=1)) / (x.size * mw * mw)
+    return float(logz), float(np.sqrt(var))
 
 
 def model_stats(residuals, err2, ndim, like_max, flags=None, nins=1):
