@@ -505,5 +505,11 @@ class PTSampler:
     # reddemcee's hybrid estimator is not reproduced: thermodynamic integration
     get_evidence_hybrid = get_evidence_ti
 
+    def save(self, path, discard=0, thin=1):
+        """Write the run in the reference's post-run backend layout
+        (``backend_io.save_run``); returns the path written."""
+        from .backend_io import save_run
+        return save_run(self, path, discard=discard, thin=thin)
+
     def get_func(self, name, kwargs=None):
         return getattr(self, name)(**(kwargs or {}))

@@ -114,3 +114,17 @@ def test_posterior_51peg_recovers_reference_fit(peg_arr, lib, cuda):
     assert np.all(np.isfinite(ll))
     lp = s.get_log_prob(flat=True, discard=1500)[0]
     assert np.all(lp <= ll + 1e-9)            # logprior <= 0 for these priors
+
+
+def test_save_run_round_trip(peg_arr, lib, cuda, tmp_path):
+    from astroemperor_gb300.backend_io import load_run
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    T, W = 3, 16
+    s = PTSampler(W, m.ndim__, m, ntemps=T, betas=[1.0, 0.3, 0.05], seed=5)
+    s.run_mcmc(_p0(m, T, W, 2), nsweeps=12)
+    back = load_run(s.save(str(tmp_path / 'run.h5'), discard=2))
+    ch = s.get_chain(discard=2)
+    for t in range(T):
+        np.testing.assert_array_equal(back[f'mcmc_t{t}/chain'], ch[t])
+        np.testing.assert_array_equal(back[f'mcmc_t{t}/accepted'], s.accepted[t])
+    np.testing.assert_array_equal(back['mcmc/tsw_history'], s.get_tsw(discard=2))
