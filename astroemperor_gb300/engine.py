@@ -505,6 +505,32 @@ class PTSampler:
     # reddemcee's hybrid estimator is not reproduced: thermodynamic integration
     get_evidence_hybrid = get_evidence_ti
 
+    def run_adaptation_batches(self, p1, adaptation_batches, adaptation_nsweeps, nsweeps, nsteps=1,
+                               tol0=10, tau_diff_to_converge=0.1):
+        """The batched-adaptation driver of ``support/endit_freeze.scr``: run
+        ``adaptation_nsweeps`` with the ladder adapting, up to
+        ``adaptation_batches`` times, until the cold chain's integrated
+        autocorrelation times are below 1/``tol0`` of the iterations and
+        changed by less than ``tau_diff_to_converge`` since the last batch;
+        then freeze the ladder (``config_adaptation_halflife = 0``) and run
+        ``nsweeps`` more.  Returns (state, converged_during_adaptation, tau)."""
+        state = p1
+        old_tau = np.inf
+        converged = False
+        tau0 = None
+        for _ in range(int(adaptation_batches)):
+            state = self.run_mcmc(state, nsweeps=adaptation_nsweeps, nsteps=nsteps)
+            tau0 = self.get_autocorr_time(quiet=True, tol=0)[0]
+            niter = self.iteration
+            converged = bool(np.all(tau0 * tol0 < niter))
+            converged &= bool(np.all(np.abs(old_tau - tau0) / tau0 < tau_diff_to_converge))
+            old_tau = tau0
+            if converged:
+                break
+        self.config_adaptation_halflife = 0
+        state = self.run_mcmc(state, nsweeps=nsweeps, nsteps=nsteps)
+        return state, converged, tau0
+
     def save(self, path, discard=0, thin=1):
         """Write the run in the reference's post-run backend layout
         (``backend_io.save_run``); returns the path written."""

@@ -101,7 +101,11 @@ class Simulation:
                               'progress': True, 'precision': 'mixed', 'seed': None,
                               'use_graph': True}
         self.run_config = {'burnin': None, 'adaptation_batches': None, 'adaptation_nsweeps': None,
-                           'thin': 1, 'discard': 0.5, 'logger_level': 'CRITICAL'}
+                           'thin': 1, 'discard': 0.5, 'logger_level': 'CRITICAL',
+                           # 'freeze1' (the reference's choice, emp.py:692-704) or 'batches'
+                           # (support/endit_freeze.scr)
+                           'adaptation_driver': 'freeze1'}
+        self.evidence_method = 'hybrid'                    # emp.py:127-129
 
     # ---------------------------------------------------------------- blocks
     def add_keplerian(self):
@@ -230,7 +234,11 @@ class Simulation:
         self.reddemcee_discard = self._discard()
         self.reddemcee_thin = int(self.run_config['thin'])
         ab, an = self.run_config['adaptation_batches'], self.run_config['adaptation_nsweeps']
-        if ab and an:
+        if ab and an and self.run_config.get('adaptation_driver') == 'batches':
+            # endit_freeze.scr: adaptation batches until the autocorrelation
+            # times settle, freeze, production
+            self.sampler.run_adaptation_batches(p1, ab, an, nsweeps, nsteps=nsteps)
+        elif ab and an:
             # endit_freeze1.scr: adaptation burn-in, freeze, production
             n1 = self.reddemcee_discard
             state = self.sampler.run_mcmc(p1, nsweeps=n1, nsteps=nsteps)
@@ -253,10 +261,18 @@ class Simulation:
         self.fit_median = np.median(self.chain[0], axis=0)
         self.post_max = float(self.posts[0][self.best_loc_post])
         self.like_max = float(self.likes[0][self.best_loc_like])
+        # emp.py:1431-1446: the configured estimator, then TI, then TI without
+        # the PCHIP interpolation
+        method = getattr(self, 'evidence_method', 'hybrid')
         try:
-            self.evidence = self.sampler.get_evidence_ti(discard=self.reddemcee_discard)
+            z = getattr(self.sampler, f'get_evidence_{method}')(discard=self.reddemcee_discard)[:2]
+            if z[0] == -np.inf:
+                z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard)[:2]
+            if z[0] == -np.inf:
+                z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard, pchip=False)[:2]
         except Exception:
-            self.evidence = (-np.inf, np.inf)
+            z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard, pchip=False)[:2]
+        self.evidence = (z[0], z[1])
         resid, err2 = self.residuals(self.fit_max)
         st = model_stats(resid, err2, self.model.ndim__, self.like_max,
                          flags=self.my_data.Flag, nins=self.nins__)

@@ -128,3 +128,20 @@ def test_save_run_round_trip(peg_arr, lib, cuda, tmp_path):
         np.testing.assert_array_equal(back[f'mcmc_t{t}/chain'], ch[t])
         np.testing.assert_array_equal(back[f'mcmc_t{t}/accepted'], s.accepted[t])
     np.testing.assert_array_equal(back['mcmc/tsw_history'], s.get_tsw(discard=2))
+
+
+def test_adaptation_batches_driver_freezes_the_ladder(peg_arr, lib, cuda):
+    """support/endit_freeze.scr: adapt in batches, then freeze and sample."""
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    T, W = 4, 32
+    s = PTSampler(W, m.ndim__, m, ntemps=T, betas=[1.0, 0.4, 0.1, 0.01], seed=9, adapt_tau=10)
+    state, conv, tau = s.run_adaptation_batches(_p0(m, T, W, 3), adaptation_batches=3,
+                                                adaptation_nsweeps=40, nsweeps=30)
+    assert s.config_adaptation_halflife == 0
+    bh = s.get_betas()
+    n = s.iteration
+    assert n in (40 + 30, 80 + 30, 120 + 30)
+    # adapting before the freeze, constant after it
+    assert np.any(bh[n - 31] != bh[0])
+    np.testing.assert_array_equal(bh[n - 30:], np.repeat(bh[n - 30:n - 29], 30, axis=0))
+    assert np.isfinite(s.get_evidence_ss()[0]) and np.isfinite(s.get_evidence_ti()[0])
