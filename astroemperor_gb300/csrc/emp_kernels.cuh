@@ -437,6 +437,34 @@ __device__ __forceinline__ void kepler_f32_n(const float (&M)[NE], const float (
 // would be; only the special-function and rounding-to-integer steps stay
 // per element.
 // ----------------------------------------------------------------------------
+// special-function unit approximations (PTX .approx.ftz forms); used where
+// the result only steers an iteration or is refined afterwards
+__device__ __forceinline__ float rcp_fast(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_fast(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2_fast(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float ex2_fast(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+// 1/x to about 1 ulp: the approximation and one Newton step
+__device__ __forceinline__ float rcp_nr(float x) {
+    const float r = rcp_fast(x);
+    return __fmaf_rn(__fmaf_rn(-x, r, 1.f), r, r);
+}
+
 __device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
@@ -444,10 +472,12 @@ __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a
 // a - b with one rounding (the product b * -1 is exact)
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.f), a); }
 __device__ __forceinline__ float2 rint2(float2 a) { return make_float2(rintf(a.x), rintf(a.y)); }
-__device__ __forceinline__ float2 rcp_approx2(float2 a) {
-    return make_float2(__fdividef(1.f, a.x), __fdividef(1.f, a.y));
+__device__ __forceinline__ float2 rcp_approx2(float2 a) { return make_float2(rcp_fast(a.x), rcp_fast(a.y)); }
+// 1/a to about 1 ulp per element
+__device__ __forceinline__ float2 rcp_nr2(float2 a) {
+    const float2 r = rcp_approx2(a);
+    return __ffma2_rn(__ffma2_rn(make_float2(-a.x, -a.y), r, make_float2(1.f, 1.f)), r, r);
 }
-__device__ __forceinline__ float2 rcp_rn2(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 
 // mean_anomaly_mixed on a pair of epochs
 __device__ __forceinline__ float2 mean_anomaly_pair(const float* pc, float2 th, float2 tl, float2& mlo) {
@@ -513,11 +543,11 @@ __device__ __forceinline__ void kepler_pairs(const float2 (&M)[NP], const float2
         const float2 b = mul2(M[k], bc2(kc[2]));
         const float2 x = fma2(b, b, bc2(kc[1]));                   // > 0: a > 0 for e < 1
         float2 t, z;
-        t.x = b.x + copysignf(x.x * rsqrtf(x.x), b.x);
-        t.y = b.y + copysignf(x.y * rsqrtf(x.y), b.y);
-        z.x = copysignf(exp2f(__log2f(fabsf(t.x)) * (1.f / 3.f)), t.x);
-        z.y = copysignf(exp2f(__log2f(fabsf(t.y)) * (1.f / 3.f)), t.y);
-        float2 sm = sub2(z, make_float2(__fdividef(ka, z.x), __fdividef(ka, z.y)));
+        t.x = b.x + copysignf(x.x * rsqrt_fast(x.x), b.x);
+        t.y = b.y + copysignf(x.y * rsqrt_fast(x.y), b.y);
+        z.x = copysignf(ex2_fast(lg2_fast(fabsf(t.x)) * (1.f / 3.f)), t.x);
+        z.y = copysignf(ex2_fast(lg2_fast(fabsf(t.y)) * (1.f / 3.f)), t.y);
+        float2 sm = sub2(z, mul2(bc2(ka), rcp_approx2(z)));
         float2 s2 = mul2(sm, sm);
         sm = fma2(mul2(mul2(bc2(-kc[3]), s2), s2), sm, sm);
         s2 = mul2(sm, sm);
@@ -987,7 +1017,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                             // (A (cos E - e) - B sin E) / (1 - e cos E) + C with
                             // float-float A, B, C, e
                             const float2 cme = sub2(sub2(cs[j], bc2(ec)), bc2(el));
-                            const float2 inv = rcp_rn2(fma2(bc2(-el), cs[j], fma2(bc2(-ec), cs[j], bc2(1.f))));
+                            const float2 inv = rcp_nr2(fma2(bc2(-el), cs[j], fma2(bc2(-ec), cs[j], bc2(1.f))));
                             const float2 hi = fma2(fma2(bc2(pc[5]), cme, mul2(bc2(-pc[6]), sn[j])), inv, bc2(pc[7]));
                             const float2 lo = fma2(fma2(bc2(pc[9]), cme, mul2(bc2(-pc[10]), sn[j])), inv, bc2(pc[11]));
                             mod2[j] = add2(mod2[j], add2(hi, lo));
@@ -1021,7 +1051,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                                           __fsub_rn((float)s_ylo[ps], (float)ic[2]));
                     R w, lt;
                     if (PREC == EMP_PREC_FP64) { w = R(1) / err2; lt = (R)log((double)err2); }
-                    else { w = (R)__frcp_rn((float)err2); lt = (R)(__log2f((float)err2) * 0.69314718055994531f); }
+                    else { w = (R)rcp_nr((float)err2); lt = (R)(lg2_fast((float)err2) * 0.69314718055994531f); }
                     if (Q == 0) {
                         ks.add(b * b * w + lt);
                     } else {
@@ -1034,7 +1064,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                             const R dtc = s_dt[c * tile + ps];
                             R a;
                             if (PREC == EMP_PREC_FP64) a = ic[3 + 2 * c] * (R)exp((double)(dtc * ic[4 + 2 * c]));
-                            else a = ic[3 + 2 * c] * (R)exp2f((float)(dtc * ic[4 + 2 * c]));
+                            else a = ic[3 + 2 * c] * (R)ex2_fast((float)(dtc * ic[4 + 2 * c]));
                             x -= a * xh[c];
 #pragma unroll
                             for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
