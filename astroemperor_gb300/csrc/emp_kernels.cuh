@@ -566,7 +566,7 @@ __device__ __forceinline__ void kepler_pairs(const float2 (&M)[NP], const float2
         const float2 d = mul2(mul2(f, f1), rcp_approx2(den));
         const float2 d2 = mul2(d, d);
         const float2 cd = fma2(bc2(-0.5f), d2, one);
-        const float2 sd = mul2(d, fma2(d2, bc2(-1.f / 6.f), one));
+        const float2 sd = d;      // |d| <= 4e-3: the d^3/6 term is below 1.1e-8
         s[k] = fma2(mul2(ca, sd), bc2(-1.f), mul2(sa, cd));
         c[k] = fma2(sa, sd, mul2(ca, cd));
     }
@@ -1038,20 +1038,51 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                         }
                     }
                 }
+                // mixed: the per-epoch quantities that do not depend on the MA
+                // state (residual, 1/err2, log err2, MA coefficients) two epochs
+                // per instruction; the recurrence below stays sequential
+                R bb[NE], ww[NE], lw[NE], aa[NE][NQ];
+                if constexpr (PREC == EMP_PREC_MIXED) {
+#pragma unroll
+                    for (int j = 0; j < NE / 2; ++j) {
+                        const int p0 = pos[2 * j], p1 = pos[2 * j + 1];
+                        const float* i0 = (const float*)(insc + s_in[p0] * INSW);
+                        const float* i1 = (const float*)(insc + s_in[p1] * INSW);
+                        const float2 m2 = make_float2((float)model[2 * j], (float)model[2 * j + 1]);
+                        const float2 b2 = add2(sub2(sub2(make_float2(s_y[p0], s_y[p1]), make_float2(i0[0], i1[0])), m2),
+                                               sub2(make_float2(s_ylo[p0], s_ylo[p1]), make_float2(i0[2], i1[2])));
+                        const float2 e2 = add2(make_float2(s_s2[p0], s_s2[p1]), make_float2(i0[1], i1[1]));
+                        const float2 w2 = rcp_nr2(e2);
+                        const float2 l2 = mul2(make_float2(lg2_fast(e2.x), lg2_fast(e2.y)),
+                                               bc2(0.69314718055994531f));
+                        bb[2 * j] = b2.x; bb[2 * j + 1] = b2.y;
+                        ww[2 * j] = w2.x; ww[2 * j + 1] = w2.y;
+                        lw[2 * j] = l2.x; lw[2 * j + 1] = l2.y;
+#pragma unroll
+                        for (int c = 0; c < Q; ++c) {
+                            const float2 x2 = mul2(make_float2(s_dt[c * tile + p0], s_dt[c * tile + p1]),
+                                                   make_float2(i0[4 + 2 * c], i1[4 + 2 * c]));
+                            const float2 a2 = mul2(make_float2(i0[3 + 2 * c], i1[3 + 2 * c]),
+                                                   make_float2(ex2_fast(x2.x), ex2_fast(x2.y)));
+                            aa[2 * j][c] = a2.x; aa[2 * j + 1][c] = a2.y;
+                        }
+                    }
+                }
 #pragma unroll
                 for (int e = 0; e < NE; ++e) {
                     if (!ok[e]) continue;
                     const int ps = pos[e];
-                    const int ki = s_in[ps];
-                    const R* ic = insc + ki * INSW;
-                    const R err2 = s_s2[ps] + ic[1];
-                    R b;
-                    if (PREC == EMP_PREC_FP64) b = s_y[ps] - (model[e] + ic[0]);
-                    else b = (R)__fadd_rn(__fsub_rn(__fsub_rn((float)s_y[ps], (float)ic[0]), (float)model[e]),
-                                          __fsub_rn((float)s_ylo[ps], (float)ic[2]));
-                    R w, lt;
-                    if (PREC == EMP_PREC_FP64) { w = R(1) / err2; lt = (R)log((double)err2); }
-                    else { w = (R)rcp_nr((float)err2); lt = (R)(lg2_fast((float)err2) * 0.69314718055994531f); }
+                    R b, w, lt;
+                    const R* ic = insc;
+                    if constexpr (PREC == EMP_PREC_FP64) {
+                        ic = insc + s_in[ps] * INSW;
+                        const R err2 = s_s2[ps] + ic[1];
+                        b = s_y[ps] - (model[e] + ic[0]);
+                        w = R(1) / err2;
+                        lt = (R)log((double)err2);
+                    } else {
+                        b = bb[e]; w = ww[e]; lt = lw[e];
+                    }
                     if (Q == 0) {
                         ks.add(b * b * w + lt);
                     } else {
@@ -1061,10 +1092,11 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                         for (int q2 = 0; q2 < NQ; ++q2) gn[q2] = R(0);
 #pragma unroll
                         for (int c = 0; c < Q; ++c) {
-                            const R dtc = s_dt[c * tile + ps];
                             R a;
-                            if (PREC == EMP_PREC_FP64) a = ic[3 + 2 * c] * (R)exp((double)(dtc * ic[4 + 2 * c]));
-                            else a = ic[3 + 2 * c] * (R)ex2_fast((float)(dtc * ic[4 + 2 * c]));
+                            if constexpr (PREC == EMP_PREC_FP64)
+                                a = ic[3 + 2 * c] * (R)exp((double)(s_dt[c * tile + ps] * ic[4 + 2 * c]));
+                            else
+                                a = aa[e][c];
                             x -= a * xh[c];
 #pragma unroll
                             for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
