@@ -127,6 +127,7 @@ struct KArgs {
     int step_in_sweep;
     uint64_t seed;
     double a;
+    double a_inv_exact;        // 1/a when a is a power of two (then zz^2/a == zz^2 * (1/a)), else 0
     // systems (one for a plain handle; many for a batch handle)
     int T;                     // temperatures per system (PT modes)
     int n_sys;                 // systems processed by this launch

@@ -808,7 +808,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                 const int slot_k = A.members[pbase + t_idx * A.W + k_idx];
                 // emcee StretchMove.get_proposal: zz = ((a-1) u + 1)^2 / a
                 const double zz = __dadd_rn(__dmul_rn(A.a - 1.0, u53(rr.x, rr.y)), 1.0);
-                z = __dmul_rn(zz, zz) / A.a;
+                z = A.a_inv_exact != 0.0 ? __dmul_rn(__dmul_rn(zz, zz), A.a_inv_exact)
+                                         : __dmul_rn(zz, zz) / A.a;
                 if (r == 0) misc[2] = z;
                 const double* sj = A.st_theta + (size_t)slot_j * ds;
                 const double* ck = A.st_theta + (size_t)slot_k * ds;

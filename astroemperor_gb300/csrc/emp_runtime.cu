@@ -371,6 +371,10 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
             a.step_in_sweep = step;
             a.seed = st->seed;
             a.a = st->a;
+            {
+                int ex = 0;
+                a.a_inv_exact = frexp(st->a, &ex) == 0.5 ? 1.0 / st->a : 0.0;   // a = 2^(ex-1)
+            }
             if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr))) return rc;
             ++kcount;
         }
