@@ -287,13 +287,9 @@ def main_ragged(args):
     clk = clocks.stop()
     fp64_steps = args.fp64_steps or max(5, steps // 20)
     ms_fp64, _, bt64 = timed('fp64', fp64_steps, 3)
-    t_mixed = ms_mixed / 1e3
-    if world > 1:
-        tt = torch.tensor([t_mixed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_mixed = float(tt.item())
+    from astroemperor_gb300.replicas import job_rate
     units_per_sweep = T * W * nsteps * int(n_ep.sum())
-    value = units_per_sweep * steps * world / t_mixed
+    _, t_mixed, value = job_rate(units_per_sweep * steps, ms_mixed / 1e3, device=dev)
     fp64_value = units_per_sweep * fp64_steps / (ms_fp64 / 1e3)
 
     # roofline: the stretch half-step shape (T*W/2 walkers of every system),
@@ -489,13 +485,10 @@ def main():
     fp64_steps = args.fp64_steps or max(20, args.steps // 20)
     ms_fp64, _, _ = timed_sweeps('fp64', fp64_steps, 3)
 
-    t_mixed = ms_mixed / 1e3
-    if world > 1:
-        tt = torch.tensor([t_mixed], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_mixed = float(tt.item())
+    from astroemperor_gb300.replicas import job_rate
     units_per_sweep = T * W * nsteps * n
-    value = units_per_sweep * args.steps * world / t_mixed
+    # replicas: summed work over the slowest rank's time
+    _, t_mixed, value = job_rate(units_per_sweep * args.steps, ms_mixed / 1e3, device=dev)
     sweeps_s = args.steps * world / t_mixed
     fp64_value = units_per_sweep * fp64_steps / (ms_fp64 / 1e3)
 
