@@ -43,6 +43,11 @@ WORKLOADS = {
 }
 SEED = 1234
 
+# DRAM bytes (read + write) of one stretch half-step launch, from the ncu
+# captures summarised in profiles/ (k_logpost_mixed_c2_halfstep.md,
+# k_logpost_mixed_c3_ragged_stretch.md); None where no capture was taken
+NCU_TRAFFIC = {'c2': 610816, 'c3': 582504448}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -308,7 +313,9 @@ def main_ragged(args):
     achieved = flops_launch / (k_ms * 1e-3) / 1e12
     peak32 = f32.value / 1e12
     roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s',
-            'frac': achieved / peak32, 'traffic': None,
+            'frac': achieved / peak32, 'traffic': NCU_TRAFFIC.get('c3'),
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch',
+            'algorithmic_bytes': int(n_ep.sum()) * 25 + ctx.S * (T * W // 2) * (8 * ctx.ndim + 16),
             'kernel': 'k_logpost<MIXED,Q=0> over all systems (stretch half-step shape)',
             'kernel_ms': k_ms, 'flop_per_eval_epoch': '58*planets + 10 per system',
             'launch': {'lanes': bt.launch[0], 'tile': bt.launch[1]},
@@ -511,7 +518,9 @@ def main():
     achieved = flops_launch / (k_ms * 1e-3) / 1e12
     peak32 = f32.value / 1e12
     roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s',
-            'frac': achieved / peak32, 'traffic': None,
+            'frac': achieved / peak32, 'traffic': NCU_TRAFFIC.get(args.config),
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch',
+            'algorithmic_bytes': n * 25 + (T * W // 2) * (8 * D + 16),
             'kernel': 'k_logpost<MIXED,Q=1> (stretch half-step shape)',
             'kernel_ms': k_ms, 'flop_per_eval_epoch': F,
             'launch': {'lanes': s_mixed.launch[0], 'tile': s_mixed.launch[1]} if s_mixed.launch else None,
