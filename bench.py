@@ -46,7 +46,7 @@ SEED = 1234
 # DRAM bytes (read + write) of one stretch half-step launch, from the ncu
 # captures summarised in profiles/ (k_logpost_mixed_c2_halfstep.md,
 # k_logpost_mixed_c3_ragged_stretch.md); None where no capture was taken
-NCU_TRAFFIC = {'c2': 610816, 'c3': 582504448}
+NCU_TRAFFIC = {'c2': 607488, 'c3': 581037824}
 
 
 def parse():
