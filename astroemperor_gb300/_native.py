@@ -12,11 +12,18 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, '_lib', 'libemp_gpu.so')
 
-EMP_ABI_VERSION = 1
+EMP_ABI_VERSION = 2
 EMP_MAX_PARAMS = 160
 EMP_MAX_PLANETS = 16
 EMP_MAX_INS = 16
 EMP_MAX_MA = 3
+EMP_MAX_GP_TERMS = 8
+
+EMP_GP_REAL = 1
+EMP_GP_MATERN32 = 2
+EMP_GP_ROTATION = 3
+EMP_GP_GROT = 4
+EMP_GP_SHO = 16
 
 EMP_OK = 0
 EMP_E_INVALID = -1
@@ -60,6 +67,9 @@ class EmpModelDesc(C.Structure):
         ('prior_const', C.c_double),
         ('n_prior_var', C.c_int32), ('_pad1', C.c_int32),
         ('prior_var', C.c_int32 * (EMP_MAX_PARAMS + 2 * EMP_MAX_PLANETS)),
+        ('gp_nterms', C.c_int32), ('_pad2', C.c_int32),
+        ('gp_kind', C.c_int32 * EMP_MAX_GP_TERMS),
+        ('gp_slot', (C.c_int32 * 5) * EMP_MAX_GP_TERMS),
     ]
 
 

@@ -102,6 +102,16 @@ struct DevData {
 
 enum Mode : int { kModeLogpost = 0, kModeStretch = 1, kModeSlots = 2 };
 
+// what the stretch kernel hands to the GP kernel per proposal
+struct GPMeta {
+    double lp;                 // log-prior of the proposal (-inf: outside the support)
+    double z;                  // stretch factor
+    uint32_t uword;            // Metropolis random word
+    int slot;                  // physical slot of the walker
+    int pos;                   // logical position t * W + j within its system
+    int t;                     // temperature index
+};
+
 struct KArgs {
     const emp_model_desc* md;
     DevData d;
@@ -138,7 +148,15 @@ struct KArgs {
     int* work_counter;         // persistent scheduling counter, null = one item per CTA
     int dstride;               // theta row stride (largest free dimension)
     int lay_full, lay_free, lay_planets, lay_ins, lay_acc;   // layout maxima
+    // GP likelihood (md->gp_nterms > 0): the kernel writes the residuals and
+    // err2 of every walker row, epoch-major ([n][nwalk]), and in stretch mode
+    // the proposal; k_gp then forms the log-likelihood (and the Metropolis test)
+    double* gp_r;
+    double* gp_e;
+    double* gp_prop;           // [nwalk][dstride] proposals (stretch)
+    GPMeta* gp_meta;           // [nwalk] (stretch)
 };
+
 
 // ----------------------------------------------------------------------------
 // shared memory layout (bytes), computed identically on host and device

@@ -894,6 +894,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     __syncthreads();
     const double lp = active ? misc[0] : -INFINITY;
     const bool valid = active && (lp > -INFINITY);
+    // GP likelihood: this kernel writes the residuals, k_gp does the rest
+    const bool gp_on = A.gp_r != nullptr;
 
     // ---------------- likelihood over epoch tiles ------------------------
     const int n = A.sys_off != nullptr ? (int)(A.sys_off[sys + 1] - e0) : A.d.n;
@@ -1084,6 +1086,13 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     } else {
                         b = bb[e]; w = ww[e]; lt = lw[e];
                     }
+                    if (gp_on) {
+                        // GP likelihood: hand the residual and err2 to k_gp
+                        const size_t gi = (size_t)(base + r * C + k0 + e) * A.nwalk + wk;
+                        A.gp_r[gi] = (double)b;
+                        A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
+                        continue;
+                    }
                     if (Q == 0) {
                         ks.add(b * b * w + lt);
                     } else {
@@ -1197,7 +1206,23 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     const double logl = (valid && r == 0) ? (-0.5 * v + md->loglike_const) : -INFINITY;
 
     // ---------------- epilogue --------------------------------------------
-    if (A.mode == kModeLogpost) {
+    if (gp_on) {
+        // the prior (and in stretch mode the proposal) for k_gp
+        if (active && r == 0) {
+            if (A.mode == kModeLogpost) A.logprior[slot_j] = lp;
+            else if (A.mode == kModeSlots) A.st_logprior[slot_j] = lp;
+            else {
+                GPMeta m;
+                m.lp = lp; m.z = z; m.uword = uword; m.slot = slot_j;
+                m.pos = t_idx * A.W + j_idx; m.t = t_idx;
+                A.gp_meta[wk] = m;
+            }
+        }
+        if (active && A.mode == kModeStretch) {
+            double* dst = A.gp_prop + (size_t)wk * ds;
+            for (int d = r; d < n_free; d += L) dst[d] = thp[d];
+        }
+    } else if (A.mode == kModeLogpost) {
         if (active && r == 0) {
             A.logl[slot_j] = logl;
             A.logprior[slot_j] = lp;

@@ -19,6 +19,7 @@
 #include "emp_pt.cuh"
 #include "emp_model_eval.cuh"
 #include "emp_grad.cuh"
+#include "emp_gp.cuh"
 
 namespace emp {
 using KFn = void (*)(KArgs);
@@ -26,6 +27,7 @@ KFn get_kernel_fp64(int q, int lidx);
 KFn get_kernel_mixed(int q, int lidx);
 using GFn = void (*)(GArgs);
 GFn get_kernel_grad(int q, int lidx);
+KFn get_kernel_gp(int M);
 }  // namespace emp
 
 using namespace emp;
@@ -101,6 +103,15 @@ struct emp_handle {
     bool attr_done[2][4][6] = {};
     bool swap_attr = false;
     bool swap_attr_batch = false;
+    // celerite GP likelihood: state dimension of k_gp (0: Gaussian likelihood)
+    // and its row buffers (residuals and err2 [n][rows], proposals, meta)
+    int gp_M = 0;
+    int64_t gp_rows = 0;
+    void* gp_buf = nullptr;
+    double* gp_r = nullptr;
+    double* gp_e = nullptr;
+    double* gp_prop = nullptr;
+    GPMeta* gp_meta = nullptr;
 };
 
 // dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
@@ -170,6 +181,29 @@ int validate_model(const emp_model_desc* m) {
         if ((rc = chk(m->ma_slot, cnt, "MA"))) return rc;
     }
     if (m->acc_order > 0 && m->acc_slot < 0) return fail(EMP_E_INVALID, "acceleration without slot");
+    if (m->gp_nterms < 0 || m->gp_nterms > EMP_MAX_GP_TERMS)
+        return fail(EMP_E_SIZE, "gp_nterms=%d outside [0, %d]", m->gp_nterms, EMP_MAX_GP_TERMS);
+    if (m->gp_nterms > 0) {
+        if (m->ma_order > 0) return fail(EMP_E_UNSUPPORTED, "a GP likelihood with an MA model");
+        int dims = 0;
+        for (int j = 0; j < m->gp_nterms; ++j) {
+            const int kind = m->gp_kind[j];
+            const int nd = gp_term_dims(kind);
+            if (nd < 0) return fail(EMP_E_UNSUPPORTED, "GP term %d: kind %d unknown", j, kind);
+            dims += nd;
+            const int np = kind == EMP_GP_REAL || kind == EMP_GP_MATERN32 ? 2
+                         : kind == EMP_GP_ROTATION ? 5 : kind == EMP_GP_GROT ? 4 : 3;
+            for (int i = 0; i < 5; ++i) {
+                const int sl = m->gp_slot[j][i];
+                if (i < np && (sl < 0 || sl >= m->n_full))
+                    return fail(EMP_E_INVALID, "GP term %d parameter %d: slot %d out of range", j, i, sl);
+                if (i >= np && sl != -1)
+                    return fail(EMP_E_INVALID, "GP term %d: slot %d of an unused parameter must be -1", j, i);
+            }
+        }
+        if (dims > 16)
+            return fail(EMP_E_UNSUPPORTED, "GP terms of %d state dimensions (at most 16)", dims);
+    }
     std::vector<int> seen(m->n_free, 0);
     for (int s = 0; s < m->n_full; ++s) {
         int src = m->full_src[s];
@@ -296,6 +330,17 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     a.sys_t0 = h->sys_t0;
     a.sys_order = h->sys_order;
     if (a.nwalk <= 0) return EMP_OK;
+    KFn gfn = nullptr;
+    if (h->gp_M > 0) {
+        if (a.nwalk > h->gp_rows)
+            return fail(EMP_E_INVALID, "GP workspace holds %lld rows, launch has %d", (long long)h->gp_rows, a.nwalk);
+        gfn = get_kernel_gp(h->gp_M);
+        if (!gfn) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", h->gp_M);
+        a.gp_r = h->gp_r;
+        a.gp_e = h->gp_e;
+        a.gp_prop = h->gp_prop;
+        a.gp_meta = h->gp_meta;
+    }
     a.cps = (a.nwalk + G - 1) / G;
     const int64_t items = (int64_t)a.cps * h->n_sys;
     if (items > 0x7fffffff) return fail(EMP_E_SIZE, "%lld CTA items exceed 2^31-1", (long long)items);
@@ -309,6 +354,44 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     fn<<<grid, NT, lay.total, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
+    if (gfn) {
+        // one thread (one warp per 32 rows) per row: the rows spread over the SMs
+        gfn<<<(a.nwalk + 31) / 32, 32, 0, s>>>(a);
+        g_launches.fetch_add(1);
+        CUDA_TRY(cudaGetLastError());
+    }
+    return EMP_OK;
+}
+
+// GP row buffers for launches of up to `rows` walker rows; allocated (or
+// grown) outside any stream capture, before the launches that use them.  A
+// captured sweep graph refers to the old buffers, so growing drops it.
+int gp_reserve(emp_handle* h, int64_t rows) {
+    if (h->gp_M == 0 || rows <= h->gp_rows) return EMP_OK;
+    const size_t n = (size_t)h->n, D = (size_t)std::max(h->lay[1], 1);
+    const size_t al = 256;
+    auto up = [al](size_t b) { return (b + al - 1) & ~(al - 1); };
+    const size_t b_re = up(8 * n * (size_t)rows);
+    const size_t b_prop = up(8 * D * (size_t)rows);
+    const size_t b_meta = up(sizeof(GPMeta) * (size_t)rows);
+    const size_t total = 2 * b_re + b_prop + b_meta;
+    if (total > ((size_t)64 << 30))
+        return fail(EMP_E_SIZE, "GP workspace of %zu B for %lld rows exceeds 64 GiB", total, (long long)rows);
+    h->gc.reset();
+    if (h->gp_buf) {
+        cudaFree(h->gp_buf);
+        h->gp_buf = nullptr;
+        h->gp_rows = 0;
+    }
+    void* b = nullptr;
+    CUDA_TRY(cudaMalloc(&b, total));
+    unsigned char* c = (unsigned char*)b;
+    h->gp_buf = b;
+    h->gp_r = (double*)c;
+    h->gp_e = (double*)(c + b_re);
+    h->gp_prop = (double*)(c + 2 * b_re);
+    h->gp_meta = (GPMeta*)(c + 2 * b_re + b_prop);
+    h->gp_rows = rows;
     return EMP_OK;
 }
 
@@ -376,7 +459,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                 a.a_inv_exact = frexp(st->a, &ex) == 0.5 ? 1.0 / st->a : 0.0;   // a = 2^(ex-1)
             }
             if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr))) return rc;
-            ++kcount;
+            kcount += h->gp_M > 0 ? 2 : 1;
         }
     }
     SwapArgs S{};
@@ -600,6 +683,8 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
             return fail(EMP_E_UNSUPPORTED, "system %d: MA order %d differs from system 0's %d", s,
                         ma_order_on_device(m), q);
         if ((rc = check_system(m, data, s, &nsys[s]))) return rc;
+        if (S > 1 && m->gp_nterms > 0)
+            return fail(EMP_E_UNSUPPORTED, "system %d: GP likelihoods take a one-system handle", s);
         total += nsys[s];
         lay[0] = std::max(lay[0], m->n_full);
         lay[1] = std::max(lay[1], m->n_free);
@@ -646,6 +731,12 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
     h->n_sys = S;
     for (int k = 0; k < 5; ++k) h->lay[k] = lay[k];
     h->q = q;
+    if (models[0].gp_nterms > 0) {
+        int dims = 0;
+        for (int j = 0; j < models[0].gp_nterms; ++j) dims += gp_term_dims(models[0].gp_kind[j]);
+        h->gp_M = 2;
+        while (h->gp_M < dims) h->gp_M <<= 1;
+    }
 
     // one device allocation for the dataset, descriptors and system tables
     size_t bytes = 0;
@@ -734,6 +825,7 @@ int emp_destroy(emp_handle* h) {
     h->gc.reset();
     if (h->own) cudaStreamDestroy(h->own);
     if (h->dbuf) cudaFree(h->dbuf);
+    if (h->gp_buf) cudaFree(h->gp_buf);
     delete h;
     return EMP_OK;
 }
@@ -782,6 +874,8 @@ int emp_logpost(emp_handle* h, const double* theta, int B, const int32_t* system
     a.logl = logl;
     a.logprior = logprior;
     a.logp = logp;
+    int rc = gp_reserve(h, B);
+    if (rc) return rc;
     return launch_eval(h, precision, a, (cudaStream_t)stream);
 }
 
@@ -816,6 +910,7 @@ int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, do
     if (!theta || !logl || !logprior || !grad_logl || !grad_logprior)
         return fail(EMP_E_INVALID, "a NULL argument");
     if (h->n_sys > 1) return fail(EMP_E_UNSUPPORTED, "the gradient takes a one-system handle");
+    if (h->gp_M > 0) return fail(EMP_E_UNSUPPORTED, "gradient: GP likelihoods are not built");
     const emp_model_desc& m = h->md;
     for (int p = 0; p < m.n_planets; ++p)
         if (m.kep_param[p] != 0 && m.kep_param[p] != 1)
@@ -879,6 +974,7 @@ int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream) {
     a.st_theta = st->theta;
     a.st_logl = st->logl;
     a.st_logprior = st->logprior;
+    if ((rc = gp_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
     return launch_eval(h, st->precision, a, (cudaStream_t)stream);
 }
 
@@ -886,6 +982,7 @@ int emp_pt_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec
     if (!h) return fail(EMP_E_INVALID, "handle is NULL");
     int rc = check_state(h, st);
     if (rc) return rc;
+    if ((rc = gp_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
     return enqueue_sweep(h, st, rec, (cudaStream_t)stream, nullptr);
 }
 
@@ -950,6 +1047,9 @@ extern "C" int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st, const 
     local.work = ws;
     local.work_bytes = (int64_t)kStaticWorkBytes;
     if ((rc = check_state(h, &local))) return rc;
+    if (h->gp_M > 0 && h->gp_rows < walkers)
+        return fail(EMP_E_UNSUPPORTED, "a GP model needs its row workspace (emp_pt_evaluate or emp_pt_sweep "
+                    "allocates it) before the allocation-free sweep");
     cudaStream_t s = (cudaStream_t)stream;
     CUDA_TRY(cudaMemsetAsync(ws, 0, kStaticHeaderBytes, s));
     return enqueue_sweep(h, &local, rec, s, nullptr);
@@ -964,6 +1064,7 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, 
     if (rc) return rc;
     if (nsweeps < 0) return fail(EMP_E_INVALID, "nsweeps=%d < 0", nsweeps);
     if (nsweeps == 0) return EMP_OK;
+    if ((rc = gp_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (!use_graph) {
         for (int i = 0; i < nsweeps; ++i)

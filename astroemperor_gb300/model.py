@@ -204,6 +204,42 @@ def MagneticCycleBlock(number: int) -> Parameter_Block:
                            number_=number)
 
 
+# GP term names of param_repo.py:204-345 by (term, celerite2 keyword)
+_GP_NAMES = {'RealTerm': 'Real Term', 'Matern32Term': 'Matern32 Term', 'RotationTerm': 'Rotation Term',
+             'SHOTerm': 'SHO Term', 'GonzRotationTerm': 'GRot Term'}
+GP_TERMS = tuple(_GP_NAMES)
+
+
+def CeleriteBlock(my_kernel: dict) -> Parameter_Block:
+    """block_repo.py:350-413: the GP hyperparameters of a celerite2 kernel.
+
+    ``my_kernel = {'terms': ['SHOTerm', ...], 'params': [{'rho': None, 'tau': None,
+    'S0': 2.0}, ...]}``: a None value is a free parameter, a number fixes it.
+    Parameters follow each term's dictionary order, which is the order in which
+    the reference's generated ``my_model`` reads ``theta_gp`` (emp.py:347-370);
+    with several terms each name carries the term's 1-based number
+    (block_repo.py:393-400).  'GonzRotationTerm' is the reference's two-SHO
+    rotation kernel (rho, tau, A1, A2; emp.py:397-412).
+    """
+    terms, plist = list(my_kernel['terms']), list(my_kernel['params'])
+    if len(terms) != len(plist) or not terms:
+        raise ValueError('my_kernel needs one params dict per term')
+    ps = []
+    for t, (term, pd) in enumerate(zip(terms, plist)):
+        if term not in _GP_NAMES:
+            raise ValueError(f'GP term {term!r} is not built ({", ".join(GP_TERMS)})')
+        if term == 'GonzRotationTerm':
+            pd = {k: pd.get(k) for k in ('rho', 'tau', 'A1', 'A2')}
+        for k, v in pd.items():
+            p = Parameter(f'{_GP_NAMES[term]} {k}' + (str(t + 1) if len(terms) > 1 else ''))
+            p.gp_term, p.gp_key = t, k
+            if v is not None:
+                p.fixed = float(v)
+            ps.append(p)
+    return Parameter_Block(ps, name_='CeleriteBlock', type_='Celerite2', class_='Model',
+                           number_=len(terms), my_kernel={'terms': terms, 'params': plist})
+
+
 class SmartSetter:
     """Data-derived default limits and priors (block_repo.py:505-868)."""
 
@@ -304,6 +340,12 @@ class SmartSetter:
         lims = [[1.5, per], [1e-6, amp], [1e-6, amp], list(self.angular), list(self.angular)]
         return lims, ['Uniform'] * 5, [None] * 5
 
+    def set_Celerite2(self, b, **kw):
+        """block_repo.py:761-790: free hyperparameters Uniform in [1e-5, 5]
+        ([1e-5, 1] for the RotationTerm mixing fraction f)."""
+        lims = [[1e-5, 1.0] if p.gp_key == 'f' else [1e-5, 5.0] for p in b]
+        return lims, ['Uniform' if p.fixed is None else 'Fixed' for p in b], [None] * len(lims)
+
     def set_Acceleration(self, b, **kw):
         return [[-1, 1]] * b.number_, ['Uniform'] * b.number_, [None] * b.number_
 
@@ -350,7 +392,8 @@ class ReddModel:
     free (``C_``) and fixed (``A_``) index maps, ``ndim__``.
     """
 
-    HOT_TYPES = ('Keplerian', 'Acceleration', 'Offset', 'Jitter', 'MOAV', 'Sinusoid', 'MagneticCycle')
+    HOT_TYPES = ('Keplerian', 'Acceleration', 'Offset', 'Jitter', 'MOAV', 'Sinusoid', 'MagneticCycle',
+                 'Celerite2')
 
     def __init__(self, blocks, data, moav_reference_quirk=False):
         self.blocks = list(blocks)
@@ -379,6 +422,11 @@ class ReddModel:
         self.mod_fixed = np.array(fixed, dtype=object)
         self.kplan__ = sum(1 for b in self.blocks if b.type_ == 'Keplerian')
         self.nins__ = self.data.nins
+        gp = [b for b in self.blocks if b.type_ == 'Celerite2']
+        if len(gp) > 1:
+            raise ValueError('one Celerite2 block per model')
+        if gp and any(b.type_ == 'MOAV' for b in self.blocks):
+            raise ValueError('a GP likelihood and a MOAV block cannot be combined on this path')
         # the MOAV residual is taken after every mean-model block
         seen_moav = False
         for b in self.blocks:
@@ -400,9 +448,39 @@ class ReddModel:
             if b.type_ == 'MOAV':
                 d['order'] = b.moav
                 d['global'] = b.is_global
+            if b.type_ == 'Celerite2':
+                d['gp_terms'] = self.gp_terms()
             out.append(d)
         return {'nins': self.nins__, 'blocks': out,
                 'moav_reference_quirk': self.moav_reference_quirk}
+
+    def gp_terms(self):
+        """[(kind, [full-theta slot of each canonical parameter])] of the
+        Celerite2 block (kinds and canonical orders of oracle.gp / EMP_GP_*)."""
+        out = []
+        for b in self.blocks:
+            if b.type_ != 'Celerite2':
+                continue
+            for t, term in enumerate(b.my_kernel['terms']):
+                slot = {p.gp_key: b.slice.start + i for i, p in enumerate(b) if p.gp_term == t}
+                keys = tuple(slot)
+                if term == 'SHOTerm':
+                    amp = 'sigma' if 'sigma' in slot else 'S0'
+                    freq = 'rho' if 'rho' in slot else 'w0'
+                    qual = 'tau' if 'tau' in slot else 'Q'
+                    if {amp, freq, qual} != set(keys):
+                        raise ValueError(f'SHOTerm keywords {sorted(keys)} are not (S0|sigma, w0|rho, Q|tau)')
+                    kind = N.EMP_GP_SHO + (amp == 'sigma') + 2 * (freq == 'rho') + 4 * (qual == 'tau')
+                    order = (amp, freq, qual)
+                else:
+                    kind, order = {'RealTerm': (N.EMP_GP_REAL, ('a', 'c')),
+                                   'Matern32Term': (N.EMP_GP_MATERN32, ('sigma', 'rho')),
+                                   'RotationTerm': (N.EMP_GP_ROTATION, ('sigma', 'period', 'Q0', 'dQ', 'f')),
+                                   'GonzRotationTerm': (N.EMP_GP_GROT, ('rho', 'tau', 'A1', 'A2'))}[term]
+                    if set(order) != set(keys):
+                        raise ValueError(f'{term} takes {order}, got {keys}')
+                out.append((kind, [slot[k] for k in order]))
+        return out
 
     def free_parameters(self):
         return [p for b in self.blocks for p in b if p.fixed is None]
@@ -450,6 +528,8 @@ class ReddModel:
                     md.derived[planet][0] = prior_struct('None', None, None)
                     md.derived[planet][1] = prior_struct('None', None, None)
                     planet += 1
+            elif b.type_ == 'Celerite2':
+                pass                                          # gp_terms below
             elif b.type_ == 'Offset':
                 md.offset_slot = s0
             elif b.type_ == 'Jitter':
@@ -478,6 +558,14 @@ class ReddModel:
                     md.full_src[slot] = -1
                     md.full_fixed[slot] = float(p.fixed)
         md.n_planets = planet
+        gpt = self.gp_terms()
+        if len(gpt) > N.EMP_MAX_GP_TERMS:
+            raise ValueError(f'{len(gpt)} GP terms exceed {N.EMP_MAX_GP_TERMS}')
+        md.gp_nterms = len(gpt)
+        for k, (kind, slots) in enumerate(gpt):
+            md.gp_kind[k] = kind
+            for i in range(5):
+                md.gp_slot[k][i] = slots[i] if i < len(slots) else -1
         md.loglike_const = float(- 0.5 * np.log(2 * np.pi) * self.data.ndata)
         # constant prior terms summed in my_prior's order (block by block,
         # each Keplerian block followed by its derived priors)

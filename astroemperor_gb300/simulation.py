@@ -15,7 +15,7 @@ Instead of writing a temporary script and running it in a child
 interpreter (``emp.py:137-175, 2559-2582``), ``run`` compiles the model
 (:class:`~astroemperor_gb300.model.ReddModel`) and runs the GPU
 :class:`~astroemperor_gb300.engine.PTSampler` in-process.  Plotting,
-logging and astrometry/GP blocks are not part of this path.
+logging and astrometry blocks are not part of this path.
 """
 from __future__ import annotations
 
@@ -25,8 +25,8 @@ import time
 import numpy as np
 
 from .data import RVData, load_target, preprocess_instruments
-from .model import (AccelerationBlock, JitterBlock, KeplerianBlock, MOAVBlock, OffsetBlock,
-                    ReddModel, SmartSetter, full_theta)
+from .model import (AccelerationBlock, CeleriteBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock,
+                    MOAVBlock, OffsetBlock, ReddModel, SinusoidBlock, SmartSetter, full_theta)
 from .stats import model_stats
 
 
@@ -46,6 +46,10 @@ class Simulation:
         self.switch_first_run = True
         self.moav = {'order': 0, 'global': False}
         self.moav_reference_quirk = False
+        self.switch_celerite = False
+        self.my_kernel = {'terms': ['RealTerm'], 'params': [{'a': None, 'c': None}]}
+        self.sinusoid = 0
+        self.magnetic_cycle = 0
         self.eccentricity_limits = [0, 1]
         self.eccentricity_prargs = [0, 0.1]
         self.jitter_limits = [0, 1]
@@ -135,8 +139,26 @@ class Simulation:
         self.SmartSetter(b)
         self.blocks__.append(b)
 
+    def add_celerite(self):
+        """emp.py:1283-1296: a celerite2 GP over the residuals, hyperparameters
+        from ``my_kernel``."""
+        b = CeleriteBlock(self.my_kernel)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def add_sinusoid(self):
+        b = SinusoidBlock(self.sinusoid)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def add_magnetic_cycle(self):
+        b = MagneticCycleBlock(self.magnetic_cycle)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
     def _autorun_add_RV_ins(self):
-        """emp.py:2628-2650 (the blocks of this path, in the same order)."""
+        """emp.py:2628-2650 (the blocks of this path, in the same order; the
+        astrometry-correction block is not on it)."""
         if self.acceleration:
             self.add_acceleration()
         self.add_offset()
@@ -144,6 +166,12 @@ class Simulation:
             self.add_jitter()
         if self.moav['order']:
             self.add_moav()
+        if self.switch_celerite:
+            self.add_celerite()
+        if self.sinusoid:
+            self.add_sinusoid()
+        if self.magnetic_cycle:
+            self.add_magnetic_cycle()
 
     # ------------------------------------------------------------ conditions
     def add_condition(self, cond):

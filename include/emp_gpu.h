@@ -28,12 +28,25 @@
 extern "C" {
 #endif
 
-#define EMP_ABI_VERSION 1
+#define EMP_ABI_VERSION 2
 
 #define EMP_MAX_PARAMS   160   /* full theta length incl. fixed parameters */
 #define EMP_MAX_PLANETS  16
 #define EMP_MAX_INS      16
 #define EMP_MAX_MA       3     /* moving-average order q */
+#define EMP_MAX_GP_TERMS 8
+
+/* GP terms of a celerite2 kernel (support/kernels/00.kernel, emp.py:341-412),
+   as k(tau) = sum exp(-c tau) (a cos(d tau) + b sin(d tau)); gp_slot[k][i]
+   is the full-theta index of the term's i-th parameter in the order below */
+#define EMP_GP_REAL      1   /* RealTerm(a, c) */
+#define EMP_GP_MATERN32  2   /* Matern32Term(sigma, rho), eps = 0.01 */
+#define EMP_GP_ROTATION  3   /* RotationTerm(sigma, period, Q0, dQ, f) */
+#define EMP_GP_GROT      4   /* the reference's GonzRotationTerm(rho, tau, A1, A2):
+                                SHO(S0=A1, rho, tau) + SHO(S0=A2, rho/2, tau) */
+#define EMP_GP_SHO      16   /* SHOTerm(amplitude, frequency, quality): + 1 if the
+                                amplitude is sigma (else S0), + 2 if the frequency is
+                                rho (else w0), + 4 if the quality is tau (else Q) */
 
 /* status codes */
 #define EMP_OK             0
@@ -115,6 +128,14 @@ typedef struct emp_model_desc {
     /* their indices: i < n_free -> free parameter i,
        n_free + 2p + k -> derived prior k of planet p */
     int32_t prior_var[EMP_MAX_PARAMS + 2 * EMP_MAX_PLANETS];
+    /* Gaussian-process likelihood (support/likelihoods/02.like): with
+       gp_nterms > 0 the log-likelihood is the celerite GP log-likelihood of the
+       residuals with diagonal err2 instead of the independent Gaussian sum;
+       not combined with MOAV */
+    int32_t gp_nterms;
+    int32_t _pad2;
+    int32_t gp_kind[EMP_MAX_GP_TERMS];
+    int32_t gp_slot[EMP_MAX_GP_TERMS][5];
 } emp_model_desc;
 
 /*

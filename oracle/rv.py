@@ -343,6 +343,8 @@ class OracleRV:
                 M1 = freq1 * X_ + phase1
                 M2 = freq2 * X_ + phase2
                 model0 += A1 * np.cos(M1) + A2 * np.cos(M2)
+            elif t == 'Celerite2':                             # hyperparameters only
+                pass
             elif t == 'Acceleration':                          # acc.model:2
                 model0 += np.polyval(np.concatenate([theta[sl], [0]]), (X_ - X_[0]))
             elif t == 'Offset':                                # offset00.model:3
@@ -423,7 +425,15 @@ class OracleRV:
                         residuals[idx[ii]] -= MA
 
     def my_likelihood(self, theta):
-        """support/likelihoods/00.like:3-5."""
+        """support/likelihoods/00.like:3-5; with a Celerite2 block
+        support/likelihoods/02.like (oracle/gp.py)."""
+        gp_terms = [b['gp_terms'] for b in self.blocks if b['type'] == 'Celerite2']
+        if gp_terms:
+            from . import gp
+            model, err2 = self.my_model(theta)
+            th = self.full_theta(theta)
+            co = gp.coefficients([(k, [th[i] for i in sl]) for k, sl in gp_terms[0]])
+            return gp.semisep_loglike(self.X_, self.Y_ - model, err2, co)
         model, err2 = self.my_model(theta)
         return -0.5 * (np.sum((self.Y_ - model) ** 2 / err2 + np.log(err2))) \
             + self.likelihood_constant

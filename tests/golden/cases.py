@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 
 from astroemperor_gb300.data import preprocess_instruments
-from astroemperor_gb300.model import (AccelerationBlock, JitterBlock, KeplerianBlock,
+from astroemperor_gb300.model import (AccelerationBlock, CeleriteBlock, JitterBlock, KeplerianBlock,
                                       MagneticCycleBlock, MOAVBlock, OffsetBlock, ReddModel,
                                       SinusoidBlock, SmartSetter)
 from astroemperor_gb300 import synth
@@ -33,7 +33,7 @@ def _kep(ss, par, number, **lims):
 
 
 def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=None, quirk=False,
-                sinusoid=False, cycle=False):
+                sinusoid=False, cycle=False, gp=None):
     data = peg_data(arr)
     ss = SmartSetter(data)
     blocks = []
@@ -77,7 +77,43 @@ def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=N
         mb = MOAVBlock(1, moav)
         ss(mb)
         blocks.append(mb)
+    if gp is not None:
+        gb = CeleriteBlock(gp)
+        ss(gb)
+        blocks.append(gb)
     return ReddModel(blocks, data, moav_reference_quirk=quirk), data
+
+
+# celerite2 kernels of the GP cases: name -> my_kernel (None: free)
+GP_KERNELS = {
+    'sho_rho_tau_sigma': {'terms': ['SHOTerm'], 'params': [{'rho': None, 'tau': None, 'sigma': None}]},
+    'sho_S0_w0_Q': {'terms': ['SHOTerm'], 'params': [{'S0': None, 'w0': None, 'Q': None}]},
+    'grot': {'terms': ['GonzRotationTerm'], 'params': [{'rho': None, 'tau': None, 'A1': None, 'A2': None}]},
+    'rotation': {'terms': ['RotationTerm'],
+                 'params': [{'sigma': None, 'period': None, 'Q0': None, 'dQ': None, 'f': None}]},
+    'real_matern': {'terms': ['RealTerm', 'Matern32Term'],
+                    'params': [{'a': None, 'c': 0.5}, {'sigma': None, 'rho': None}]},
+}
+
+
+def gp_case_models(arr, n_in=12, n_near=8):
+    """name -> (ReddModel, RVData, thetas): 51 Peg, one Keplerian, offset,
+    jitter and a celerite2 GP; thetas drawn inside the limits (some past
+    the eccentricity support), near the fit with GP amplitudes of a few m/s,
+    and out of bounds."""
+    rng = np.random.default_rng(20240917)
+    out = {}
+    for name, ker in GP_KERNELS.items():
+        m, d = model_51peg(arr, k=1, par=1, gp=ker)
+        free = m.free_parameters()
+        lim = m.limits_free()
+        c = np.array(PEG_MAP_P1 + [0.0] * (len(free) - len(PEG_MAP_P1)))
+        # GP hyperparameters near the middle of their limits
+        for j in range(len(PEG_MAP_P1), len(free)):
+            c[j] = 0.5 * (lim[j, 0] + lim[j, 1])
+        th = draw_thetas(m, rng, n_in=n_in, center=c, n_near=n_near)
+        out[name] = (m, d, th)
+    return out
 
 
 def draw_thetas(model, rng, n_in=24, center=None, spread=0.02, n_near=8, n_out=4):

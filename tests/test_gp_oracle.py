@@ -1,0 +1,143 @@
+"""Celerite GP likelihood on the CPU: the oracle's semiseparable recursion
+against the dense definition, the model layer's GP descriptor, and the
+Simulation block order of the reference's GP runs.
+
+Tolerance: recursion vs dense Cholesky, |dlogL| / |logL| <= 1e-10.
+"""
+import numpy as np
+import pytest
+
+from astroemperor_gb300 import _native as N
+from astroemperor_gb300.model import CeleriteBlock, MOAVBlock, ReddModel
+from oracle import gp
+from oracle.rv import OracleRV
+from tests.golden.cases import GP_KERNELS, gp_case_models, model_51peg, peg_data
+
+RTOL = 1e-10
+
+
+def _series(rng, n):
+    t = np.sort(rng.uniform(0, 300, n))
+    t[5] = t[4]                                    # a repeated epoch
+    return t, rng.normal(0, 3, n), rng.uniform(0.5, 4, n)
+
+
+TERM_CASES = [
+    (gp.GP_REAL, [2.0, 0.3]),
+    (gp.GP_MATERN32, [1.5, 4.0]),
+    (gp.GP_ROTATION, [2.0, 12.0, 0.8, 1.5, 0.4]),
+    (gp.GP_GROT, [9.0, 20.0, 3.0, 1.0]),
+    (gp.GP_GROT, [9.0, 0.5, 3.0, 1.0]),            # Q < 1/2: the real-component regime
+    (gp.GP_SHO, [4.0, 0.9, 3.0]),                  # S0, w0, Q
+    (gp.GP_SHO, [4.0, 0.9, 0.2]),                  # Q < 1/2
+    (gp.GP_SHO + 7, [2.0, 7.0, 15.0]),             # sigma, rho, tau
+    (gp.GP_SHO + 3, [2.0, 7.0, 0.3]),              # sigma, rho, Q
+]
+
+
+@pytest.mark.parametrize('kind,p', TERM_CASES)
+def test_semiseparable_recursion_equals_dense(kind, p):
+    rng = np.random.default_rng(kind * 31 + len(p))
+    t, r, diag = _series(rng, 120)
+    co = gp.coefficients([(kind, p)])
+    a = gp.semisep_loglike(t, r, diag, co)
+    b = gp.dense_loglike(t, r, diag, co)
+    assert np.isfinite(a)
+    assert abs(a - b) <= RTOL * abs(b), (a, b)
+
+
+def test_sum_of_terms_equals_dense():
+    rng = np.random.default_rng(5)
+    t, r, diag = _series(rng, 200)
+    terms = [(gp.GP_REAL, [1.0, 0.05]), (gp.GP_SHO + 7, [2.0, 7.0, 15.0]), (gp.GP_GROT, [9.0, 20.0, 3.0, 1.0])]
+    co = gp.coefficients(terms)
+    assert len(co[0]) == 1 and len(co[2]) == 3
+    a = gp.semisep_loglike(t, r, diag, co)
+    b = gp.dense_loglike(t, r, diag, co)
+    assert abs(a - b) <= RTOL * abs(b)
+
+
+def test_sho_parameterisations_agree():
+    # (sigma, rho, tau) and the equivalent (S0, w0, Q) give one kernel
+    sigma, rho, tau = 2.0, 7.0, 15.0
+    w0 = 2 * np.pi / rho
+    Q = 0.5 * w0 * tau
+    S0 = sigma ** 2 / (w0 * Q)
+    tau_grid = np.linspace(0, 50, 11)
+    k1 = gp.kernel_value(gp.coefficients([(gp.GP_SHO + 7, [sigma, rho, tau])]), tau_grid)
+    k2 = gp.kernel_value(gp.coefficients([(gp.GP_SHO, [S0, w0, Q])]), tau_grid)
+    np.testing.assert_allclose(k1, k2, rtol=1e-14)
+    assert abs(k1[0] - sigma ** 2) < 1e-12
+
+
+def test_model_descriptor_gp_fields(peg_arr):
+    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['real_matern'])
+    terms = m.gp_terms()
+    names = [p.name for b in m.blocks for p in b]
+    assert names[-4:] == ['Real Term a1', 'Real Term c1', 'Matern32 Term sigma2', 'Matern32 Term rho2']
+    assert [k for k, _ in terms] == [N.EMP_GP_REAL, N.EMP_GP_MATERN32]
+    md = m.descriptor()
+    assert md.gp_nterms == 2
+    assert list(md.gp_kind[:2]) == [N.EMP_GP_REAL, N.EMP_GP_MATERN32]
+    assert list(md.gp_slot[0]) == terms[0][1] + [-1, -1, -1]
+    assert list(md.gp_slot[1]) == terms[1][1] + [-1, -1, -1]
+    # the fixed RealTerm c is a fixed slot, the others are free
+    c_slot = terms[0][1][1]
+    assert md.full_src[c_slot] == -1 and md.full_fixed[c_slot] == 0.5
+    assert all(md.full_src[s] >= 0 for s in terms[1][1])
+    # default limits of the reference's smart setter
+    lim = m.limits_free()
+    np.testing.assert_allclose(lim[-3:], [[1e-5, 5.0]] * 3)
+
+
+def test_sho_kinds_and_rotation_mixing_limit(peg_arr):
+    m, _ = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['sho_rho_tau_sigma'])
+    (kind, slots), = m.gp_terms()
+    assert kind == N.EMP_GP_SHO + 7
+    names = [p.name for b in m.blocks for p in b]
+    # canonical order (sigma, rho, tau) from the dictionary order (rho, tau, sigma)
+    assert [names[s] for s in slots] == ['SHO Term sigma', 'SHO Term rho', 'SHO Term tau']
+    m, _ = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['rotation'])
+    lim = m.limits_free()
+    np.testing.assert_allclose(lim[-1], [1e-5, 1.0])
+
+
+def test_oracle_gp_likelihood_equals_dense(peg_arr):
+    cases = gp_case_models(peg_arr, n_in=4, n_near=3)
+    for name, (m, d, th) in cases.items():
+        o = OracleRV(m.spec(), d.as_dict())
+        (terms,) = [b['gp_terms'] for b in o.blocks if b['type'] == 'Celerite2']
+        n_fin = 0
+        for x in th:
+            if not np.isfinite(o.my_prior(x)):
+                continue
+            model, err2 = o.my_model(x)
+            full = o.full_theta(x)
+            co = gp.coefficients([(k, [full[i] for i in sl]) for k, sl in terms])
+            dense = gp.dense_loglike(o.X_, o.Y_ - model, err2, co)
+            assert abs(o.my_likelihood(x) - dense) <= RTOL * abs(dense), name
+            n_fin += 1
+        assert n_fin >= 3, name
+
+
+def test_gp_with_moav_rejected(peg_arr):
+    data = peg_data(peg_arr)
+    with pytest.raises(ValueError, match='MOAV'):
+        ReddModel([MOAVBlock(1, {'order': 1, 'global': True}), CeleriteBlock(GP_KERNELS['grot'])], data)
+
+
+def test_unknown_term_rejected():
+    with pytest.raises(ValueError, match='not built'):
+        CeleriteBlock({'terms': ['CosineTerm'], 'params': [{'sigma': None, 'period': None}]})
+
+
+def test_simulation_block_order(peg_arr):
+    from astroemperor_gb300.simulation import Simulation
+    sim = Simulation()
+    sim.load_arrays([peg_arr], ['51peg.vels'])
+    sim.switch_celerite = True
+    sim.my_kernel = GP_KERNELS['grot']
+    sim.sinusoid = 1
+    sim._autorun_add_RV_ins()
+    # emp.py:2628-2650: offset, jitter, celerite, sinusoid
+    assert [b.type_ for b in sim.blocks__] == ['Offset', 'Jitter', 'Celerite2', 'Sinusoid']
