@@ -45,22 +45,22 @@ def candidates(n_epochs, batch):
     return out
 
 
-def graph_time(args, reps, stream):
-    """Device milliseconds per ``emp_logpost(*args)`` launch: ``reps``
-    launches (fewer for launches above ~5 ms) captured in one CUDA graph and
-    replayed between two events, so that host-side call overhead does not
-    enter the measurement."""
+def graph_time(args, reps, stream, entry='emp_logpost'):
+    """Device milliseconds per ``entry(*args)`` call (default
+    ``emp_logpost``): ``reps`` calls (fewer for calls above ~5 ms) captured
+    in one CUDA graph and replayed between two events, so that host-side call
+    overhead does not enter the measurement."""
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with torch.cuda.stream(stream):
         e0.record(stream)
-        N.call('emp_logpost', *args)                               # warm, sets attributes
+        N.call(entry, *args)                                       # warm, sets attributes
         e1.record(stream)
     e1.synchronize()
     reps = int(max(1, min(reps, round(20.0 / max(e0.elapsed_time(e1), 1e-3)))))
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g, stream=stream):
         for _ in range(reps):
-            N.call('emp_logpost', *args)
+            N.call(entry, *args)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     # replay() launches on the current stream: keep the warm-up and the
     # timed replay on the same stream so that they cannot overlap

@@ -100,7 +100,8 @@ struct DevData {
     const int* inst;       // [n] 0-based instrument
 };
 
-enum Mode : int { kModeLogpost = 0, kModeStretch = 1, kModeSlots = 2 };
+// kModeGPOnly: k_gp alone on caller residual rows (emp_gp_logl)
+enum Mode : int { kModeLogpost = 0, kModeStretch = 1, kModeSlots = 2, kModeGPOnly = 3 };
 
 // what the stretch kernel hands to the GP kernel per proposal
 struct GPMeta {
@@ -155,6 +156,10 @@ struct KArgs {
     double* gp_e;
     double* gp_prop;           // [nwalk][dstride] proposals (stretch)
     GPMeta* gp_meta;           // [nwalk] (stretch)
+    double* gp_u;              // [n][nwalk][M] U, V and phi of the recursion (k_gp_prep)
+    double* gp_v;
+    double* gp_ph;
+    double* gp_asum;           // [nwalk] k(0) of each row's kernel (NaN: bad coefficients)
 };
 
 

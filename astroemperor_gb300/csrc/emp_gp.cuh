@@ -16,10 +16,15 @@
 //   f_n = phi_n (f_{n-1} + W_{n-1} z_{n-1}), z_n = r_n - U_n^T f_n,
 //   logL = -0.5 sum(z_n^2 / D_n + log D_n) - 0.5 N log(2 pi).
 //
-// k_logpost writes each valid row's residuals and err2 (epoch-major, so the
-// threads of a warp -- one row each -- read consecutive addresses) and the
-// prior; k_gp runs the recursion in FP64, one thread per row, and finishes the
-// mode: log-posterior rows, state slots, or the stretch move's Metropolis test.
+// k_logpost writes each valid row's residuals and err2 (epoch-major) and the
+// prior; k_gp_prep evaluates, for every (row, epoch) in parallel, the parts of
+// the recursion that do not depend on its state (the sincos and exp); k_gp
+// runs the sequential recursion in FP64 with one lane per state dimension and
+// finishes the mode: log-posterior rows, state slots, or the stretch move's
+// Metropolis test.  FP64 on this GPU issues one warp instruction per ~64
+// cycles per SM sub-partition, so the recursion is bound by the length of its
+// per-epoch FP64 chain: the transcendentals leave it for the parallel kernel,
+// the lanes share a row's S, and log det needs no log per epoch.
 #pragma once
 
 #include "emp_kernels.cuh"
@@ -114,129 +119,196 @@ __device__ inline int gp_fill(const emp_model_desc* md, const double* th, GPDim*
     return k;
 }
 
-// log-likelihood of one row; r and e are the row's residuals and err2 with
-// stride ld between epochs
+// the prior and free parameters of row `row` in the launch's mode
+__device__ inline double gp_row(const KArgs& A, int row, const double** th) {
+    const int ds = A.dstride;
+    if (A.mode == kModeGPOnly) { *th = A.theta + (size_t)row * ds; return 0.0; }
+    if (A.mode == kModeLogpost) { *th = A.theta + (size_t)row * ds; return A.logprior[row]; }
+    if (A.mode == kModeSlots) { *th = A.st_theta + (size_t)row * ds; return A.st_logprior[row]; }
+    *th = A.gp_prop + (size_t)row * ds;
+    return A.gp_meta[row].lp;
+}
+
+// Everything of the recursion that does not depend on its state, for every
+// (row, epoch) in parallel: U_n, V_n and phi_n (one sincos and one exp per
+// component).  Thread (row, g): rows across the warp's lanes (coalesced
+// [n][rows][M] writes), epochs g, g + E, ... with E = 8 * gridDim.y.
 template <int M>
-__device__ double gp_loglike(const emp_model_desc* md, const double* th, const double* t, int n,
-                             const double* r, const double* e, int ld) {
+__global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
+    const int row = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int E = gridDim.y * 8;
+    const int g = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (row >= A.nwalk) return;
+    const double* th;
+    const double lp = gp_row(A, row, &th);
+    if (!(lp > -INFINITY)) return;
     double pa[M], pb[M], pc[M], pd[M], pv[M];
     bool ps[M];
+    bool finite = true;
     double asum = 0.0;
     {
         GPDim dm[M];
 #pragma unroll
         for (int k = 0; k < M; ++k) dm[k] = GPDim{0.0, 0.0, 0.0, 0.0, 0, 0};
-        gp_fill(md, th, dm);
+        gp_fill(A.md, th, dm);
 #pragma unroll
         for (int k = 0; k < M; ++k) {
             pa[k] = dm[k].a; pb[k] = dm[k].b; pc[k] = dm[k].c; pd[k] = dm[k].d;
             ps[k] = dm[k].sinpart != 0;
             pv[k] = dm[k].live ? 1.0 : 0.0;
             if (!ps[k]) asum += dm[k].a;
-            if (!(isfinite(dm[k].a) && isfinite(dm[k].b) && isfinite(dm[k].c) && isfinite(dm[k].d)))
-                return -INFINITY;
+            finite = finite && isfinite(dm[k].a) && isfinite(dm[k].b) && isfinite(dm[k].c) &&
+                     isfinite(dm[k].d);
         }
     }
-    // S is symmetric: the upper triangle is kept
-    double S[M][M], f[M], W[M];
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        f[i] = 0.0; W[i] = 0.0;
-#pragma unroll
-        for (int j = 0; j < M; ++j) S[i][j] = 0.0;
-    }
-    double Dp = 0.0, zp = 0.0, tp = 0.0, quad = 0.0, logdet = 0.0;
-    for (int i = 0; i < n; ++i) {
+    if (g == 0) A.gp_asum[row] = finite ? asum : NAN;
+    if (!finite) return;
+    const double* t = A.d.t;
+    const int n = A.d.n;
+    for (int i = g; i < n; i += E) {
         const double ti = t[i];
-        const double ri = r[(size_t)i * ld];
-        const double ei = e[(size_t)i * ld];
-        double U[M], V[M];
+        const double dt = i > 0 ? ti - t[i - 1] : 0.0;
+        double sn[M], cs[M], ph[M];
+        double* u = A.gp_u + ((size_t)i * A.nwalk + row) * M;
+        double* v = A.gp_v + ((size_t)i * A.nwalk + row) * M;
+        double* q = A.gp_ph + ((size_t)i * A.nwalk + row) * M;
 #pragma unroll
         for (int k = 0; k < M; ++k) {
-            double sn, cs;
-            sincos(pd[k] * ti, &sn, &cs);
-            U[k] = ps[k] ? pa[k] * sn - pb[k] * cs : pa[k] * cs + pb[k] * sn;
-            V[k] = pv[k] * (ps[k] ? sn : cs);
-        }
-        if (i > 0) {
-            const double dt = ti - tp;
-            double ph[M];
-#pragma unroll
-            for (int k = 0; k < M; ++k) ph[k] = exp(-pc[k] * dt);
-#pragma unroll
-            for (int a = 0; a < M; ++a) {
-#pragma unroll
-                for (int b = a; b < M; ++b) S[a][b] = ph[a] * ph[b] * fma(Dp * W[a], W[b], S[a][b]);
-                f[a] = ph[a] * fma(W[a], zp, f[a]);
+            if (k > 0 && ps[k]) { sn[k] = sn[k - 1]; cs[k] = cs[k - 1]; ph[k] = ph[k - 1]; }
+            else {
+                if (pd[k] != 0.0) sincos(pd[k] * ti, &sn[k], &cs[k]);
+                else { sn[k] = 0.0; cs[k] = 1.0; }
+                ph[k] = pc[k] != 0.0 ? exp(-pc[k] * dt) : 1.0;
             }
+            u[k] = ps[k] ? pa[k] * sn[k] - pb[k] * cs[k] : pa[k] * cs[k] + pb[k] * sn[k];
+            v[k] = pv[k] * (ps[k] ? sn[k] : cs[k]);
+            q[k] = ph[k];
         }
-        double SU[M];
-#pragma unroll
-        for (int a = 0; a < M; ++a) {
-            double s = 0.0;
-#pragma unroll
-            for (int b = 0; b < M; ++b) s = fma(a <= b ? S[a][b] : S[b][a], U[b], s);
-            SU[a] = s;
-        }
-        double uSu = 0.0, uf = 0.0;
-#pragma unroll
-        for (int a = 0; a < M; ++a) { uSu = fma(U[a], SU[a], uSu); uf = fma(U[a], f[a], uf); }
-        const double D = ei + asum - uSu;
-        if (!(D > 0.0)) return -INFINITY;
-        const double iD = 1.0 / D;
-#pragma unroll
-        for (int a = 0; a < M; ++a) W[a] = (V[a] - SU[a]) * iD;
-        const double z = ri - uf;
-        quad = fma(z * z, iD, quad);
-        logdet += log(D);
-        Dp = D; zp = z; tp = ti;
     }
-    return -0.5 * (quad + logdet) + md->loglike_const;
 }
 
-// one thread per walker row of the preceding k_logpost launch (same KArgs)
+// The sequential recursion, M lanes per row (lane k owns state dimension k:
+// row k of S, f_k, W_k), 32/M rows per warp.  Per epoch a lane does its S row
+// update, (S U)_k and its W_k; U^T S U and U^T f are summed over the row's
+// lanes by a butterfly (commutative, so every lane holds the same sum), and
+// log det K is kept as a product renormalised to [1, 2) with its exponent
+// counted, so no log is taken per epoch.  All lanes of a warp run every
+// epoch (rows past the launch's rows repeat the last row; rows outside the
+// prior compute on unwritten residuals and are discarded), which keeps the
+// shuffles convergent.
 template <int M>
-__global__ void __launch_bounds__(32) k_gp(KArgs A) {
-    const int row = blockIdx.x * blockDim.x + threadIdx.x;
-    if (row >= A.nwalk) return;
+__global__ void __launch_bounds__(128) k_gp(KArgs A) {
+    const unsigned FULL = 0xffffffffu;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rowr = gtid / M;
+    const int k = gtid & (M - 1);
+    const bool live = rowr < A.nwalk;
+    const int row = live ? rowr : A.nwalk - 1;
     const emp_model_desc* md = A.md;
-    const int ds = A.dstride;
-    double lp;
-    const double* free_th;
-    GPMeta m{};
-    if (A.mode == kModeLogpost) {
-        lp = A.logprior[row];
-        free_th = A.theta + (size_t)row * ds;
-    } else if (A.mode == kModeSlots) {
-        lp = A.st_logprior[row];
-        free_th = A.st_theta + (size_t)row * ds;
-    } else {
-        m = A.gp_meta[row];
-        lp = m.lp;
-        free_th = A.gp_prop + (size_t)row * ds;
+    const double* th;
+    const double lp = gp_row(A, row, &th);
+    const bool valid = live && (lp > -INFINITY);
+    const double asum = valid ? A.gp_asum[row] : 0.0;
+    const size_t ld = (size_t)A.nwalk;
+    const int n = A.d.n;
+    const double* Up = A.gp_u + (size_t)row * M + k;
+    const double* Vp = A.gp_v + (size_t)row * M + k;
+    const double* Pp = A.gp_ph + (size_t)row * M + k;
+    const double* rp = A.gp_r + row;
+    const double* ep = A.gp_e + row;
+    double S[M];
+#pragma unroll
+    for (int j = 0; j < M; ++j) S[j] = 0.0;
+    double f = 0.0, W = 0.0, Dp = 0.0, zp = 0.0, quad = 0.0, prod = 1.0;
+    int pexp = 0;
+    bool bad = !isfinite(asum);
+    double Uk = 0.0, Vk = 0.0, Pk = 1.0, ri = 0.0, ei = 1.0;
+    if (valid) { Uk = Up[0]; Vk = Vp[0]; Pk = Pp[0]; ri = rp[0]; ei = ep[0]; }
+    for (int i = 0; i < n; ++i) {
+        // the next epoch's inputs are loaded while this one computes
+        double Un = 0.0, Vn = 0.0, Pn = 1.0, rn = 0.0, en = 1.0;
+        if (valid && i + 1 < n) {
+            const size_t o = (size_t)(i + 1) * ld;
+            Un = Up[o * M]; Vn = Vp[o * M]; Pn = Pp[o * M]; rn = rp[o]; en = ep[o];
+        }
+        double Uj[M];
+#pragma unroll
+        for (int j = 0; j < M; ++j) Uj[j] = __shfl_sync(FULL, Uk, j, M);
+        if (i > 0) {
+            const double dw = Dp * W;
+#pragma unroll
+            for (int j = 0; j < M; ++j) {
+                const double Wj = __shfl_sync(FULL, W, j, M);
+                const double pj = __shfl_sync(FULL, Pk, j, M);
+                S[j] = (Pk * pj) * fma(dw, Wj, S[j]);
+            }
+            f = Pk * fma(W, zp, f);
+        }
+        double su = 0.0;
+#pragma unroll
+        for (int j = 0; j < M; ++j) su = fma(S[j], Uj[j], su);
+        double p1 = Uk * su, p2 = Uk * f;
+#pragma unroll
+        for (int off = M / 2; off >= 1; off >>= 1) {
+            p1 += __shfl_xor_sync(FULL, p1, off, M);
+            p2 += __shfl_xor_sync(FULL, p2, off, M);
+        }
+        const double D = ei + asum - p1;
+        bad = bad || !(D > 0.0);
+        const double iD = 1.0 / D;
+        W = (Vk - su) * iD;
+        const double z = ri - p2;
+        quad = fma(z * z, iD, quad);
+        // prod *= D, then its binary exponent moves into pexp
+        prod *= D;
+        {
+            const int hi = __double2hiint(prod);
+            const int ex = ((hi >> 20) & 0x7ff) - 1023;
+            pexp += ex;
+            prod = __hiloint2double(hi - (int)((unsigned)ex << 20), __double2loint(prod));
+        }
+        Dp = D; zp = z;
+        Uk = Un; Vk = Vn; Pk = Pn; ri = rn; ei = en;
     }
     double ll = -INFINITY;
-    if (lp > -INFINITY)
-        ll = gp_loglike<M>(md, free_th, A.d.t, A.d.n, A.gp_r + row, A.gp_e + row, A.nwalk);
-    if (A.mode == kModeLogpost) {
-        A.logl[row] = lp > -INFINITY ? ll : -INFINITY;
-        if (A.logp != nullptr && A.beta != nullptr)
-            A.logp[row] = (lp > -INFINITY && ll > -INFINITY) ? __dadd_rn(__dmul_rn(A.beta[row], ll), lp)
-                                                              : -INFINITY;
+    if (valid && !bad) {
+        const double logdet = log(prod) + (double)pexp * 0.6931471805599453;
+        ll = -0.5 * (quad + logdet) + md->loglike_const;
+        if (!isfinite(ll)) ll = -INFINITY;
+    }
+    if (A.mode == kModeGPOnly) {
+        if (live && k == 0) A.logl[row] = ll;
+    } else if (A.mode == kModeLogpost) {
+        if (live && k == 0) {
+            A.logl[row] = valid ? ll : -INFINITY;
+            if (A.logp != nullptr && A.beta != nullptr)
+                A.logp[row] = (valid && ll > -INFINITY) ? __dadd_rn(__dmul_rn(A.beta[row], ll), lp) : -INFINITY;
+        }
     } else if (A.mode == kModeSlots) {
-        A.st_logl[row] = ll;
-    } else if (lp > -INFINITY && ll > -INFINITY) {
-        const double beta = A.betas[m.t];
-        const double lpj = A.st_logprior[m.slot];
-        const double llj = A.st_logl[m.slot];
-        const double cur = lpj > -INFINITY ? __dadd_rn(__dmul_rn(beta, llj), lpj) : -INFINITY;
-        const double nlp = __dadd_rn(__dmul_rn(beta, ll), lp);
-        if (metropolis(nlp, cur, m.z, md->n_free - 1, m.uword)) {
-            A.st_logl[m.slot] = ll;
-            A.st_logprior[m.slot] = lp;
-            A.accepted[m.pos] += 1;
-            double* dst = A.st_theta + (size_t)m.slot * ds;
-            for (int d = 0; d < md->n_free; ++d) dst[d] = free_th[d];
+        if (live && k == 0) A.st_logl[row] = ll;
+    } else {
+        // stretch: every lane of the row takes the same decision; the
+        // current walker's values are read before lane 0 replaces them
+        bool acc = false;
+        GPMeta m{};
+        if (valid && ll > -INFINITY) {
+            m = A.gp_meta[row];
+            const double beta = A.betas[m.t];
+            const double lpj = A.st_logprior[m.slot];
+            const double llj = A.st_logl[m.slot];
+            const double cur = lpj > -INFINITY ? __dadd_rn(__dmul_rn(beta, llj), lpj) : -INFINITY;
+            const double nlp = __dadd_rn(__dmul_rn(beta, ll), lp);
+            acc = metropolis(nlp, cur, m.z, md->n_free - 1, m.uword);
+        }
+        __syncwarp();
+        if (acc) {
+            if (k == 0) {
+                A.st_logl[m.slot] = ll;
+                A.st_logprior[m.slot] = lp;
+                A.accepted[m.pos] += 1;
+            }
+            double* dst = A.st_theta + (size_t)m.slot * A.dstride;
+            for (int d = k; d < md->n_free; d += M) dst[d] = th[d];
         }
     }
 }

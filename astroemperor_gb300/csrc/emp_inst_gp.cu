@@ -6,12 +6,14 @@ namespace emp {
 
 using KFn = void (*)(KArgs);
 
-KFn get_kernel_gp(int M) {
+// the recursion kernel of M state dimensions, or (prep != 0) its parallel
+// preparation kernel
+KFn get_kernel_gp(int M, int prep) {
     switch (M) {
-        case 2: return k_gp<2>;
-        case 4: return k_gp<4>;
-        case 8: return k_gp<8>;
-        case 16: return k_gp<16>;
+        case 2: return prep ? k_gp_prep<2> : k_gp<2>;
+        case 4: return prep ? k_gp_prep<4> : k_gp<4>;
+        case 8: return prep ? k_gp_prep<8> : k_gp<8>;
+        case 16: return prep ? k_gp_prep<16> : k_gp<16>;
         default: return nullptr;
     }
 }

@@ -27,7 +27,7 @@ KFn get_kernel_fp64(int q, int lidx);
 KFn get_kernel_mixed(int q, int lidx);
 using GFn = void (*)(GArgs);
 GFn get_kernel_grad(int q, int lidx);
-KFn get_kernel_gp(int M);
+KFn get_kernel_gp(int M, int prep);
 }  // namespace emp
 
 using namespace emp;
@@ -112,10 +112,17 @@ struct emp_handle {
     double* gp_e = nullptr;
     double* gp_prop = nullptr;
     GPMeta* gp_meta = nullptr;
+    double* gp_u = nullptr;
+    double* gp_v = nullptr;
+    double* gp_ph = nullptr;
+    double* gp_asum = nullptr;
+    int sms = 0;
 };
 
 // dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
 static const size_t kSwapSmemMax = 200 * 1024;
+// threads per CTA of the GP recursion (M lanes per walker row)
+static const int kGPBlock = 128;
 
 namespace {
 
@@ -296,6 +303,9 @@ int prepare_eval(emp_handle* h, int prec) {
     return EMP_OK;
 }
 
+void gp_args(const emp_handle* h, KArgs& a);
+int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s);
+
 // counter: for a batch, the int that CTAs of a persistent launch claim
 // items from (zeroed here, in stream order); null launches one CTA per item
 int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* counter = nullptr) {
@@ -330,16 +340,12 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     a.sys_t0 = h->sys_t0;
     a.sys_order = h->sys_order;
     if (a.nwalk <= 0) return EMP_OK;
-    KFn gfn = nullptr;
+    bool gp = false;
     if (h->gp_M > 0) {
         if (a.nwalk > h->gp_rows)
             return fail(EMP_E_INVALID, "GP workspace holds %lld rows, launch has %d", (long long)h->gp_rows, a.nwalk);
-        gfn = get_kernel_gp(h->gp_M);
-        if (!gfn) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", h->gp_M);
-        a.gp_r = h->gp_r;
-        a.gp_e = h->gp_e;
-        a.gp_prop = h->gp_prop;
-        a.gp_meta = h->gp_meta;
+        gp = true;
+        gp_args(h, a);
     }
     a.cps = (a.nwalk + G - 1) / G;
     const int64_t items = (int64_t)a.cps * h->n_sys;
@@ -354,12 +360,7 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     fn<<<grid, NT, lay.total, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
-    if (gfn) {
-        // one thread (one warp per 32 rows) per row: the rows spread over the SMs
-        gfn<<<(a.nwalk + 31) / 32, 32, 0, s>>>(a);
-        g_launches.fetch_add(1);
-        CUDA_TRY(cudaGetLastError());
-    }
+    if (gp) return launch_gp(h, a, s);
     return EMP_OK;
 }
 
@@ -374,7 +375,9 @@ int gp_reserve(emp_handle* h, int64_t rows) {
     const size_t b_re = up(8 * n * (size_t)rows);
     const size_t b_prop = up(8 * D * (size_t)rows);
     const size_t b_meta = up(sizeof(GPMeta) * (size_t)rows);
-    const size_t total = 2 * b_re + b_prop + b_meta;
+    const size_t b_uvp = up(8 * n * (size_t)rows * (size_t)h->gp_M);
+    const size_t b_asum = up(8 * (size_t)rows);
+    const size_t total = 2 * b_re + b_prop + b_meta + 3 * b_uvp + b_asum;
     if (total > ((size_t)64 << 30))
         return fail(EMP_E_SIZE, "GP workspace of %zu B for %lld rows exceeds 64 GiB", total, (long long)rows);
     h->gc.reset();
@@ -391,7 +394,47 @@ int gp_reserve(emp_handle* h, int64_t rows) {
     h->gp_e = (double*)(c + b_re);
     h->gp_prop = (double*)(c + 2 * b_re);
     h->gp_meta = (GPMeta*)(c + 2 * b_re + b_prop);
+    unsigned char* c2 = c + 2 * b_re + b_prop + b_meta;
+    h->gp_u = (double*)c2;
+    h->gp_v = (double*)(c2 + b_uvp);
+    h->gp_ph = (double*)(c2 + 2 * b_uvp);
+    h->gp_asum = (double*)(c2 + 3 * b_uvp);
+    if (h->sms <= 0) {
+        int dev = 0;
+        CUDA_TRY(cudaGetDevice(&dev));
+        CUDA_TRY(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, dev));
+    }
     h->gp_rows = rows;
+    return EMP_OK;
+}
+
+void gp_args(const emp_handle* h, KArgs& a) {
+    a.gp_r = h->gp_r;
+    a.gp_e = h->gp_e;
+    a.gp_prop = h->gp_prop;
+    a.gp_meta = h->gp_meta;
+    a.gp_u = h->gp_u;
+    a.gp_v = h->gp_v;
+    a.gp_ph = h->gp_ph;
+    a.gp_asum = h->gp_asum;
+}
+
+// k_gp_prep (every row x epoch, about 16 warps per SM) then the recursion
+// k_gp (M lanes per row) for the rows of `a`
+int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s) {
+    const int M = h->gp_M;
+    KFn prep = get_kernel_gp(M, 1), rec = get_kernel_gp(M, 0);
+    if (!prep || !rec) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", M);
+    const int gx = (a.nwalk + 31) / 32;
+    const int want_warps = std::max(1, h->sms) * 16;
+    const int gy = std::max(1, std::min((h->n + 7) / 8, (want_warps + 8 * gx - 1) / (8 * gx)));
+    prep<<<dim3(gx, gy), 256, 0, s>>>(a);
+    g_launches.fetch_add(1);
+    CUDA_TRY(cudaGetLastError());
+    const int64_t threads = (int64_t)a.nwalk * M;
+    rec<<<(unsigned)((threads + kGPBlock - 1) / kGPBlock), kGPBlock, 0, s>>>(a);
+    g_launches.fetch_add(1);
+    CUDA_TRY(cudaGetLastError());
     return EMP_OK;
 }
 
@@ -459,7 +502,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                 a.a_inv_exact = frexp(st->a, &ex) == 0.5 ? 1.0 / st->a : 0.0;   // a = 2^(ex-1)
             }
             if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr))) return rc;
-            kcount += h->gp_M > 0 ? 2 : 1;
+            kcount += h->gp_M > 0 ? 3 : 1;
         }
     }
     SwapArgs S{};
@@ -900,6 +943,29 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, dou
         CUDA_TRY(cudaGetLastError());
     }
     return EMP_OK;
+}
+
+int emp_gp_logl(emp_handle* h, const double* theta, int B, const double* resid, const double* err2,
+                double* logl, void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (h->gp_M == 0) return fail(EMP_E_UNSUPPORTED, "the handle's model has no GP");
+    if (B < 0) return fail(EMP_E_INVALID, "B=%d < 0", B);
+    if (B == 0) return EMP_OK;
+    if (!theta || !resid || !err2 || !logl) return fail(EMP_E_INVALID, "a NULL argument");
+    int rc = gp_reserve(h, B);
+    if (rc) return rc;
+    KArgs a{};
+    a.md = h->md_dev;
+    a.d = h->dd;
+    a.mode = kModeGPOnly;
+    a.nwalk = B;
+    a.theta = theta;
+    a.logl = logl;
+    a.dstride = h->lay[1];
+    gp_args(h, a);
+    a.gp_r = const_cast<double*>(resid);
+    a.gp_e = const_cast<double*>(err2);
+    return launch_gp(h, a, (cudaStream_t)stream);
 }
 
 int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, double* logprior,

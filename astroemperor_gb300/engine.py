@@ -140,6 +140,19 @@ class Context:
         N.call('emp_model_eval', self.h, _ptr(theta), B, _ptr(model), _ptr(err2), s.cuda_stream)
         return model, err2
 
+    def gp_logl(self, theta: torch.Tensor, resid: torch.Tensor, err2: torch.Tensor, stream=None):
+        """Celerite GP log-likelihood [B] of residual rows resid [B, ndata] with
+        diagonal err2 [B, ndata] (time order) under the GP hyperparameters of
+        theta [B, ndim] -- ``gp_.log_likelihood(Y_)`` with ``gp_.mean = model``."""
+        theta = theta.contiguous()
+        B = theta.shape[0]
+        r = resid.t().contiguous()                     # epoch-major [ndata, B]
+        e = err2.t().contiguous()
+        logl = torch.empty(B, dtype=torch.float64, device=theta.device)
+        s = stream if stream is not None else torch.cuda.current_stream(theta.device)
+        N.call('emp_gp_logl', self.h, _ptr(theta), B, _ptr(r), _ptr(e), _ptr(logl), s.cuda_stream)
+        return logl
+
 
 PRECISIONS = {'fp64': N.EMP_PREC_FP64, 'mixed': N.EMP_PREC_MIXED,
               N.EMP_PREC_FP64: N.EMP_PREC_FP64, N.EMP_PREC_MIXED: N.EMP_PREC_MIXED}

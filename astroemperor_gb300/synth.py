@@ -22,7 +22,8 @@ from __future__ import annotations
 import numpy as np
 
 from .data import preprocess_instruments
-from .model import JitterBlock, KeplerianBlock, MOAVBlock, OffsetBlock, ReddModel, SmartSetter
+from .model import (CeleriteBlock, JitterBlock, KeplerianBlock, MOAVBlock, OffsetBlock, ReddModel,
+                    SmartSetter)
 
 BJD0 = 2450000.0
 
@@ -83,7 +84,33 @@ CONFIGS = {
                K=[8.0, 6.0, 10.0, 4.0, 12.0, 7.0, 15.0], e=None, w=None,
                offsets=[0.0, 20.0, -10.0, 35.0], jitters=[1.0, 1.5, 2.0, 3.0],
                ma=dict(order=2, phi=[0.4, 0.2], tau=[5.0, 10.0]), setup=[32, 1024, 5000, 1]),
+    # C2's planets and cadence with stellar-rotation noise instead of MA: a
+    # GonzRotationTerm GP (SHO terms at the rotation period and its half)
+    'gp': dict(n=1024, nins=2, split=[614, 410], span=3000.0, clumpy=True,
+               P=[4.6, 61.0, 1250.0], K=[12.0, 5.0, 20.0], e=None, w=None,
+               offsets=[0.0, 30.0], jitters=[1.0, 3.0], ma=None,
+               gp=dict(rho=25.0, tau=50.0, A1=4.0, A2=1.5), setup=[10, 256, 2000, 1]),
 }
+
+
+def _sho_cov(tau, S0, w0, Q):
+    """Stochastically driven damped oscillator covariance for Q > 1/2
+    (Foreman-Mackey et al. 2017, eq. 20 with eta = sqrt(1 - 1/(4 Q^2)))."""
+    eta = np.sqrt(1.0 - 1.0 / (4.0 * Q * Q))
+    x = w0 * np.abs(tau)
+    return S0 * w0 * Q * np.exp(-x / (2 * Q)) * (np.cos(eta * x) + np.sin(eta * x) / (2 * eta * Q))
+
+
+def rotation_gp_noise(rng, t, gp):
+    """A draw of the GonzRotationTerm GP (SHO(S0=A1, rho, tau) + SHO(S0=A2,
+    rho/2, tau)) at times t, by a dense Cholesky factor."""
+    tau = t[:, None] - t[None, :]
+    K = np.zeros_like(tau)
+    for S0, rho in ((gp['A1'], gp['rho']), (gp['A2'], 0.5 * gp['rho'])):
+        w0 = 2 * np.pi / rho
+        K += _sho_cov(tau, S0, w0, 0.5 * w0 * gp['tau'])
+    K[np.diag_indices_from(K)] += 1e-9 * K[0, 0]
+    return np.linalg.cholesky(K) @ rng.normal(size=len(t))
 
 
 def make_system(name: str, seed: int = 1234):
@@ -106,6 +133,11 @@ def make_system(name: str, seed: int = 1234):
     rv = np.zeros(n)
     for p in range(kp):
         rv += keplerian(tr, cfg['P'][p], cfg['K'][p], phase[p], e[p], w[p])
+    if cfg.get('gp'):
+        order = np.argsort(tr, kind='mergesort')
+        g = np.empty(n)
+        g[order] = rotation_gp_noise(rng, tr[order], cfg['gp'])
+        rv += g
     sig = rng.uniform(1.5, 3.0, n)
     instruments = []
     for k in range(nins):
@@ -119,7 +151,7 @@ def make_system(name: str, seed: int = 1234):
         yk = rv[m] + cfg['offsets'][k] + noise
         instruments.append(np.column_stack([tk, yk, sig[m]]))
     truth = dict(P=cfg['P'], K=cfg['K'], phase=phase, e=e, w=w, offsets=cfg['offsets'],
-                 jitters=cfg['jitters'], ma=cfg['ma'])
+                 jitters=cfg['jitters'], ma=cfg['ma'], gp=cfg.get('gp'))
     return instruments, truth
 
 
@@ -161,6 +193,14 @@ def build_model(name: str, seed: int = 1234, parameterisation: int = 1,
             elif p.name.startswith('MATimescale'):
                 p.limits = [1.0, 50.0]
         blocks.append(mb)
+    if cfg.get('gp'):
+        gb = CeleriteBlock({'terms': ['GonzRotationTerm'],
+                            'params': [{'rho': None, 'tau': None, 'A1': None, 'A2': None}]})
+        ss(gb)
+        # search boxes around the rotation signal, as a user's conditions set them
+        for p, lim in zip(gb, ([10.0, 40.0], [10.0, 100.0], [1e-5, 20.0], [1e-5, 20.0])):
+            p.limits = lim
+        blocks.append(gb)
     model = ReddModel(blocks, data, moav_reference_quirk=moav_reference_quirk)
     theta = truth_theta(model, truth, data, parameterisation)
     return model, data, list(cfg['setup']), theta
@@ -188,6 +228,9 @@ def truth_theta(model, truth, data, parameterisation=1):
             for k in range(len(b) // (2 * b.moav)):
                 for c in range(b.moav):
                     vals += [truth['ma']['phi'][c], truth['ma']['tau'][c]]
+        elif b.type_ == 'Celerite2':
+            g = truth['gp']
+            vals += [g['rho'], g['tau'], g['A1'], g['A2']]
     return np.array(vals, dtype=np.float64)
 
 

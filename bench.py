@@ -40,6 +40,8 @@ WORKLOADS = {
     'c5': 'RV PT sweep: 7 Keplerians, 4 instruments, N=16384, per-instrument MA(2)',
     'c3': 'RV PT sweep of a ragged batch: 4096 independent systems, N log-uniform in [50, 2000], '
           '1-4 Keplerians, 1-3 instruments',
+    'gp': 'RV PT sweep with a celerite GP likelihood: 3 Keplerians, 2 instruments, N=1024, '
+          'GonzRotationTerm GP (4 hyperparameters)',
 }
 SEED = 1234
 
@@ -503,15 +505,16 @@ def main():
     # (T*W/2 walkers x N epochs), launches captured in a CUDA graph and timed
     # with events on their stream
     th_half = torch.as_tensor(p0.reshape(-1, D)[: T * W // 2], dtype=torch.float64, device=dev)
-    ll = torch.empty(th_half.shape[0], dtype=torch.float64, device=dev)
+    B = th_half.shape[0]
+    ll = torch.empty(B, dtype=torch.float64, device=dev)
     lp = torch.empty_like(ll)
     rs = torch.cuda.Stream(device=dev)
     from astroemperor_gb300.autotune import graph_time
-    k_ms = graph_time((ctx.h, th_half.data_ptr(), th_half.shape[0], None, None, ll.data_ptr(),
+    k_ms = graph_time((ctx.h, th_half.data_ptr(), B, None, None, ll.data_ptr(),
                        lp.data_ptr(), None, N.EMP_PREC_MIXED, rs.cuda_stream), 50, rs)
     kp, q = model.kplan__, ma_order(model)
     F = 58 * kp + 10 + 7 * q                                   # FLOP per eval*epoch
-    flops_launch = F * (T * W // 2) * n
+    flops_launch = F * B * n
     import ctypes as C
     f32, f64p = C.c_double(), C.c_double()
     N.call('emp_probe_peaks', C.byref(f32), C.byref(f64p), rs.cuda_stream)
@@ -520,13 +523,38 @@ def main():
     roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s',
             'frac': achieved / peak32, 'traffic': NCU_TRAFFIC.get(args.config),
             'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch',
-            'algorithmic_bytes': n * 25 + (T * W // 2) * (8 * D + 16),
-            'kernel': 'k_logpost<MIXED,Q=1> (stretch half-step shape)',
+            'algorithmic_bytes': n * 25 + B * (8 * D + 16),
+            'kernel': f'k_logpost<MIXED,Q={q}> (stretch half-step shape)',
             'kernel_ms': k_ms, 'flop_per_eval_epoch': F,
             'launch': {'lanes': s_mixed.launch[0], 'tile': s_mixed.launch[1]} if s_mixed.launch else None,
             'peak_source': 'measured on this GPU by the library FMA probe (MEASURED_PEAKS.json '
                            'has no CUDA-core figure); compute-issue bound, not HBM or tensor',
             'fp64_peak_tflops': f64p.value / 1e12}
+    if any(b.type_ == 'Celerite2' for b in model.blocks):
+        # the GP sweep's dominant kernel is k_gp (FP64 recursion, one thread
+        # per walker row): timed alone through emp_gp_logl on the half-step's
+        # rows and their residuals; the mixed k_logpost that writes those
+        # residuals is reported beside it
+        mod, e2 = ctx.model_eval(th_half)
+        y = torch.as_tensor(data.RV, dtype=torch.float64, device=dev)
+        rr = (y[None, :] - mod).t().contiguous()
+        ee = e2.t().contiguous()
+        gl = torch.empty(B, dtype=torch.float64, device=dev)
+        g_ms = graph_time((ctx.h, th_half.data_ptr(), B, rr.data_ptr(), ee.data_ptr(), gl.data_ptr(),
+                           rs.cuda_stream), 50, rs, entry='emp_gp_logl')
+        Mg = 4                                                  # state dimensions of the kernel
+        Fg = 4.5 * Mg * Mg + 16.5 * Mg + 8                      # FLOP per row*epoch
+        ach = Fg * B * n / (g_ms * 1e-3) / 1e12
+        p64 = f64p.value / 1e12
+        roof = {'bound': 'fp64', 'achieved': ach, 'peak': p64, 'unit': 'TFLOP/s', 'frac': ach / p64,
+                'traffic': NCU_TRAFFIC.get(args.config),
+                'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch',
+                'algorithmic_bytes': B * (16 * n + 8 * D + 8) + 8 * n,
+                'kernel': 'k_gp<4> (celerite recursion, half-step rows)', 'kernel_ms': g_ms,
+                'flop_per_row_epoch': Fg,
+                'peak_source': 'FP64 peak measured on this GPU by the library FMA probe',
+                'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp)',
+                              'kernel_ms_with_k_gp': k_ms, 'launch': roof['launch']}}
 
     # ---- end to end through the public sampler with host buffers
     s = s_mixed

@@ -7,7 +7,9 @@ over ``multiprocessing.Pool(ncores)`` (``support/pools/01.pool:10-12``,
 ``emp.py:503-517``).  This module does the same with the oracle's
 restatement; the per-instrument moving-average block runs the reference's
 literal loop (``support/models/moav00.model``), whose writes are discarded,
-so the timed work equals the reference's.  The pool is started with the
+so the timed work equals the reference's.  A celerite GP likelihood runs the
+compiled recursion of ``gp_semisep.c`` (the reference calls celerite2's
+compiled core there).  The pool is started with the
 ``spawn`` method so that it is safe to create after CUDA is initialised.
 
 Caveat: the Kepler equation is solved by the oracle's vectorised numpy
@@ -25,6 +27,9 @@ from . import rv
 
 
 def _init(spec, data):
+    if any(b['type'] == 'Celerite2' for b in spec['blocks']):
+        from . import gp
+        gp.use_compiled(True)
     rv.install_global(spec, data)
 
 

@@ -17,10 +17,67 @@ factor) and ``semisep_loglike`` (the O(N J^2) recursion of Foreman-Mackey,
 Agol, Ambikasaran & Angus 2017, AJ 154, 220, which the device implements).
 Parity with celerite2 itself is unpinned: neither the library nor outputs
 of it are available.
+
+``gp_semisep.c`` states the recursion in C (compiled here with gcc on first
+use); ``use_compiled(True)`` routes ``semisep_loglike`` through it, which the
+CPU baseline does so that a host evaluation costs what celerite2's compiled
+core costs.  The tests check the two against each other.
 """
 from __future__ import annotations
 
+import ctypes
+import os
+import subprocess
+
 import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, 'gp_semisep.c')
+_LIB = os.path.join(_HERE, '_build', 'libgp_oracle.so')
+_c = None
+_use_c = False
+
+
+def build_c():
+    """Compile gp_semisep.c into oracle/_build (skipped when up to date)."""
+    if os.path.exists(_LIB) and os.path.getmtime(_LIB) >= os.path.getmtime(_SRC):
+        return _LIB
+    os.makedirs(os.path.dirname(_LIB), exist_ok=True)
+    tmp = _LIB + f'.{os.getpid()}.tmp'
+    subprocess.run(['gcc', '-O2', '-shared', '-fPIC', '-o', tmp, _SRC, '-lm'], check=True)
+    os.replace(tmp, _LIB)
+    return _LIB
+
+
+def _load_c():
+    global _c
+    if _c is None:
+        lib = ctypes.CDLL(build_c())
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.emp_oracle_gp_loglike.restype = ctypes.c_double
+        lib.emp_oracle_gp_loglike.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_int, dp, dp,
+                                              ctypes.c_int, dp, dp, dp, dp]
+        _c = lib
+    return _c
+
+
+def use_compiled(flag=True):
+    """Route semisep_loglike through the compiled recursion (or back)."""
+    global _use_c
+    if flag:
+        _load_c()
+    _use_c = bool(flag)
+
+
+def semisep_loglike_c(t, r, diag, coeffs):
+    """semisep_loglike through gp_semisep.c."""
+    lib = _load_c()
+    ar, cr, a, b, c, d = (np.ascontiguousarray(x, dtype=np.float64) for x in coeffs)
+    t, r, diag = (np.ascontiguousarray(x, dtype=np.float64) for x in (t, r, diag))
+    dp = ctypes.POINTER(ctypes.c_double)
+    P = lambda x: x.ctypes.data_as(dp)
+    return float(lib.emp_oracle_gp_loglike(len(t), P(t), P(r), P(diag), len(ar), P(ar), P(cr),
+                                           len(a), P(a), P(b), P(c), P(d)))
 
 # term kinds of the compiled descriptor (include/emp_gpu.h, EMP_GP_*)
 GP_REAL, GP_MATERN32, GP_ROTATION, GP_GROT = 1, 2, 3, 4
@@ -137,6 +194,8 @@ def semisep_loglike(t, r, diag, coeffs):
       D_n = A_n - U_n^T S_n U_n,  W_n = (V_n - S_n U_n) / D_n,
       f_n = phi_n (f_{n-1} + W_{n-1} z_{n-1}),  z_n = r_n - U_n^T f_n,
     logL = -0.5 sum(z_n^2 / D_n + log D_n) - 0.5 N log 2 pi."""
+    if _use_c:
+        return semisep_loglike_c(t, r, diag, coeffs)
     ar, cr, a, b, c, d = (np.asarray(x, dtype=np.float64) for x in coeffs)
     A = np.concatenate([ar, a])
     Bc = np.concatenate([np.zeros_like(ar), b])

@@ -141,3 +141,18 @@ def test_simulation_block_order(peg_arr):
     sim._autorun_add_RV_ins()
     # emp.py:2628-2650: offset, jitter, celerite, sinusoid
     assert [b.type_ for b in sim.blocks__] == ['Offset', 'Jitter', 'Celerite2', 'Sinusoid']
+
+
+@pytest.mark.parametrize('kind,p', TERM_CASES[:5])
+def test_compiled_recursion_equals_python(kind, p):
+    rng = np.random.default_rng(kind + 100)
+    t, r, diag = _series(rng, 150)
+    co = gp.coefficients([(kind, p), (gp.GP_REAL, [0.7, 0.02])])
+    a = gp.semisep_loglike(t, r, diag, co)
+    b = gp.semisep_loglike_c(t, r, diag, co)
+    assert abs(a - b) <= 1e-12 * abs(a), (a, b)
+    # not positive definite -> -inf in both
+    bad = [x.copy() if hasattr(x, 'copy') else list(x) for x in co]
+    bad[0] = [-50.0] + list(bad[0])[1:]
+    assert gp.semisep_loglike(t, r, diag, bad) == -np.inf
+    assert gp.semisep_loglike_c(t, r, diag, bad) == -np.inf

@@ -145,3 +145,35 @@ def test_gp_pt_graph_equals_eager_and_state_consistent(peg_arr, lib, cuda, preci
             ref = o.my_likelihood(x)
             assert abs(ll[t, -1, w] - ref) <= tol * abs(ref), (t, w, ll[t, -1, w], ref)
     assert np.all(np.isfinite(ll[:, -1]))
+
+
+def test_gp_logl_of_given_residuals(cases):
+    """emp_gp_logl on residuals from emp_model_eval equals the GP part of the
+    log-posterior entry (FP64) at every theta inside the prior."""
+    for name in ('grot', 'real_matern'):
+        m, th, klp, kll, ctx = cases[name]
+        fin = np.isfinite(klp)
+        t = torch.as_tensor(th[fin], dtype=torch.float64, device='cuda:0')
+        model, err2 = ctx.model_eval(t)
+        y = torch.as_tensor(m.data.RV, dtype=torch.float64, device="cuda:0")
+        ll = ctx.gp_logl(t, y[None, :] - model, err2).cpu().numpy()
+        ref, _ = _eval(ctx, th[fin], N.EMP_PREC_FP64)
+        np.testing.assert_allclose(ll, ref, rtol=1e-12, err_msg=name)
+        np.testing.assert_allclose(ll, kll[fin], rtol=FP64_RTOL, err_msg=name)
+
+
+def test_gp_unsupported_paths(peg_arr, lib, cuda):
+    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'])
+    ctx = Context(m, 'cuda:0')
+    t = torch.as_tensor(np.tile(m.limits_free().mean(axis=1), (2, 1)), dtype=torch.float64, device='cuda:0')
+    with pytest.raises(N.EmpError, match='GP'):
+        ctx.logpost_grad(t)
+    m0, _ = model_51peg(peg_arr, k=1, par=1)
+    ctx0 = Context(m0, 'cuda:0')
+    t0 = torch.as_tensor(np.tile(m0.limits_free().mean(axis=1), (2, 1)), dtype=torch.float64, device='cuda:0')
+    r = torch.zeros(2, m0.data.ndata, dtype=torch.float64, device='cuda:0')
+    with pytest.raises(N.EmpError, match='no GP'):
+        ctx0.gp_logl(t0, r, r + 1.0)
+    from astroemperor_gb300.batch import BatchContext
+    with pytest.raises(N.EmpError, match='one-system'):
+        BatchContext([m, m], 'cuda:0')
