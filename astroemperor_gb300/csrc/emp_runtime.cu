@@ -121,8 +121,10 @@ struct emp_handle {
 
 // dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
 static const size_t kSwapSmemMax = 200 * 1024;
-// threads per CTA of the GP recursion (M lanes per walker row)
-static const int kGPBlock = 128;
+// threads per CTA of the GP recursion (M lanes per walker row): one warp,
+// so that the recursion's warps spread over the SMs (measured 5 % faster
+// than four warps per CTA for 1280 rows; FP64 issue is per SM sub-partition)
+static const int kGPBlock = 32;
 
 namespace {
 

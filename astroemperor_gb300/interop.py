@@ -12,8 +12,8 @@ from __future__ import annotations
 import numpy as np
 
 from .data import RVData
-from .model import (AccelerationBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock, MOAVBlock,
-                    OffsetBlock, Parameter, ReddModel, SinusoidBlock)
+from .model import (AccelerationBlock, CeleriteBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock,
+                    MOAVBlock, OffsetBlock, Parameter, ReddModel, SinusoidBlock)
 
 
 def data_from_frame(df, labels=None, common_t=0.0) -> RVData:
@@ -42,8 +42,12 @@ def _copy_params(src_block, dst_block):
     return dst_block
 
 
-def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False) -> ReddModel:
-    """ReddModel from the reference's block list (emp_model.py:32-170 objects)."""
+def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False, my_kernel=None) -> ReddModel:
+    """ReddModel from the reference's block list (emp_model.py:32-170 objects).
+
+    A 'Celerite2' block needs the Simulation's ``my_kernel`` (the reference's
+    block does not keep it; emp.py:1283-1296 builds it from ``self.my_kernel``).
+    """
     out = []
     for b in blocks:
         t = b.type_
@@ -71,6 +75,10 @@ def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False) -> ReddM
             nb = SinusoidBlock(int(b.number_))
         elif t == 'MagneticCycle':
             nb = MagneticCycleBlock(int(b.number_))
+        elif t == 'Celerite2':
+            if my_kernel is None:
+                raise ValueError('a Celerite2 block needs my_kernel (Simulation.my_kernel)')
+            nb = CeleriteBlock(my_kernel)
         else:
             raise ValueError(f'block type {t!r} is not on the GPU hot path')
         out.append(_copy_params(b, nb))

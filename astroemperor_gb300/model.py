@@ -208,6 +208,12 @@ def MagneticCycleBlock(number: int) -> Parameter_Block:
 _GP_NAMES = {'RealTerm': 'Real Term', 'Matern32Term': 'Matern32 Term', 'RotationTerm': 'Rotation Term',
              'SHOTerm': 'SHO Term', 'GonzRotationTerm': 'GRot Term'}
 GP_TERMS = tuple(_GP_NAMES)
+# terms whose parameters the reference names in a fixed order (block_repo.py:358-370)
+# while its kernel text passes the values by the params dictionary's order
+# (emp.py:352-366): the i-th parameter takes the i-th name below and the i-th
+# dictionary keyword
+_GP_FIXED_NAMES = {'RealTerm': ('a', 'c'), 'Matern32Term': ('sigma', 'rho'),
+                   'RotationTerm': ('period', 'sigma', 'Q0', 'dQ', 'f')}
 
 
 def CeleriteBlock(my_kernel: dict) -> Parameter_Block:
@@ -230,8 +236,13 @@ def CeleriteBlock(my_kernel: dict) -> Parameter_Block:
             raise ValueError(f'GP term {term!r} is not built ({", ".join(GP_TERMS)})')
         if term == 'GonzRotationTerm':
             pd = {k: pd.get(k) for k in ('rho', 'tau', 'A1', 'A2')}
-        for k, v in pd.items():
-            p = Parameter(f'{_GP_NAMES[term]} {k}' + (str(t + 1) if len(terms) > 1 else ''))
+        names = list(pd)
+        if term in _GP_FIXED_NAMES:
+            names = list(_GP_FIXED_NAMES[term])
+            if sorted(names) != sorted(pd):
+                raise ValueError(f'{term} takes {names}, got {list(pd)}')
+        for nm, (k, v) in zip(names, pd.items()):
+            p = Parameter(f'{_GP_NAMES[term]} {nm}' + (str(t + 1) if len(terms) > 1 else ''))
             p.gp_term, p.gp_key = t, k
             if v is not None:
                 p.fixed = float(v)

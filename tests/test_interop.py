@@ -44,3 +44,26 @@ def test_model_from_reference_blocks(peg_arr):
     o = OracleRV(m2.spec(), d2.as_dict())
     th = np.array([4.231, 55.957, 1.769, 0.087, 0.061, 3.642, 2.961, 0.1, 10.0])
     assert np.isfinite(o.my_prior(th)) and np.isfinite(o.my_likelihood(th))
+
+
+def test_model_with_gp_from_reference_blocks(peg_arr):
+    from tests.golden.cases import GP_KERNELS
+    ker = GP_KERNELS['real_matern']
+    m, d = model_51peg(peg_arr, k=1, par=1, gp=ker)
+    frame = {'BJD': d.BJD, 'RV': d.RV, 'eRV': d.eRV, 'Flag': d.Flag}
+    d2 = data_from_frame(frame, common_t=d.common_t)
+    m2 = model_from_blocks([_ref_like(b) for b in m.blocks], d2, my_kernel=ker)
+    assert bytes(m.descriptor()) == bytes(m2.descriptor())
+    import pytest
+    with pytest.raises(ValueError, match='my_kernel'):
+        model_from_blocks([_ref_like(b) for b in m.blocks], d2)
+
+
+def test_rotation_term_names_follow_the_reference():
+    # names in the reference's fixed order, values by the dictionary's order
+    from astroemperor_gb300.model import CeleriteBlock
+    b = CeleriteBlock({'terms': ['RotationTerm'],
+                       'params': [{'sigma': None, 'period': None, 'Q0': None, 'dQ': None, 'f': None}]})
+    assert [p.name for p in b] == ['Rotation Term period', 'Rotation Term sigma', 'Rotation Term Q0',
+                                   'Rotation Term dQ', 'Rotation Term f']
+    assert [p.gp_key for p in b] == ['sigma', 'period', 'Q0', 'dQ', 'f']
