@@ -12,7 +12,7 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, '_lib', 'libemp_gpu.so')
 
-EMP_ABI_VERSION = 2
+EMP_ABI_VERSION = 3
 EMP_MAX_PARAMS = 160
 EMP_MAX_PLANETS = 16
 EMP_MAX_INS = 16
@@ -70,6 +70,7 @@ class EmpModelDesc(C.Structure):
         ('gp_nterms', C.c_int32), ('_pad2', C.c_int32),
         ('gp_kind', C.c_int32 * EMP_MAX_GP_TERMS),
         ('gp_slot', (C.c_int32 * 5) * EMP_MAX_GP_TERMS),
+        ('hill_mask', C.c_int32), ('_pad3', C.c_int32), ('hill_starmass', C.c_double),
     ]
 
 

@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
     __syncthreads();
     if (active && r == 0) {
         double lp = -INFINITY;
-        if (flag[0] == 0) {
+        if (flag[0] == 0 && (md->hill_mask == 0 || hill_stable(md, full))) {
             lp = md->prior_const;
             for (int i = 0; i < md->n_prior_var; ++i) lp += pterm[md->prior_var[i]];
         }

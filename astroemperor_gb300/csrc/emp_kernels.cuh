@@ -57,6 +57,62 @@ __device__ __forceinline__ double derived_x(const double* th, int k) {
     return k == 0 ? th[3] * th[3] + th[4] * th[4] : th[1] * th[1] + th[2] * th[2];
 }
 
+// Hill stability priors (FP64, one thread).  The reference gives every
+// Keplerian block after the first its own Hill prior over the planets up to
+// and including it (block_repo.py:611-626 runs per block; the flag that would
+// stop the repetition is only set in a local copy), so the prior is -inf
+// unless, for every j in md->hill_mask, the first j Keplerians pass
+// support/priors/Hill.prior: ordered by semi-major axis, each adjacent pair
+// needs LHS > RHS.  Semi-major axes and minimum masses follow math_utils.py:31-61
+// (cps); (P, K, e) are read per parameterisation as support/PAE/0*.pae reads
+// them.  As in the reference, gamma = sqrt(1 - e) keeps the planets' own
+// order while the masses and axes are sorted.
+__device__ inline bool hill_stable(const emp_model_desc* md, const double* full) {
+    const int mask = md->hill_mask;
+    int K = 0;
+    for (int j = 2; j <= EMP_MAX_PLANETS; ++j)
+        if (mask & (1 << j)) K = j;
+    const double Ms = md->hill_starmass;
+    const double kPi = 3.141592653589793;
+    double sma[EMP_MAX_PLANETS], mm[EMP_MAX_PLANETS], gam[EMP_MAX_PLANETS];
+    for (int p = 0; p < K; ++p) {
+        const double* v = full + md->kep_slot[p];
+        const int par = md->kep_param[p];
+        double P = v[0], Kp = v[1];
+        if (par == 2 || par == 6) P = exp(v[0]);
+        if (par == 2) Kp = v[1] * v[1] + v[2] * v[2];
+        const double e = (par == 0 || par == 3 || par == 6) ? v[3] : v[3] * v[3] + v[4] * v[4];
+        const double Ps = P * 86400.0;
+        const double a = pow(6.6743e-11 * (Ms * 1.98847e30) * (Ps * Ps) / (4.0 * (kPi * kPi)), 1.0 / 3.0) /
+                         1.495978707e11;
+        sma[p] = a;
+        mm[p] = (Kp / 28.4329) * sqrt(1.0 - e * e) * sqrt(Ms * a);
+        gam[p] = sqrt(1.0 - e);
+    }
+    for (int j = 2; j <= K; ++j) {
+        if (!(mask & (1 << j))) continue;
+        int idx[EMP_MAX_PLANETS];
+        for (int p = 0; p < j; ++p) idx[p] = p;
+        for (int i = 1; i < j; ++i)                      // order by semi-major axis
+            for (int q = i; q > 0 && sma[idx[q]] < sma[idx[q - 1]]; --q) {
+                const int t = idx[q]; idx[q] = idx[q - 1]; idx[q - 1] = t;
+            }
+        double Mt = 0.0;
+        for (int p = 0; p < j; ++p) Mt += mm[idx[p]];
+        Mt = Ms * 1047.56 + Mt;
+        for (int i = 0; i + 1 < j; ++i) {
+            const double m0 = mm[idx[i]] / Mt, m1 = mm[idx[i + 1]] / Mt;
+            const double alpha = m0 + m1;
+            const double delta = sqrt(sma[idx[i + 1]] / sma[idx[i]]);
+            const double s = m0 * gam[i] + m1 * gam[i + 1] * delta;
+            const double lhs = pow(alpha, -3.0) * (m0 + m1 / (delta * delta)) * (s * s);
+            const double rhs = 1.0 + pow(3.0 / alpha, 4.0 / 3.0) * (m0 * m1);
+            if (!(lhs > rhs)) return false;
+        }
+    }
+    return true;
+}
+
 // ----------------------------------------------------------------------------
 // float-float helpers (mixed precision phase)
 // ----------------------------------------------------------------------------
@@ -884,7 +940,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     __syncthreads();
     if (active && r == 0) {
         double lp = -INFINITY;
-        if (flag[0] == 0) {
+        if (flag[0] == 0 && (md->hill_mask == 0 || hill_stable(md, full))) {
             lp = md->prior_const;
             const int nv = md->n_prior_var;
             for (int i = 0; i < nv; ++i) lp += pterm[md->prior_var[i]];

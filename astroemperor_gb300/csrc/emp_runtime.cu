@@ -190,6 +190,24 @@ int validate_model(const emp_model_desc* m) {
         if ((rc = chk(m->ma_slot, cnt, "MA"))) return rc;
     }
     if (m->acc_order > 0 && m->acc_slot < 0) return fail(EMP_E_INVALID, "acceleration without slot");
+    if (m->hill_mask != 0) {
+        if (m->hill_mask & ~(int)(((1u << (EMP_MAX_PLANETS + 1)) - 1u) & ~3u))
+            return fail(EMP_E_INVALID, "hill_mask 0x%x names planet counts outside 2..%d", m->hill_mask,
+                        EMP_MAX_PLANETS);
+        int top = 0;
+        for (int j = 2; j <= EMP_MAX_PLANETS; ++j)
+            if (m->hill_mask & (1 << j)) top = j;
+        if (top > m->n_planets)
+            return fail(EMP_E_INVALID, "Hill prior over %d Keplerians, the model has %d terms", top, m->n_planets);
+        if (!(m->hill_starmass > 0))
+            return fail(EMP_E_INVALID, "Hill prior: star mass %g must be > 0", m->hill_starmass);
+        for (int p = 0; p < top; ++p) {
+            const int par = m->kep_param[p];
+            if (!(par == 0 || par == 1 || par == 2 || par == 3 || par == 4 || par == 6))
+                return fail(EMP_E_UNSUPPORTED, "Hill prior: term %d has parameterisation %d (0-4, 6 read "
+                            "as the reference reads them)", p, par);
+        }
+    }
     if (m->gp_nterms < 0 || m->gp_nterms > EMP_MAX_GP_TERMS)
         return fail(EMP_E_SIZE, "gp_nterms=%d outside [0, %d]", m->gp_nterms, EMP_MAX_GP_TERMS);
     if (m->gp_nterms > 0) {

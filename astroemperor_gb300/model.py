@@ -263,7 +263,8 @@ class SmartSetter:
         per = float(self.data.BJD.max() - self.data.BJD.min())
         return sig * np.sqrt(4), per
 
-    def set_Keplerian(self, b, ecc_limits=(0, 1), ecc_prargs=(0, 0.1)):
+    def set_Keplerian(self, b, ecc_limits=(0, 1), ecc_prargs=(0, 0.1), starmass=None, dynamics=False,
+                      kplan=None, dynamics_already_included=False):
         amp, per = self._amp_per()
         uni = 'Uniform'
         par = b.parameterisation
@@ -312,6 +313,12 @@ class SmartSetter:
                 if b.number_:
                     ap.name += f' {b.number_}'
             b.additional_parameters = [e, w]
+        kplan = b.number_ if kplan is None else kplan
+        if starmass and dynamics and not dynamics_already_included and kplan > 1:
+            # block_repo.py:611-626: a Hill prior over the first kplan planets
+            b.additional_parameters = list(b.additional_parameters) + [
+                Parameter('Hill', prior='Hill', limits=[None, None], prargs=[int(kplan), float(starmass)],
+                          has_prior=True, has_posterior=False)]
         return lims, priors, prargs
 
     def _per_ins_absmax(self, b):
@@ -523,7 +530,16 @@ class ReddModel:
                 for ap in b.additional_parameters:
                     if not getattr(ap, 'has_prior', False):
                         continue
-                    if ap.name[:3] == 'Ecc':
+                    if ap.name == 'Hill':
+                        j = int(ap.prargs[0])
+                        if j > 1:                             # emp.py:222
+                            if j > N.EMP_MAX_PLANETS:
+                                raise ValueError(f'Hill prior over {j} planets')
+                            if md.hill_mask and md.hill_starmass != float(ap.prargs[1]):
+                                raise ValueError('Hill priors with different star masses')
+                            md.hill_mask |= 1 << j
+                            md.hill_starmass = float(ap.prargs[1])
+                    elif ap.name[:3] == 'Ecc':
                         md.derived[planet][0] = prior_struct(ap.prior, ap.limits, ap.prargs)
                     elif ap.name[:3] == 'Amp':
                         md.derived[planet][1] = prior_struct(ap.prior, ap.limits, ap.prargs)

@@ -56,6 +56,8 @@ class Simulation:
         self.jitter_prargs = [5, 5]
         self.instrument_names_RV = None
         self.starmass = 1.
+        self.switch_dynamics = False
+        self.dynamics_already_included = False
         self.cores__ = 1
         self.engine__ = None
         self.engine_config = {}
@@ -116,7 +118,9 @@ class Simulation:
         """emp.py:1212-1236; Keplerian blocks go in front of the data blocks."""
         self.kplanets__ += 1
         kb = KeplerianBlock(self.keplerian_parameterisation, self.kplanets__)
-        self.SmartSetter(kb, ecc_limits=self.eccentricity_limits, ecc_prargs=self.eccentricity_prargs)
+        self.SmartSetter(kb, ecc_limits=self.eccentricity_limits, ecc_prargs=self.eccentricity_prargs,
+                         starmass=self.starmass, dynamics=self.switch_dynamics, kplan=self.kplanets__,
+                         dynamics_already_included=self.dynamics_already_included)
         self.blocks__.insert(self.kplanets__ - 1, kb)
 
     def add_offset(self):

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define EMP_ABI_VERSION 2
+#define EMP_ABI_VERSION 3
 
 #define EMP_MAX_PARAMS   160   /* full theta length incl. fixed parameters */
 #define EMP_MAX_PLANETS  16
@@ -136,6 +136,17 @@ typedef struct emp_model_desc {
     int32_t _pad2;
     int32_t gp_kind[EMP_MAX_GP_TERMS];
     int32_t gp_slot[EMP_MAX_GP_TERMS][5];
+    /* Hill stability priors (support/priors/Hill.prior, emp.py:222-227,
+       block_repo.py:611-626): for every bit j (2 <= j <= EMP_MAX_PLANETS)
+       set in hill_mask the prior is -inf unless each adjacent pair of the
+       first j Keplerians, ordered by semi-major axis, passes the Hill
+       criterion for a star of hill_starmass solar masses (the reference
+       attaches one such prior to Keplerian block j for j = 2, 3, ...);
+       periods, amplitudes and eccentricities are read as
+       support/PAE/0<parameterisation>.pae reads them (0, 1, 2, 3, 4, 6) */
+    int32_t hill_mask;
+    int32_t _pad3;
+    double  hill_starmass;
 } emp_model_desc;
 
 /*

@@ -182,6 +182,58 @@ PRIORS = {'Uniform': prior_Uniform, 'Normal': prior_Normal,
           'Jeffreys': prior_Jeffreys, 'Beta': prior_Beta, 'Fixed': prior_Fixed}
 
 
+def cps(pers, amps, eccs, starmass):
+    """math_utils.py:31-61: semi-major axes (AU, Kepler's third law without
+    the planet mass) and minimum masses (M_Jup) from P [d], K [m/s], e."""
+    G, M_sun, AU, day = 6.6743e-11, 1.98847e30, 1.495978707e11, 86400.0
+    P = np.asarray(pers, dtype=float) * day
+    K = np.asarray(amps, dtype=float)
+    e = np.asarray(eccs, dtype=float)
+    a_m = (G * (starmass * M_sun) * P ** 2 / (4.0 * np.pi ** 2)) ** (1.0 / 3.0)
+    sma = a_m / AU
+    minmass = (K / 28.4329) * np.sqrt(1.0 - e ** 2) * np.sqrt(starmass * sma)
+    return sma, minmass
+
+
+def prior_Hill(x, limits, args):
+    """support/priors/Hill.prior: 0 when every adjacent pair ordered by
+    semi-major axis passes LHS > RHS, else -inf.  As in the reference, gamma
+    keeps the input order while the axes and masses are sorted."""
+    kplanets, starmass = args[0], args[1]
+    periods, amps, eccs = x
+    with np.errstate(invalid='ignore', divide='ignore'):
+        gamma = np.sqrt(1 - eccs)
+        sma, minmass = cps(periods, amps, eccs, starmass)
+        orden = np.argsort(sma)
+        sma, minmass = sma[orden], minmass[orden]
+        M = starmass * 1047.56 + np.sum(minmass)
+        mu = minmass / M
+        for k in range(int(kplanets) - 1):
+            alpha = mu[k] + mu[k + 1]
+            delta = np.sqrt(sma[k + 1] / sma[k])
+            LHS = alpha ** -3 * (mu[k] + (mu[k + 1] / (delta ** 2))) * \
+                (mu[k] * gamma[k] + mu[k + 1] * gamma[k + 1] * delta) ** 2
+            RHS = 1 + (3. / alpha) ** (4. / 3) * (mu[k] * mu[k + 1])
+            if not LHS > RHS:
+                return -np.inf
+    return 0.
+
+
+def hill_x(par, theta, b_len, kplanets):
+    """support/PAE/0<par>.pae: (periods, amps, eccs) of the first kplanets
+    Keplerian blocks, read from the full theta with stride b_len."""
+    s = lambda i: theta[slice(i, b_len * kplanets, b_len)]
+    if par in (0, 3):
+        return np.array([s(0), s(1), s(3)])
+    if par in (1, 4):
+        return np.array([s(0), s(1), s(3) ** 2 + s(4) ** 2])
+    if par == 2:
+        return np.array([np.exp(s(0)), s(1) ** 2 + s(2) ** 2, s(3) ** 2 + s(4) ** 2])
+    if par == 6:
+        return np.array([np.exp(s(0)), s(1), s(3)])
+    raise ValueError(f'no PAE script for parameterisation {par}')
+
+
 # --------------------------------------------------------------------------
 # the per-theta functions
 # --------------------------------------------------------------------------
@@ -299,6 +351,9 @@ class OracleRV:
             extra = []
             for ap in b.get('additional', []):
                 if not ap.get('has_prior'):
+                    continue
+                if ap['name'] == 'Hill':                 # emp.py:222-227
+                    extra.append(('Hill', prior_Hill, list(ap['limits']), list(ap['prargs'])))
                     continue
                 args = check_prargs(ap['prior'], ap['limits'], ap.get('prargs'))
                 kind = ap['name'][:3]
@@ -453,6 +508,8 @@ class OracleRV:
                     x = theta[sl][1] ** 2 + theta[sl][2] ** 2
                 elif kind == 'Ecc':
                     x = theta[sl][3] ** 2 + theta[sl][4] ** 2
+                elif kind == 'Hill' and args[0] > 1:
+                    x = hill_x(b['parameterisation'], theta, len(b['params']), int(args[0]))
                 else:
                     continue
                 lp += fn(x, limits, args)

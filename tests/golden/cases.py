@@ -24,16 +24,19 @@ def peg_data(arr):
     return preprocess_instruments([arr], ['51peg.vels'])
 
 
-def _kep(ss, par, number, **lims):
+def _kep(ss, par, number, starmass=None, **lims):
     kb = KeplerianBlock(par, number)
-    ss(kb)
+    if starmass:
+        ss(kb, starmass=starmass, dynamics=True, kplan=number)
+    else:
+        ss(kb)
     for i, lim in lims.items():
         kb[int(i[1:])].limits = list(lim)
     return kb
 
 
 def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=None, quirk=False,
-                sinusoid=False, cycle=False, gp=None):
+                sinusoid=False, cycle=False, gp=None, hill=None):
     data = peg_data(arr)
     ss = SmartSetter(data)
     blocks = []
@@ -53,6 +56,20 @@ def model_51peg(arr, k=1, par=1, conditions=True, fixed_ecc=False, acc=0, moav=N
             kb[3].fixed = 0.0
             kb[4].fixed = 0.0
         blocks.append(kb)
+    # further Keplerians (inner pairs close enough for the Hill prior to bite)
+    for number, plim in ((2, [5.0, 30.0]), (3, [25.0, 150.0]))[:max(0, k - 1)]:
+        kb = _kep(ss, par, number, starmass=hill)
+        kb[0].limits = plim if par in (0, 1, 3, 4) else [np.log(plim[0]), np.log(plim[1])]
+        blocks.append(kb)
+    if hill:
+        # moderate eccentricities, so that the draws fall on both sides of the
+        # Hill criterion rather than mostly past it
+        for kb in blocks:
+            if kb.parameterisation in (1, 4):
+                kb[3].limits = [-0.3, 0.3]
+                kb[4].limits = [-0.3, 0.3]
+            elif kb.parameterisation in (0, 3):
+                kb[3].limits = [0.0, 0.2]
     if sinusoid:
         sb = SinusoidBlock(1)
         ss(sb)
@@ -167,4 +184,9 @@ def kat_case_models(arr):
     add('51peg_k1_sin', m, d, center=PEG_MAP_P1[:5] + [800.0, 3.0, 1.0] + PEG_MAP_P1[5:])
     m, d = model_51peg(arr, k=1, par=0, cycle=True, moav={'order': 1, 'global': True})
     add('51peg_k1_cycle_gma1', m, d)
+    # Hill stability priors (support/priors/Hill.prior) on 2 and 3 Keplerians
+    m, d = model_51peg(arr, k=2, par=1, hill=1.11)
+    add('51peg_k2_hill', m, d)
+    m, d = model_51peg(arr, k=3, par=0, hill=1.11)
+    add('51peg_k3_hill_p0', m, d)
     return cases

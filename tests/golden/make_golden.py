@@ -11,6 +11,10 @@ Writes
   logpost_kat.npz   -- oracle known-answer vectors: (logL, logprior) of a
                        fixed set of theta for several model specs, used to
                        pin the oracle (CPU tests) and the CUDA path (GPU tests)
+  hill_kat.npz      -- the reference's own Hill prior (support/priors/Hill.prior
+                       with math_utils.cps, executed from the reference's
+                       files) at seeded planet sets, to pin the oracle's
+                       restatement
 """
 from __future__ import annotations
 
@@ -44,6 +48,36 @@ def main(ref_root):
     out['specs_json'] = np.array(json.dumps(specs))
     np.savez_compressed(os.path.join(HERE, 'logpost_kat.npz'), **out)
     print('wrote', sorted(k for k in out if k.endswith('__logl')))
+    hill_fixture(ref_root)
+
+
+def hill_fixture(ref_root):
+    """Evaluate the reference's Hill prior on seeded planet sets."""
+    import importlib.util
+    src = os.path.join(ref_root, 'src', 'astroemperor')
+    spec = importlib.util.spec_from_file_location('_ref_math_utils', os.path.join(src, 'math_utils.py'))
+    mu = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mu)
+    ns = {'np': np, 'cps': mu.cps}
+    exec(open(os.path.join(src, 'support', 'priors', 'Hill.prior')).read(), ns)
+    rng = np.random.default_rng(4321)
+    X, A, out = [], [], []
+    for i in range(400):
+        k = int(rng.integers(2, 5))
+        per = np.exp(rng.uniform(np.log(2.0), np.log(300.0), k))
+        amp = np.exp(rng.uniform(np.log(0.5), np.log(60.0), k))
+        ecc = rng.uniform(0.0, 0.4, k)
+        mstar = float(rng.uniform(0.3, 1.5))
+        x = np.zeros((3, 4))
+        x[:, :k] = [per, amp, ecc]
+        with np.errstate(all='ignore'):
+            v = ns['Hill'](np.array([per, amp, ecc]), [None, None], [k, mstar])
+        X.append(x)
+        A.append([k, mstar])
+        out.append(v)
+    np.savez_compressed(os.path.join(HERE, 'hill_kat.npz'), x=np.array(X), args=np.array(A),
+                        value=np.array(out))
+    print('hill_kat:', int(np.sum(np.isfinite(out))), 'stable of', len(out))
 
 
 if __name__ == '__main__':
