@@ -68,7 +68,7 @@ __device__ __forceinline__ double derived_x(const double* th, int k) {
 // them.  As in the reference, gamma = sqrt(1 - e) keeps the planets' own
 // order while the masses and axes are sorted.  Not inlined: its dynamically
 // indexed arrays would otherwise take the log-posterior kernels' registers.
-__device__ __noinline__ bool hill_stable(const emp_model_desc* md, const double* full) {
+static __device__ __noinline__ bool hill_stable(const emp_model_desc* md, const double* full) {
     const int mask = md->hill_mask;
     int K = 0;
     for (int j = 2; j <= EMP_MAX_PLANETS; ++j)
