@@ -287,9 +287,17 @@ class PTSampler:
         dev = self.device
         f64 = dict(dtype=torch.float64, device=dev)
         i32 = dict(dtype=torch.int32, device=dev)
-        self.theta = torch.zeros(T * W, D, **f64)
-        self.logl = torch.full((T * W,), -math.inf, **f64)
-        self.logprior = torch.full((T * W,), -math.inf, **f64)
+        # walker state by slot in one allocation (theta rows, then logl, then
+        # logprior), so that a host round trip is one copy each way
+        self._state = torch.empty(T * W * (D + 2), **f64)
+        self.theta = self._state[: T * W * D].view(T * W, D)
+        self.logl = self._state[T * W * D: T * W * (D + 1)]
+        self.logprior = self._state[T * W * (D + 1):]
+        self.theta.zero_()
+        self.logl.fill_(-math.inf)
+        self.logprior.fill_(-math.inf)
+        self._st_key = None
+        self._st = None
         self.members = torch.arange(T * W, **i32)
         self.betas_d = torch.tensor(betas, **f64)
         self.counters = torch.zeros(4, dtype=torch.int64, device=dev)
@@ -307,6 +315,10 @@ class PTSampler:
 
     # ------------------------------------------------------------------
     def _state_struct(self, nsteps: int) -> N.EmpPtState:
+        key = (int(nsteps), self.adaptive, self.seed, self.a, self.adapt_tau, self.adapt_nu,
+               self.adapt_mode, self.precision, self.work.data_ptr())
+        if key == self._st_key:
+            return self._st
         st = N.EmpPtState()
         st.ntemps, st.nwalkers, st.ndim, st.nsteps = self.ntemps, self.nwalkers, self.ndim, int(nsteps)
         st.theta, st.logl, st.logprior = _ptr(self.theta), _ptr(self.logl), _ptr(self.logprior)
@@ -320,6 +332,7 @@ class PTSampler:
         st.precision = self.precision
         st.work, st.work_bytes = _ptr(self.work), int(self.work.numel())
         st.n_systems = 1
+        self._st_key, self._st = key, st
         return st
 
     def _record_struct(self) -> N.EmpPtRecord:
@@ -414,6 +427,38 @@ class PTSampler:
             h_logl.copy_(self.logl, non_blocking=True)
             h_logprior.copy_(self.logprior, non_blocking=True)
         s.synchronize()
+
+    def host_state(self):
+        """A pinned host buffer laid out like the device state (theta rows by
+        slot, then logl, then logprior), holding the current state."""
+        h = torch.empty(self._state.numel(), dtype=torch.float64).pin_memory()
+        self.stream.synchronize()
+        h.copy_(self._state)
+        return h
+
+    def sweep_host_packed(self, h_state, use_graph=None):
+        """``sweep_host`` with the state in one pinned buffer from
+        ``host_state()``: one host-to-device copy, one sweep, one copy back."""
+        if not self._initialised:
+            raise RuntimeError('run_mcmc or set_positions first')
+        s = self.stream
+        with torch.cuda.stream(s):
+            self._state.copy_(h_state, non_blocking=True)
+            if self.cap == 0:
+                self._grow(1)
+            st = self._state_struct(1)
+            rec = self._rec_cached()
+            ug = self.use_graph if use_graph is None else bool(use_graph)
+            N.call('emp_pt_run', self.ctx.h, C.byref(st), C.byref(rec), 1, 1 if ug else 0, s.cuda_stream)
+            h_state.copy_(self._state, non_blocking=True)
+        s.synchronize()
+
+    def _rec_cached(self):
+        key = (self.cap, self.chain.data_ptr() if self.chain is not None else 0,
+               self.tsw_history_bool, self.smd_history_bool)
+        if getattr(self, '_rec_key', None) != key:
+            self._rec_key, self._rec = key, self._record_struct()
+        return self._rec
 
     def select_adjustment(self, name='00'):
         """Freeze the ladder (endit_freeze1.scr:11 calls ``select_adjustment('00')``)."""

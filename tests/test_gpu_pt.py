@@ -176,3 +176,30 @@ def test_posterior_quantiles_match_the_oracle_sampler(peg_arr, lib, cuda):
         width = np.percentile(cpu[:, j], 84) - np.percentile(cpu[:, j], 16)
         for q in (16, 50, 84):
             assert abs(np.percentile(g[:, j], q) - np.percentile(cpu[:, j], q)) < 0.5 * width, (j, q)
+
+
+def test_sweep_host_equals_device_sweep(peg_arr, lib, cuda):
+    """A sweep through pinned host state (packed and three-tensor forms) is
+    the device sweep: same counters and random words, same state after."""
+    from astroemperor_gb300.engine import Context, PTState
+    m, d = model_51peg(peg_arr, k=1, par=1)
+    T, W = 3, 32
+    p0 = _p0(m, T, W, 21)
+    ctx = Context(m, 'cuda:0')
+    ss = [PTSampler(W, m.ndim__, m, ntemps=T, betas=[1.0, 0.3, 0.05], precision='mixed', seed=8,
+                    context=ctx, autotune=False) for _ in range(3)]
+    for s in ss:
+        s.run_mcmc(p0, nsweeps=4)
+    h = ss[0].host_state()
+    for _ in range(3):
+        ss[0].sweep_host_packed(h)
+    ht = ss[1].theta.cpu().pin_memory()
+    hl = ss[1].logl.cpu().pin_memory()
+    hp = ss[1].logprior.cpu().pin_memory()
+    for _ in range(3):
+        ss[1].sweep_host(ht, hl, hp)
+    ss[2].run_mcmc(PTState(ss[2]), nsweeps=3)
+    ref = torch.cat([ss[2].theta.reshape(-1), ss[2].logl, ss[2].logprior]).cpu()
+    np.testing.assert_array_equal(h.numpy(), ref.numpy())
+    np.testing.assert_array_equal(torch.cat([ht.reshape(-1), hl, hp]).numpy(), ref.numpy())
+    assert not np.array_equal(ref.numpy()[: T * W * m.ndim__], p0.reshape(-1))
