@@ -124,6 +124,8 @@ SIGNATURES = {
     'emp_pt_run': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord), C.c_int,
                              C.c_int, C.c_void_p]),
     'emp_pt_evaluate': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.c_void_p]),
+    'emp_pt_run_host': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord), C.c_void_p,
+                                  C.c_void_p]),
     'emp_pt_work_bytes': (C.c_int64, [C.c_int, C.c_int, C.c_int]),
     'emp_set_launch': (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     'emp_get_launch': (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),

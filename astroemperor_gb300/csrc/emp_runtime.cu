@@ -68,6 +68,7 @@ struct GraphCache {
     cudaStream_t stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    void* host = nullptr;        // packed host state copied in and out (emp_pt_run_host)
     int kernels_per_launch = 0;
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -99,7 +100,8 @@ struct emp_handle {
     int tile[2] = {0, 0};
     int* dev2orig = nullptr;
     cudaStream_t own = nullptr;
-    GraphCache gc;
+    GraphCache gc;               // emp_pt_run
+    GraphCache gch;              // emp_pt_run_host
     bool attr_done[2][4][6] = {};
     bool swap_attr = false;
     bool swap_attr_batch = false;
@@ -401,6 +403,7 @@ int gp_reserve(emp_handle* h, int64_t rows) {
     if (total > ((size_t)64 << 30))
         return fail(EMP_E_SIZE, "GP workspace of %zu B for %lld rows exceeds 64 GiB", total, (long long)rows);
     h->gc.reset();
+    h->gch.reset();
     if (h->gp_buf) {
         cudaFree(h->gp_buf);
         h->gp_buf = nullptr;
@@ -886,6 +889,7 @@ int emp_num_systems(emp_handle* h) {
 int emp_destroy(emp_handle* h) {
     if (!h) return EMP_OK;
     h->gc.reset();
+    h->gch.reset();
     if (h->own) cudaStreamDestroy(h->own);
     if (h->dbuf) cudaFree(h->dbuf);
     if (h->gp_buf) cudaFree(h->gp_buf);
@@ -904,6 +908,7 @@ int emp_set_launch(emp_handle* h, int precision, int lanes_per_walker, int tile_
     h->L[precision] = lanes_per_walker;
     h->tile[precision] = tile_epochs;
     h->gc.reset();
+    h->gch.reset();
     return EMP_OK;
 }
 
@@ -1143,6 +1148,118 @@ extern "C" int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st, const 
 
 extern "C" {
 
+}  // extern "C"
+
+namespace {
+
+// Capture one sweep into gc (replacing what it held): with `host` non-null
+// the packed walker state is copied in from `host` before the sweep and back
+// after it, inside the graph.  Kernel attributes and the persistent grid are
+// set up before the capture (it forbids cudaFuncSetAttribute side effects on
+// some drivers).
+int capture_sweep(emp_handle* h, GraphCache& gc, const emp_pt_state* st, const emp_pt_record* rec,
+                  cudaStream_t ls, void* host, size_t host_bytes) {
+    int rc;
+    emp_pt_record rcopy{};
+    const bool has_rec = rec != nullptr;
+    if (has_rec) rcopy = *rec;
+    gc.reset();
+    if ((rc = prepare_eval(h, st->precision))) return rc;
+    if (!h->swap_attr) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+        h->swap_attr = true;
+    }
+    if (!h->swap_attr_batch) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+        h->swap_attr_batch = true;
+    }
+    CUDA_TRY(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
+    int nk = 0;
+    int64_t before = g_launches.load();
+    rc = EMP_OK;
+    if (host) {
+        cudaError_t e = cudaMemcpyAsync(st->theta, host, host_bytes, cudaMemcpyHostToDevice, ls);
+        if (e != cudaSuccess) rc = fail(EMP_E_CUDA, "state copy in: %s", cudaGetErrorString(e));
+    }
+    if (!rc) rc = enqueue_sweep(h, st, has_rec ? &rcopy : nullptr, ls, &nk);
+    if (!rc && host) {
+        cudaError_t e = cudaMemcpyAsync(host, st->theta, host_bytes, cudaMemcpyDeviceToHost, ls);
+        if (e != cudaSuccess) rc = fail(EMP_E_CUDA, "state copy out: %s", cudaGetErrorString(e));
+    }
+    g_launches.store(before);   // captured, not launched
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ls, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(EMP_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return fail(EMP_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    }
+    gc.graph = graph;
+    gc.exec = exec;
+    gc.st = *st;
+    gc.rec = rcopy;
+    gc.has_rec = has_rec;
+    gc.stream = ls;
+    gc.host = host;
+    gc.kernels_per_launch = nk;
+    gc.valid = true;
+    return EMP_OK;
+}
+
+bool graph_matches(const GraphCache& gc, const emp_pt_state* st, const emp_pt_record* rec, cudaStream_t ls,
+                   void* host) {
+    const bool has_rec = rec != nullptr;
+    return gc.valid && gc.stream == ls && gc.host == host && same_state(gc.st, *st) && gc.has_rec == has_rec &&
+           (!has_rec || same_rec(gc.rec, *rec));
+}
+
+// launch the captured graph `times` times on ls, ordered after and before the
+// caller's stream s
+int launch_graph(GraphCache& gc, cudaStream_t s, cudaStream_t ls, int times) {
+    cudaEvent_t ev = nullptr;
+    if (ls != s) {
+        CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventRecord(ev, s));
+        CUDA_TRY(cudaStreamWaitEvent(ls, ev, 0));
+    }
+    for (int i = 0; i < times; ++i) {
+        cudaError_t e = cudaGraphLaunch(gc.exec, ls);
+        if (e != cudaSuccess) {
+            if (ev) cudaEventDestroy(ev);
+            return fail(EMP_E_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+        }
+        g_launches.fetch_add(gc.kernels_per_launch);
+    }
+    if (ls != s) {
+        CUDA_TRY(cudaEventRecord(ev, ls));
+        CUDA_TRY(cudaStreamWaitEvent(s, ev, 0));
+        cudaEventDestroy(ev);
+    }
+    return EMP_OK;
+}
+
+// graphs are captured and launched on a non-legacy stream
+int launch_stream(emp_handle* h, cudaStream_t s, cudaStream_t* ls) {
+    *ls = s;
+    if (s == nullptr || s == cudaStreamLegacy) {
+        if (!h->own) CUDA_TRY(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
+        *ls = h->own;
+    }
+    return EMP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, int nsweeps,
                int use_graph, void* stream) {
     if (!h) return fail(EMP_E_INVALID, "handle is NULL");
@@ -1157,79 +1274,33 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, 
             if ((rc = enqueue_sweep(h, st, rec, s, nullptr))) return rc;
         return EMP_OK;
     }
-    // graphs are captured and launched on a non-legacy stream
-    cudaStream_t ls = s;
-    if (s == nullptr || s == cudaStreamLegacy) {
-        if (!h->own) CUDA_TRY(cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking));
-        ls = h->own;
-    }
-    emp_pt_record rcopy{};
-    bool has_rec = rec != nullptr;
-    if (has_rec) rcopy = *rec;
-    GraphCache& gc = h->gc;
-    if (!(gc.valid && gc.stream == ls && same_state(gc.st, *st) && gc.has_rec == has_rec &&
-          (!has_rec || same_rec(gc.rec, rcopy)))) {
-        gc.reset();
-        // kernel attributes and the persistent grid are set up outside the
-        // capture (it forbids cudaFuncSetAttribute side effects on some drivers)
-        if ((rc = prepare_eval(h, st->precision))) return rc;
-        if (!h->swap_attr) {
-            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
-            h->swap_attr = true;
-        }
-        if (!h->swap_attr_batch) {
-            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, true>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
-            h->swap_attr_batch = true;
-        }
-        CUDA_TRY(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
-        int nk = 0;
-        int64_t before = g_launches.load();
-        rc = enqueue_sweep(h, st, has_rec ? &rcopy : nullptr, ls, &nk);
-        g_launches.store(before);   // captured, not launched
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamEndCapture(ls, &graph);
-        if (rc) {
-            if (graph) cudaGraphDestroy(graph);
+    cudaStream_t ls;
+    if ((rc = launch_stream(h, s, &ls))) return rc;
+    if (!graph_matches(h->gc, st, rec, ls, nullptr))
+        if ((rc = capture_sweep(h, h->gc, st, rec, ls, nullptr, 0))) return rc;
+    return launch_graph(h->gc, s, ls, nsweeps);
+}
+
+int emp_pt_run_host(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, void* host_state,
+                    void* stream) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    int rc = check_state(h, st);
+    if (rc) return rc;
+    if (!host_state) return fail(EMP_E_INVALID, "host state is NULL");
+    if (h->n_sys > 1) return fail(EMP_E_UNSUPPORTED, "the host-state sweep takes a one-system handle");
+    const size_t tw = (size_t)st->ntemps * st->nwalkers;
+    if (st->logl != st->theta + tw * st->ndim || st->logprior != st->logl + tw)
+        return fail(EMP_E_INVALID, "state buffers not packed (theta rows, then logl, then logprior)");
+    cudaPointerAttributes pa{};
+    CUDA_TRY(cudaPointerGetAttributes(&pa, host_state));
+    if (pa.type != cudaMemoryTypeHost) return fail(EMP_E_INVALID, "host state is not page-locked host memory");
+    if ((rc = gp_reserve(h, (int64_t)tw))) return rc;
+    cudaStream_t s = (cudaStream_t)stream, ls;
+    if ((rc = launch_stream(h, s, &ls))) return rc;
+    if (!graph_matches(h->gch, st, rec, ls, host_state))
+        if ((rc = capture_sweep(h, h->gch, st, rec, ls, host_state, tw * (st->ndim + 2) * sizeof(double))))
             return rc;
-        }
-        if (e != cudaSuccess) return fail(EMP_E_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e));
-        cudaGraphExec_t exec = nullptr;
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        if (e != cudaSuccess) {
-            cudaGraphDestroy(graph);
-            return fail(EMP_E_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
-        }
-        gc.graph = graph;
-        gc.exec = exec;
-        gc.st = *st;
-        gc.rec = rcopy;
-        gc.has_rec = has_rec;
-        gc.stream = ls;
-        gc.kernels_per_launch = nk;
-        gc.valid = true;
-    }
-    cudaEvent_t ev = nullptr;
-    if (ls != s) {
-        CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        CUDA_TRY(cudaEventRecord(ev, s));
-        CUDA_TRY(cudaStreamWaitEvent(ls, ev, 0));
-    }
-    for (int i = 0; i < nsweeps; ++i) {
-        cudaError_t e = cudaGraphLaunch(gc.exec, ls);
-        if (e != cudaSuccess) {
-            if (ev) cudaEventDestroy(ev);
-            return fail(EMP_E_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
-        }
-        g_launches.fetch_add(gc.kernels_per_launch);
-    }
-    if (ls != s) {
-        CUDA_TRY(cudaEventRecord(ev, ls));
-        CUDA_TRY(cudaStreamWaitEvent(s, ev, 0));
-        cudaEventDestroy(ev);
-    }
-    return EMP_OK;
+    return launch_graph(h->gch, s, ls, 1);
 }
 
 int emp_probe_peaks(double* fp32_flops, double* fp64_flops, void* stream) {

@@ -436,22 +436,22 @@ class PTSampler:
         h.copy_(self._state)
         return h
 
-    def sweep_host_packed(self, h_state, use_graph=None):
+    def sweep_host_packed(self, h_state):
         """``sweep_host`` with the state in one pinned buffer from
-        ``host_state()``: one host-to-device copy, one sweep, one copy back."""
+        ``host_state()``: the copy in, the sweep and the copy back run as one
+        CUDA graph (``emp_pt_run_host``); returns after the copy back."""
         if not self._initialised:
             raise RuntimeError('run_mcmc or set_positions first')
-        s = self.stream
-        with torch.cuda.stream(s):
-            self._state.copy_(h_state, non_blocking=True)
-            if self.cap == 0:
-                self._grow(1)
-            st = self._state_struct(1)
-            rec = self._rec_cached()
-            ug = self.use_graph if use_graph is None else bool(use_graph)
-            N.call('emp_pt_run', self.ctx.h, C.byref(st), C.byref(rec), 1, 1 if ug else 0, s.cuda_stream)
-            h_state.copy_(self._state, non_blocking=True)
-        s.synchronize()
+        if not h_state.is_pinned() or h_state.numel() != self._state.numel() or \
+                h_state.dtype != torch.float64:
+            raise ValueError('h_state must be the pinned float64 buffer of host_state()')
+        if self.cap == 0:
+            self._grow(1)
+        st = self._state_struct(1)
+        rec = self._rec_cached()
+        N.call('emp_pt_run_host', self.ctx.h, C.byref(st), C.byref(rec), h_state.data_ptr(),
+               self.stream.cuda_stream)
+        self.stream.synchronize()
 
     def _rec_cached(self):
         key = (self.cap, self.chain.data_ptr() if self.chain is not None else 0,

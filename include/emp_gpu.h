@@ -311,6 +311,16 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st,
                const emp_pt_record* rec, int nsweeps, int use_graph,
                void* stream);
 
+/* One sweep with the walker state in page-locked host memory, as a plugin
+   whose caller keeps the state on the host would run it: host_state holds
+   the state packed like the device buffers of `st` (theta rows by slot, then
+   logl, then logprior; st->logl and st->logprior must follow st->theta that
+   way), is copied in, swept and copied back, all inside one CUDA graph
+   cached for (st, rec, host_state).  Launches only: the caller synchronises
+   `stream` before reading host_state.  One-system handles. */
+int emp_pt_run_host(emp_handle* h, const emp_pt_state* st,
+                    const emp_pt_record* rec, void* host_state, void* stream);
+
 /* (Re)compute logl/logprior of every slot of `st` (initial state). */
 int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream);
 
