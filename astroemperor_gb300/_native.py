@@ -117,7 +117,7 @@ SIGNATURES = {
                                    C.c_void_p, C.c_void_p, C.c_void_p]),
     'emp_model_eval': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     'emp_gp_logl': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
-                              C.c_void_p]),
+                              C.c_int, C.c_void_p]),
     'emp_pt_sweep': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord), C.c_void_p]),
     'emp_pt_sweep_static': (C.c_int, [C.c_void_p, C.POINTER(EmpPtState), C.POINTER(EmpPtRecord),
                                       C.c_void_p]),

@@ -133,7 +133,7 @@ __device__ inline double gp_row(const KArgs& A, int row, const double** th) {
 // (row, epoch) in parallel: U_n, V_n and phi_n (one sincos and one exp per
 // component).  Thread (row, g): rows across the warp's lanes (coalesced
 // [n][rows][M] writes), epochs g, g + E, ... with E = 8 * gridDim.y.
-template <int M>
+template <int M, bool FFO>
 __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
     const int row = blockIdx.x * 32 + (threadIdx.x & 31);
     const int E = gridDim.y * 8;
@@ -169,9 +169,7 @@ __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
         const double ti = t[i];
         const double dt = i > 0 ? ti - t[i - 1] : 0.0;
         double sn[M], cs[M], ph[M];
-        double* u = A.gp_u + ((size_t)i * A.nwalk + row) * M;
-        double* v = A.gp_v + ((size_t)i * A.nwalk + row) * M;
-        double* q = A.gp_ph + ((size_t)i * A.nwalk + row) * M;
+        const size_t o = ((size_t)i * A.nwalk + row) * M;
 #pragma unroll
         for (int k = 0; k < M; ++k) {
             if (k > 0 && ps[k]) { sn[k] = sn[k - 1]; cs[k] = cs[k - 1]; ph[k] = ph[k - 1]; }
@@ -180,9 +178,63 @@ __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
                 else { sn[k] = 0.0; cs[k] = 1.0; }
                 ph[k] = pc[k] != 0.0 ? exp(-pc[k] * dt) : 1.0;
             }
-            u[k] = ps[k] ? pa[k] * sn[k] - pb[k] * cs[k] : pa[k] * cs[k] + pb[k] * sn[k];
-            v[k] = pv[k] * (ps[k] ? sn[k] : cs[k]);
-            q[k] = ph[k];
+            const double u = ps[k] ? pa[k] * sn[k] - pb[k] * cs[k] : pa[k] * cs[k] + pb[k] * sn[k];
+            const double v = pv[k] * (ps[k] ? sn[k] : cs[k]);
+            if constexpr (FFO) {
+                // float-float pairs for the mixed recursion
+                const FF fu = ff_split(u), fv = ff_split(v), fp = ff_split(ph[k]);
+                reinterpret_cast<float2*>(A.gp_u)[o + k] = make_float2(fu.hi, fu.lo);
+                reinterpret_cast<float2*>(A.gp_v)[o + k] = make_float2(fv.hi, fv.lo);
+                reinterpret_cast<float2*>(A.gp_ph)[o + k] = make_float2(fp.hi, fp.lo);
+            } else {
+                A.gp_u[o + k] = u;
+                A.gp_v[o + k] = v;
+                A.gp_ph[o + k] = ph[k];
+            }
+        }
+    }
+}
+
+// the mode's outputs of one row (all M lanes of the row call it)
+template <int M>
+__device__ __forceinline__ void gp_finish(const KArgs& A, int row, int k, bool live, bool valid, double lp,
+                                          const double* th, double ll) {
+    const emp_model_desc* md = A.md;
+    // one value for the row: every lane takes lane 0's
+    ll = __shfl_sync(0xffffffffu, ll, 0, M);
+    if (A.mode == kModeGPOnly) {
+        if (live && k == 0) A.logl[row] = ll;
+    } else if (A.mode == kModeLogpost) {
+        if (live && k == 0) {
+            A.logl[row] = valid ? ll : -INFINITY;
+            if (A.logp != nullptr && A.beta != nullptr)
+                A.logp[row] = (valid && ll > -INFINITY) ? __dadd_rn(__dmul_rn(A.beta[row], ll), lp) : -INFINITY;
+        }
+    } else if (A.mode == kModeSlots) {
+        if (live && k == 0) A.st_logl[row] = ll;
+    } else {
+        // stretch: every lane of the row takes the same decision; the
+        // current walker's values are read before lane 0 replaces them
+        bool acc = false;
+        GPMeta m{};
+        if (valid && ll > -INFINITY) {
+            m = A.gp_meta[row];
+            const double beta = A.betas[m.t];
+            const double lpj = A.st_logprior[m.slot];
+            const double llj = A.st_logl[m.slot];
+            const double cur = lpj > -INFINITY ? __dadd_rn(__dmul_rn(beta, llj), lpj) : -INFINITY;
+            const double nlp = __dadd_rn(__dmul_rn(beta, ll), lp);
+            acc = metropolis(nlp, cur, m.z, md->n_free - 1, m.uword);
+        }
+        __syncwarp();
+        if (acc) {
+            if (k == 0) {
+                A.st_logl[m.slot] = ll;
+                A.st_logprior[m.slot] = lp;
+                A.accepted[m.pos] += 1;
+            }
+            double* dst = A.st_theta + (size_t)m.slot * A.dstride;
+            for (int d = k; d < md->n_free; d += M) dst[d] = th[d];
         }
     }
 }
@@ -276,41 +328,123 @@ __global__ void __launch_bounds__(128) k_gp(KArgs A) {
         ll = -0.5 * (quad + logdet) + md->loglike_const;
         if (!isfinite(ll)) ll = -INFINITY;
     }
-    if (A.mode == kModeGPOnly) {
-        if (live && k == 0) A.logl[row] = ll;
-    } else if (A.mode == kModeLogpost) {
-        if (live && k == 0) {
-            A.logl[row] = valid ? ll : -INFINITY;
-            if (A.logp != nullptr && A.beta != nullptr)
-                A.logp[row] = (valid && ll > -INFINITY) ? __dadd_rn(__dmul_rn(A.beta[row], ll), lp) : -INFINITY;
-        }
-    } else if (A.mode == kModeSlots) {
-        if (live && k == 0) A.st_logl[row] = ll;
-    } else {
-        // stretch: every lane of the row takes the same decision; the
-        // current walker's values are read before lane 0 replaces them
-        bool acc = false;
-        GPMeta m{};
-        if (valid && ll > -INFINITY) {
-            m = A.gp_meta[row];
-            const double beta = A.betas[m.t];
-            const double lpj = A.st_logprior[m.slot];
-            const double llj = A.st_logl[m.slot];
-            const double cur = lpj > -INFINITY ? __dadd_rn(__dmul_rn(beta, llj), lpj) : -INFINITY;
-            const double nlp = __dadd_rn(__dmul_rn(beta, ll), lp);
-            acc = metropolis(nlp, cur, m.z, md->n_free - 1, m.uword);
-        }
-        __syncwarp();
-        if (acc) {
-            if (k == 0) {
-                A.st_logl[m.slot] = ll;
-                A.st_logprior[m.slot] = lp;
-                A.accepted[m.pos] += 1;
-            }
-            double* dst = A.st_theta + (size_t)m.slot * A.dstride;
-            for (int d = k; d < md->n_free; d += M) dst[d] = th[d];
-        }
+    gp_finish<M>(A, row, k, live, valid, lp, th, ll);
+}
+
+// FP64 residual rows of a caller to the float-float pairs of k_gp_ff
+static __global__ void __launch_bounds__(256) k_gp_cvt(const double* r, const double* e, float2* ro, float2* eo,
+                                                 size_t count) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+        const FF a = ff_split(r[i]), b = ff_split(e[i]);
+        ro[i] = make_float2(a.hi, a.lo);
+        eo[i] = make_float2(b.hi, b.lo);
     }
+}
+
+// float-float helpers of the mixed recursion
+__device__ __forceinline__ FF ff_of(float2 v) { return FF{v.x, v.y}; }
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_shfl(FF a, int src, int width) {
+    return FF{__shfl_sync(0xffffffffu, a.hi, src, width), __shfl_sync(0xffffffffu, a.lo, src, width)};
+}
+__device__ __forceinline__ FF ff_shfl_xor(FF a, int m, int width) {
+    return FF{__shfl_xor_sync(0xffffffffu, a.hi, m, width), __shfl_xor_sync(0xffffffffu, a.lo, m, width)};
+}
+__device__ __forceinline__ FF ff_mulr(FF a, FF b) {                 // renormalised product
+    const FF p = ff_mul(a, b);
+    return ff_norm(p.hi, p.lo);
+}
+
+// The same recursion in float-float arithmetic (~2^-46 relative per
+// operation) for the mixed precision: FP32 instructions issue ~60 times as
+// fast as FP64 ones on this GPU.  Inputs are the float-float pairs of
+// k_gp_prep<M, true> and k_logpost's FP32 residuals; the sums across a row's
+// lanes are broadcast from lane 0 so that every lane holds the same D and z.
+template <int M>
+__global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rowr = gtid / M;
+    const int k = gtid & (M - 1);
+    const bool live = rowr < A.nwalk;
+    const int row = live ? rowr : A.nwalk - 1;
+    const emp_model_desc* md = A.md;
+    const double* th;
+    const double lp = gp_row(A, row, &th);
+    const bool valid = live && (lp > -INFINITY);
+    const double asum_d = valid ? A.gp_asum[row] : 0.0;
+    const FF asum = ff_split(isfinite(asum_d) ? asum_d : 0.0);
+    const size_t ld = (size_t)A.nwalk;
+    const int n = A.d.n;
+    const float2* Up = reinterpret_cast<const float2*>(A.gp_u) + (size_t)row * M + k;
+    const float2* Vp = reinterpret_cast<const float2*>(A.gp_v) + (size_t)row * M + k;
+    const float2* Pp = reinterpret_cast<const float2*>(A.gp_ph) + (size_t)row * M + k;
+    const float2* rp = reinterpret_cast<const float2*>(A.gp_r) + row;
+    const float2* ep = reinterpret_cast<const float2*>(A.gp_e) + row;
+    FF S[M];
+#pragma unroll
+    for (int j = 0; j < M; ++j) S[j] = FF{0.f, 0.f};
+    FF f{0.f, 0.f}, W{0.f, 0.f}, Dp{0.f, 0.f}, zp{0.f, 0.f}, quad{0.f, 0.f}, prod{1.f, 0.f};
+    int pexp = 0;
+    bool bad = !isfinite(asum_d);
+    FF Uk{0.f, 0.f}, Vk{0.f, 0.f}, Pk{1.f, 0.f}, ri{0.f, 0.f}, ei{1.f, 0.f};
+    if (valid) { Uk = ff_of(Up[0]); Vk = ff_of(Vp[0]); Pk = ff_of(Pp[0]); ri = ff_of(rp[0]); ei = ff_of(ep[0]); }
+    for (int i = 0; i < n; ++i) {
+        FF Un{0.f, 0.f}, Vn{0.f, 0.f}, Pn{1.f, 0.f}, rn{0.f, 0.f}, en{1.f, 0.f};
+        if (valid && i + 1 < n) {
+            const size_t o = (size_t)(i + 1) * ld;
+            Un = ff_of(Up[o * M]); Vn = ff_of(Vp[o * M]); Pn = ff_of(Pp[o * M]);
+            rn = ff_of(rp[o]); en = ff_of(ep[o]);
+        }
+        FF Uj[M];
+#pragma unroll
+        for (int j = 0; j < M; ++j) Uj[j] = ff_shfl(Uk, j, M);
+        if (i > 0) {
+            const FF dw = ff_mulr(Dp, W);
+#pragma unroll
+            for (int j = 0; j < M; ++j) {
+                const FF Wj = ff_shfl(W, j, M);
+                const FF pj = ff_shfl(Pk, j, M);
+                S[j] = ff_mulr(ff_mulr(Pk, pj), ff_add(ff_mul(dw, Wj), S[j]));
+            }
+            f = ff_mulr(Pk, ff_add(ff_mul(W, zp), f));
+        }
+        FF su = ff_mulr(S[0], Uj[0]);
+#pragma unroll
+        for (int j = 1; j < M; ++j) su = ff_add(su, ff_mul(S[j], Uj[j]));
+        FF p1 = ff_mulr(Uk, su), p2 = ff_mulr(Uk, f);
+#pragma unroll
+        for (int off = M / 2; off >= 1; off >>= 1) {
+            p1 = ff_add(p1, ff_shfl_xor(p1, off, M));
+            p2 = ff_add(p2, ff_shfl_xor(p2, off, M));
+        }
+        p1 = ff_shfl(p1, 0, M);
+        p2 = ff_shfl(p2, 0, M);
+        const FF D = ff_add(ff_add(ei, asum), ff_neg(p1));
+        bad = bad || !(D.hi > 0.f);
+        const FF iD = ff_recip(D);
+        W = ff_mulr(ff_add(Vk, ff_neg(su)), iD);
+        const FF z = ff_add(ri, ff_neg(p2));
+        quad = ff_add(quad, ff_mul(ff_mulr(z, z), iD));
+        // prod *= D, then its binary exponent moves into pexp (exact scaling)
+        prod = ff_mulr(prod, D);
+        {
+            const int ex = ((__float_as_int(prod.hi) >> 23) & 0xff) - 127;
+            const float sc = __int_as_float((127 - ex) << 23);
+            pexp += ex;
+            prod.hi *= sc;
+            prod.lo *= sc;
+        }
+        Dp = D; zp = z;
+        Uk = Un; Vk = Vn; Pk = Pn; ri = rn; ei = en;
+    }
+    double ll = -INFINITY;
+    if (valid && !bad) {
+        const double q = (double)quad.hi + (double)quad.lo;
+        const double logdet = log((double)prod.hi + (double)prod.lo) + (double)pexp * 0.6931471805599453;
+        ll = -0.5 * (q + logdet) + md->loglike_const;
+        if (!isfinite(ll)) ll = -INFINITY;
+    }
+    gp_finish<M>(A, row, k, live, valid, lp, th, ll);
 }
 
 }  // namespace emp

@@ -6,14 +6,20 @@ namespace emp {
 
 using KFn = void (*)(KArgs);
 
-// the recursion kernel of M state dimensions, or (prep != 0) its parallel
-// preparation kernel
-KFn get_kernel_gp(int M, int prep) {
+template <int M>
+static KFn pick_gp(int prep, int ff) {
+    if (prep) return ff ? k_gp_prep<M, true> : k_gp_prep<M, false>;
+    return ff ? k_gp_ff<M> : k_gp<M>;
+}
+
+// the recursion kernel of M state dimensions (ff != 0: float-float, for the
+// mixed precision), or (prep != 0) its parallel preparation kernel
+KFn get_kernel_gp(int M, int prep, int ff) {
     switch (M) {
-        case 2: return prep ? k_gp_prep<2> : k_gp<2>;
-        case 4: return prep ? k_gp_prep<4> : k_gp<4>;
-        case 8: return prep ? k_gp_prep<8> : k_gp<8>;
-        case 16: return prep ? k_gp_prep<16> : k_gp<16>;
+        case 2: return pick_gp<2>(prep, ff);
+        case 4: return pick_gp<4>(prep, ff);
+        case 8: return pick_gp<8>(prep, ff);
+        case 16: return pick_gp<16>(prep, ff);
         default: return nullptr;
     }
 }

@@ -1146,8 +1146,15 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     if (gp_on) {
                         // GP likelihood: hand the residual and err2 to k_gp
                         const size_t gi = (size_t)(base + r * C + k0 + e) * A.nwalk + wk;
-                        A.gp_r[gi] = (double)b;
-                        A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
+                        if constexpr (PREC == EMP_PREC_FP64) {
+                            A.gp_r[gi] = (double)b;
+                            A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
+                        } else {
+                            // float-float pairs for k_gp_ff
+                            reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)b, 0.f);
+                            reinterpret_cast<float2*>(A.gp_e)[gi] =
+                                make_float2((float)(s_s2[ps] + insc[s_in[ps] * INSW + 1]), 0.f);
+                        }
                         continue;
                     }
                     if (Q == 0) {

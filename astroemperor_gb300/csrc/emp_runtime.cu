@@ -27,7 +27,7 @@ KFn get_kernel_fp64(int q, int lidx);
 KFn get_kernel_mixed(int q, int lidx);
 using GFn = void (*)(GArgs);
 GFn get_kernel_grad(int q, int lidx);
-KFn get_kernel_gp(int M, int prep);
+KFn get_kernel_gp(int M, int prep, int ff);
 }  // namespace emp
 
 using namespace emp;
@@ -326,7 +326,7 @@ int prepare_eval(emp_handle* h, int prec) {
 }
 
 void gp_args(const emp_handle* h, KArgs& a);
-int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s);
+int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec);
 
 // counter: for a batch, the int that CTAs of a persistent launch claim
 // items from (zeroed here, in stream order); null launches one CTA per item
@@ -382,7 +382,7 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     fn<<<grid, NT, lay.total, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
-    if (gp) return launch_gp(h, a, s);
+    if (gp) return launch_gp(h, a, s, prec);
     return EMP_OK;
 }
 
@@ -443,10 +443,12 @@ void gp_args(const emp_handle* h, KArgs& a) {
 }
 
 // k_gp_prep (every row x epoch, about 16 warps per SM) then the recursion
-// k_gp (M lanes per row) for the rows of `a`
-int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s) {
+// (M lanes per row) for the rows of `a`: FP64 k_gp, or float-float k_gp_ff
+// for the mixed precision
+int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec) {
     const int M = h->gp_M;
-    KFn prep = get_kernel_gp(M, 1), rec = get_kernel_gp(M, 0);
+    const int ff = prec == EMP_PREC_MIXED ? 1 : 0;
+    KFn prep = get_kernel_gp(M, 1, ff), rec = get_kernel_gp(M, 0, ff);
     if (!prep || !rec) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", M);
     const int gx = (a.nwalk + 31) / 32;
     const int want_warps = std::max(1, h->sms) * 16;
@@ -971,8 +973,10 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, dou
 }
 
 int emp_gp_logl(emp_handle* h, const double* theta, int B, const double* resid, const double* err2,
-                double* logl, void* stream) {
+                double* logl, int precision, void* stream) {
     if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (precision != EMP_PREC_FP64 && precision != EMP_PREC_MIXED)
+        return fail(EMP_E_INVALID, "precision %d unknown", precision);
     if (h->gp_M == 0) return fail(EMP_E_UNSUPPORTED, "the handle's model has no GP");
     if (B < 0) return fail(EMP_E_INVALID, "B=%d < 0", B);
     if (B == 0) return EMP_OK;
@@ -988,9 +992,20 @@ int emp_gp_logl(emp_handle* h, const double* theta, int B, const double* resid, 
     a.logl = logl;
     a.dstride = h->lay[1];
     gp_args(h, a);
-    a.gp_r = const_cast<double*>(resid);
-    a.gp_e = const_cast<double*>(err2);
-    return launch_gp(h, a, (cudaStream_t)stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (precision == EMP_PREC_FP64) {
+        a.gp_r = const_cast<double*>(resid);
+        a.gp_e = const_cast<double*>(err2);
+    } else {
+        // float-float rows in the handle's residual buffers
+        const size_t count = (size_t)h->n * B;
+        const int grid = (int)std::min<size_t>((count + 255) / 256, (size_t)std::max(1, h->sms) * 8);
+        k_gp_cvt<<<grid, 256, 0, s>>>(resid, err2, reinterpret_cast<float2*>(h->gp_r),
+                                      reinterpret_cast<float2*>(h->gp_e), count);
+        g_launches.fetch_add(1);
+        CUDA_TRY(cudaGetLastError());
+    }
+    return launch_gp(h, a, s, precision);
 }
 
 int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, double* logprior,

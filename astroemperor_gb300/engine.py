@@ -140,7 +140,8 @@ class Context:
         N.call('emp_model_eval', self.h, _ptr(theta), B, _ptr(model), _ptr(err2), s.cuda_stream)
         return model, err2
 
-    def gp_logl(self, theta: torch.Tensor, resid: torch.Tensor, err2: torch.Tensor, stream=None):
+    def gp_logl(self, theta: torch.Tensor, resid: torch.Tensor, err2: torch.Tensor,
+                precision: int = N.EMP_PREC_FP64, stream=None):
         """Celerite GP log-likelihood [B] of residual rows resid [B, ndata] with
         diagonal err2 [B, ndata] (time order) under the GP hyperparameters of
         theta [B, ndim] -- ``gp_.log_likelihood(Y_)`` with ``gp_.mean = model``."""
@@ -150,7 +151,8 @@ class Context:
         e = err2.t().contiguous()
         logl = torch.empty(B, dtype=torch.float64, device=theta.device)
         s = stream if stream is not None else torch.cuda.current_stream(theta.device)
-        N.call('emp_gp_logl', self.h, _ptr(theta), B, _ptr(r), _ptr(e), _ptr(logl), s.cuda_stream)
+        N.call('emp_gp_logl', self.h, _ptr(theta), B, _ptr(r), _ptr(e), _ptr(logl), int(precision),
+               s.cuda_stream)
         return logl
 
 

@@ -541,7 +541,7 @@ def main():
         ee = e2.t().contiguous()
         gl = torch.empty(B, dtype=torch.float64, device=dev)
         g_ms = graph_time((ctx.h, th_half.data_ptr(), B, rr.data_ptr(), ee.data_ptr(), gl.data_ptr(),
-                           rs.cuda_stream), 50, rs, entry='emp_gp_logl')
+                           N.EMP_PREC_MIXED, rs.cuda_stream), 50, rs, entry='emp_gp_logl')
         Mg = 4                                                  # state dimensions of the kernel
         Fg = 4.5 * Mg * Mg + 16.5 * Mg + 8                      # FLOP per row*epoch
         ach = Fg * B * n / (g_ms * 1e-3) / 1e12
@@ -550,7 +550,8 @@ def main():
                 'traffic': NCU_TRAFFIC.get(args.config),
                 'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch',
                 'algorithmic_bytes': B * (16 * n + 8 * D + 8) + 8 * n,
-                'kernel': 'k_gp<4> (celerite recursion, half-step rows)', 'kernel_ms': g_ms,
+                'kernel': 'k_gp_prep<4> + k_gp_ff<4> (celerite recursion, float-float, half-step rows)',
+                'kernel_ms': g_ms,
                 'flop_per_row_epoch': Fg,
                 'peak_source': 'FP64 peak measured on this GPU by the library FMA probe',
                 'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp)',

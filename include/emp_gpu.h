@@ -225,13 +225,15 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model,
    gp_.mean = model (support/kernels/00.kernel, support/likelihoods/02.like)
    for a handle whose model has a Celerite2 GP: the celerite log-likelihood
    of B given residual rows under the GP hyperparameters of theta [B][n_free].
-   resid and err2 are device [n][B] (epoch-major, the dataset's time order);
-   logl [B].  FP64 semiseparable recursion, one thread per row; logl = -inf
-   where the covariance is not positive definite.  EMP_E_UNSUPPORTED for a
-   handle without a GP.  The log-posterior entries compute the residuals
-   themselves; this one serves callers with their own mean model. */
+   resid and err2 are device FP64 [n][B] (epoch-major, the dataset's time
+   order); logl [B].  Semiseparable recursion with M lanes per row, in FP64
+   (EMP_PREC_FP64) or float-float (EMP_PREC_MIXED, the residuals converted
+   first); logl = -inf where the covariance is not positive definite.
+   EMP_E_UNSUPPORTED for a handle without a GP.  The log-posterior entries
+   compute the residuals themselves; this one serves callers with their own
+   mean model. */
 int emp_gp_logl(emp_handle* h, const double* theta, int B, const double* resid,
-                const double* err2, double* logl, void* stream);
+                const double* err2, double* logl, int precision, void* stream);
 
 /* Parallel-tempering state, all device pointers owned by the caller.
    Walker slots are physical; `members[t*W + j]` names the slot that holds

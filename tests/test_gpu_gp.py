@@ -160,6 +160,9 @@ def test_gp_logl_of_given_residuals(cases):
         ref, _ = _eval(ctx, th[fin], N.EMP_PREC_FP64)
         np.testing.assert_allclose(ll, ref, rtol=1e-12, err_msg=name)
         np.testing.assert_allclose(ll, kll[fin], rtol=FP64_RTOL, err_msg=name)
+        # the float-float recursion on the same FP64 residuals
+        llf = ctx.gp_logl(t, y[None, :] - model, err2, precision=N.EMP_PREC_MIXED).cpu().numpy()
+        np.testing.assert_allclose(llf, ll, rtol=1e-10, err_msg=name)
 
 
 def test_gp_unsupported_paths(peg_arr, lib, cuda):
