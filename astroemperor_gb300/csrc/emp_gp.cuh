@@ -129,6 +129,22 @@ __device__ inline double gp_row(const KArgs& A, int row, const double** th) {
     return A.gp_meta[row].lp;
 }
 
+// x as a float-float pair by bit manipulation (integer and FP32 instructions
+// only; a double-to-float conversion would take the FP64 pipe): hi = x
+// truncated to 24 significant bits, lo = the remaining 29 bits rounded to a
+// float (|x - hi - lo| <= 2^-47 |x|).  |x| < 2^-125 flushes to zero; |x|
+// must be below 2^128.
+__device__ __forceinline__ float2 ff_split_bits(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+    if (e < -125) return make_float2(0.f, 0.f);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+    const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29));
+    const float lo = ldexpf(__uint2float_rn((unsigned)(m & 0x1FFFFFFFu)), e - 52);
+    return make_float2(hi, sign ? -lo : lo);
+}
+
 // Everything of the recursion that does not depend on its state, for every
 // (row, epoch) in parallel: U_n, V_n and phi_n (one sincos and one exp per
 // component).  Thread (row, g): rows across the warp's lanes (coalesced
@@ -182,10 +198,9 @@ __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
             const double v = pv[k] * (ps[k] ? sn[k] : cs[k]);
             if constexpr (FFO) {
                 // float-float pairs for the mixed recursion
-                const FF fu = ff_split(u), fv = ff_split(v), fp = ff_split(ph[k]);
-                reinterpret_cast<float2*>(A.gp_u)[o + k] = make_float2(fu.hi, fu.lo);
-                reinterpret_cast<float2*>(A.gp_v)[o + k] = make_float2(fv.hi, fv.lo);
-                reinterpret_cast<float2*>(A.gp_ph)[o + k] = make_float2(fp.hi, fp.lo);
+                reinterpret_cast<float2*>(A.gp_u)[o + k] = ff_split_bits(u);
+                reinterpret_cast<float2*>(A.gp_v)[o + k] = ff_split_bits(v);
+                reinterpret_cast<float2*>(A.gp_ph)[o + k] = ff_split_bits(ph[k]);
             } else {
                 A.gp_u[o + k] = u;
                 A.gp_v[o + k] = v;
@@ -274,15 +289,7 @@ __global__ void __launch_bounds__(128) k_gp(KArgs A) {
     double f = 0.0, W = 0.0, Dp = 0.0, zp = 0.0, quad = 0.0, prod = 1.0;
     int pexp = 0;
     bool bad = !isfinite(asum);
-    double Uk = 0.0, Vk = 0.0, Pk = 1.0, ri = 0.0, ei = 1.0;
-    if (valid) { Uk = Up[0]; Vk = Vp[0]; Pk = Pp[0]; ri = rp[0]; ei = ep[0]; }
-    for (int i = 0; i < n; ++i) {
-        // the next epoch's inputs are loaded while this one computes
-        double Un = 0.0, Vn = 0.0, Pn = 1.0, rn = 0.0, en = 1.0;
-        if (valid && i + 1 < n) {
-            const size_t o = (size_t)(i + 1) * ld;
-            Un = Up[o * M]; Vn = Vp[o * M]; Pn = Pp[o * M]; rn = rp[o]; en = ep[o];
-        }
+    auto epoch = [&](int i, double Uk, double Vk, double Pk, double ri, double ei) {
         double Uj[M];
 #pragma unroll
         for (int j = 0; j < M; ++j) Uj[j] = __shfl_sync(FULL, Uk, j, M);
@@ -320,7 +327,33 @@ __global__ void __launch_bounds__(128) k_gp(KArgs A) {
             prod = __hiloint2double(hi - (int)((unsigned)ex << 20), __double2loint(prod));
         }
         Dp = D; zp = z;
-        Uk = Un; Vk = Vn; Pk = Pn; ri = rn; ei = en;
+    };
+    // the inputs of PF epochs are loaded one block ahead of their use
+    constexpr int PF = 4;
+    double cU[PF], cV[PF], cP[PF], cr[PF], ce[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+        const bool ok = valid && q < n;
+        const size_t o = (size_t)q * ld;
+        cU[q] = ok ? Up[o * M] : 0.0; cV[q] = ok ? Vp[o * M] : 0.0; cP[q] = ok ? Pp[o * M] : 1.0;
+        cr[q] = ok ? rp[o] : 0.0; ce[q] = ok ? ep[o] : 1.0;
+    }
+    for (int i0 = 0; i0 < n; i0 += PF) {
+        double nU[PF], nV[PF], nP[PF], nr[PF], ne[PF];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            const int i = i0 + PF + q;
+            const bool ok = valid && i < n;
+            const size_t o = (size_t)i * ld;
+            nU[q] = ok ? Up[o * M] : 0.0; nV[q] = ok ? Vp[o * M] : 0.0; nP[q] = ok ? Pp[o * M] : 1.0;
+            nr[q] = ok ? rp[o] : 0.0; ne[q] = ok ? ep[o] : 1.0;
+        }
+#pragma unroll
+        for (int q = 0; q < PF; ++q)
+            if (i0 + q < n)                                    // uniform across the warp
+                epoch(i0 + q, cU[q], cV[q], cP[q], cr[q], ce[q]);
+#pragma unroll
+        for (int q = 0; q < PF; ++q) { cU[q] = nU[q]; cV[q] = nV[q]; cP[q] = nP[q]; cr[q] = nr[q]; ce[q] = ne[q]; }
     }
     double ll = -INFINITY;
     if (valid && !bad) {
@@ -386,15 +419,9 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
     FF f{0.f, 0.f}, W{0.f, 0.f}, Dp{0.f, 0.f}, zp{0.f, 0.f}, quad{0.f, 0.f}, prod{1.f, 0.f};
     int pexp = 0;
     bool bad = !isfinite(asum_d);
-    FF Uk{0.f, 0.f}, Vk{0.f, 0.f}, Pk{1.f, 0.f}, ri{0.f, 0.f}, ei{1.f, 0.f};
-    if (valid) { Uk = ff_of(Up[0]); Vk = ff_of(Vp[0]); Pk = ff_of(Pp[0]); ri = ff_of(rp[0]); ei = ff_of(ep[0]); }
-    for (int i = 0; i < n; ++i) {
-        FF Un{0.f, 0.f}, Vn{0.f, 0.f}, Pn{1.f, 0.f}, rn{0.f, 0.f}, en{1.f, 0.f};
-        if (valid && i + 1 < n) {
-            const size_t o = (size_t)(i + 1) * ld;
-            Un = ff_of(Up[o * M]); Vn = ff_of(Vp[o * M]); Pn = ff_of(Pp[o * M]);
-            rn = ff_of(rp[o]); en = ff_of(ep[o]);
-        }
+    // one epoch of the recursion (inputs: this lane's U, V, phi and the row's
+    // residual and err2)
+    auto epoch = [&](int i, FF Uk, FF Vk, FF Pk, FF ri, FF ei) {
         FF Uj[M];
 #pragma unroll
         for (int j = 0; j < M; ++j) Uj[j] = ff_shfl(Uk, j, M);
@@ -408,9 +435,15 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
             }
             f = ff_mulr(Pk, ff_add(ff_mul(W, zp), f));
         }
-        FF su = ff_mulr(S[0], Uj[0]);
+        // (S U)_k as a pairwise sum
+        FF t[M];
 #pragma unroll
-        for (int j = 1; j < M; ++j) su = ff_add(su, ff_mul(S[j], Uj[j]));
+        for (int j = 0; j < M; ++j) t[j] = ff_mul(S[j], Uj[j]);
+#pragma unroll
+        for (int w = 1; w < M; w <<= 1)
+#pragma unroll
+            for (int j = 0; j + w < M; j += 2 * w) t[j] = ff_add(t[j], t[j + w]);
+        const FF su = t[0];
         FF p1 = ff_mulr(Uk, su), p2 = ff_mulr(Uk, f);
 #pragma unroll
         for (int off = M / 2; off >= 1; off >>= 1) {
@@ -435,7 +468,34 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
             prod.lo *= sc;
         }
         Dp = D; zp = z;
-        Uk = Un; Vk = Vn; Pk = Pn; ri = rn; ei = en;
+    };
+    // the inputs of PF epochs are loaded one block ahead of their use
+    constexpr int PF = 4;
+    const float2 zero2 = make_float2(0.f, 0.f), one2 = make_float2(1.f, 0.f);
+    float2 cU[PF], cV[PF], cP[PF], cr[PF], ce[PF];
+#pragma unroll
+    for (int q = 0; q < PF; ++q) {
+        const bool ok = valid && q < n;
+        const size_t o = (size_t)q * ld;
+        cU[q] = ok ? Up[o * M] : zero2; cV[q] = ok ? Vp[o * M] : zero2; cP[q] = ok ? Pp[o * M] : one2;
+        cr[q] = ok ? rp[o] : zero2; ce[q] = ok ? ep[o] : one2;
+    }
+    for (int i0 = 0; i0 < n; i0 += PF) {
+        float2 nU[PF], nV[PF], nP[PF], nr[PF], ne[PF];
+#pragma unroll
+        for (int q = 0; q < PF; ++q) {
+            const int i = i0 + PF + q;
+            const bool ok = valid && i < n;
+            const size_t o = (size_t)i * ld;
+            nU[q] = ok ? Up[o * M] : zero2; nV[q] = ok ? Vp[o * M] : zero2; nP[q] = ok ? Pp[o * M] : one2;
+            nr[q] = ok ? rp[o] : zero2; ne[q] = ok ? ep[o] : one2;
+        }
+#pragma unroll
+        for (int q = 0; q < PF; ++q)
+            if (i0 + q < n)                                    // uniform across the warp
+                epoch(i0 + q, ff_of(cU[q]), ff_of(cV[q]), ff_of(cP[q]), ff_of(cr[q]), ff_of(ce[q]));
+#pragma unroll
+        for (int q = 0; q < PF; ++q) { cU[q] = nU[q]; cV[q] = nV[q]; cP[q] = nP[q]; cr[q] = nr[q]; ce[q] = ne[q]; }
     }
     double ll = -INFINITY;
     if (valid && !bad) {
