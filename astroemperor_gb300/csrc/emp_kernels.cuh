@@ -805,6 +805,65 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     int* flag = reinterpret_cast<int*>(misc + 4);
     constexpr int INSW = kInsW;
 
+    // epoch tile (the dataset is only read here, never written by a sweep)
+    const int tile = A.tile;
+    unsigned char* ts = smem;
+    R* s_t0;  R* s_t1;  R* s_y;  R* s_ylo;  R* s_s2;  int* s_in;  R* s_dt;
+    if (PREC == EMP_PREC_FP64) {
+        s_t0 = reinterpret_cast<R*>(ts);
+        s_t1 = s_t0;                       // unused
+        s_y = s_t0 + tile;
+        s_ylo = s_y;                       // unused
+        s_s2 = s_y + tile;
+        s_in = reinterpret_cast<int*>(s_s2 + tile);
+        s_dt = reinterpret_cast<R*>(ts + Smem::align16((3 * tile) * (int)sizeof(R) + 4 * tile));
+    } else {
+        s_t0 = reinterpret_cast<R*>(ts);
+        s_t1 = s_t0 + tile;
+        s_y = s_t1 + tile;
+        s_ylo = s_y + tile;
+        s_s2 = s_ylo + tile;
+        s_in = reinterpret_cast<int*>(s_s2 + tile);
+        s_dt = reinterpret_cast<R*>(s_in + tile);
+    }
+    // stage epochs [base, base + nt) of the series starting at e0 in the
+    // lane-chunk layout (coalesced reads, conflict-free lane reads)
+    auto stage = [&](int64_t e0s, int base, int nt) {
+        const int C = (nt + L - 1) / L;
+        for (int idx = tid; idx < nt; idx += NT) {
+            const int rr = idx / C;
+            const int kk = idx - rr * C;
+            const int pos = kk * L + ((rr + kk) & (L - 1));
+            const int64_t gi = e0s + base + idx;
+            if (PREC == EMP_PREC_FP64) {
+                s_t0[pos] = (R)A.d.t[gi];
+                s_y[pos] = (R)A.d.y[gi];
+                s_s2[pos] = (R)A.d.s2[gi];
+            } else {
+                s_t0[pos] = (R)A.d.t_hi[gi];
+                s_t1[pos] = (R)A.d.t_lo[gi];
+                s_y[pos] = (R)A.d.y32[gi];
+                s_ylo[pos] = (R)A.d.y_lo[gi];
+                s_s2[pos] = (R)A.d.s2_32[gi];
+            }
+            s_in[pos] = A.d.inst[gi];
+#pragma unroll
+            for (int c = 0; c < Q; ++c) {
+                if (PREC == EMP_PREC_FP64) s_dt[c * tile + pos] = (R)A.d.dt[(size_t)c * A.d.n + gi];
+                else s_dt[c * tile + pos] = (R)A.d.dt32[(size_t)c * A.d.n + gi];
+            }
+        }
+    };
+    // Programmatic dependent launch: the next kernel of a sweep may start its
+    // independent part once every CTA of this one runs, and this one stages
+    // the whole series of a one-system handle (one tile) before it waits for
+    // the previous kernel's results (both instructions are no-ops for a
+    // launch without the attribute).
+    asm volatile("griddepcontrol.launch_dependents;");
+    const bool prestaged = A.work_counter == nullptr && A.sys_off == nullptr && A.d.n <= tile;
+    if (prestaged) stage(0, 0, A.d.n);
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+
     // items: one per CTA for a plain handle; (system, walker chunk) pairs
     // claimed from an atomic counter, costliest systems first, for a batch
     __shared__ int s_item;
@@ -956,26 +1015,6 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
 
     // ---------------- likelihood over epoch tiles ------------------------
     const int n = A.sys_off != nullptr ? (int)(A.sys_off[sys + 1] - e0) : A.d.n;
-    const int tile = A.tile;
-    unsigned char* ts = smem;
-    R* s_t0;  R* s_t1;  R* s_y;  R* s_ylo;  R* s_s2;  int* s_in;  R* s_dt;
-    if (PREC == EMP_PREC_FP64) {
-        s_t0 = reinterpret_cast<R*>(ts);
-        s_t1 = s_t0;                       // unused
-        s_y = s_t0 + tile;
-        s_ylo = s_y;                       // unused
-        s_s2 = s_y + tile;
-        s_in = reinterpret_cast<int*>(s_s2 + tile);
-        s_dt = reinterpret_cast<R*>(ts + Smem::align16((3 * tile) * (int)sizeof(R) + 4 * tile));
-    } else {
-        s_t0 = reinterpret_cast<R*>(ts);
-        s_t1 = s_t0 + tile;
-        s_y = s_t1 + tile;
-        s_ylo = s_y + tile;
-        s_s2 = s_ylo + tile;
-        s_in = reinterpret_cast<int*>(s_s2 + tile);
-        s_dt = reinterpret_cast<R*>(s_in + tile);
-    }
 
     LaneAcc<PREC> acc;                     // lane total: FP64, or float-float
     acc.init();
@@ -987,29 +1026,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
         const int nt = min(tile, n - base);
         const int C = (nt + L - 1) / L;
         __syncthreads();
-        for (int idx = tid; idx < nt; idx += NT) {
-            const int rr = idx / C;
-            const int kk = idx - rr * C;
-            const int pos = kk * L + ((rr + kk) & (L - 1));
-            const int64_t gi = e0 + base + idx;
-            if (PREC == EMP_PREC_FP64) {
-                s_t0[pos] = (R)A.d.t[gi];
-                s_y[pos] = (R)A.d.y[gi];
-                s_s2[pos] = (R)A.d.s2[gi];
-            } else {
-                s_t0[pos] = (R)A.d.t_hi[gi];
-                s_t1[pos] = (R)A.d.t_lo[gi];
-                s_y[pos] = (R)A.d.y32[gi];
-                s_ylo[pos] = (R)A.d.y_lo[gi];
-                s_s2[pos] = (R)A.d.s2_32[gi];
-            }
-            s_in[pos] = A.d.inst[gi];
-#pragma unroll
-            for (int c = 0; c < Q; ++c) {
-                if (PREC == EMP_PREC_FP64) s_dt[c * tile + pos] = (R)A.d.dt[(size_t)c * A.d.n + gi];
-                else s_dt[c * tile + pos] = (R)A.d.dt32[(size_t)c * A.d.n + gi];
-            }
-        }
+        if (!prestaged) stage(e0, base, nt);
         __syncthreads();
 
         // per-lane sequential pass over the lane's chunk, NE epochs at a time

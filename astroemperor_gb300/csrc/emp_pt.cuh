@@ -104,6 +104,10 @@ __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
 // seed + s * 0x9E3779B97F4A7C15, and k_advance moves the shared counters.
 template <bool SMEM, bool BATCH>
 __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
+    // programmatic dependent launch (no-ops without the launch attribute):
+    // the next kernel may launch now; this one waits for the stretch moves
+    asm volatile("griddepcontrol.launch_dependents;");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     extern __shared__ __align__(16) unsigned char sm_raw[];
     __shared__ int s_cnt[kMaxTemps];
     __shared__ uint32_t s_perm[kMaxTemps][2];
@@ -301,6 +305,8 @@ struct RecArgs {
 // distance between the walkers of each accepted swap (one warp per swap;
 // the last block to finish turns the sums into means and resets them).
 __global__ void __launch_bounds__(256) k_record(RecArgs R) {
+    asm volatile("griddepcontrol.launch_dependents;");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     __shared__ int s_last;
     const int64_t row = R.work.rows[0];
     const int64_t TW = (int64_t)R.T * R.W;

@@ -328,9 +328,28 @@ int prepare_eval(emp_handle* h, int prec) {
 void gp_args(const emp_handle* h, KArgs& a);
 int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec);
 
+// a launch that may overlap the previous kernel of the stream (programmatic
+// dependent launch): the kernel starts once every CTA of the previous one
+// runs and executes griddepcontrol.wait before reading its results
+template <typename Arg>
+cudaError_t launch_pdl(void (*fn)(Arg), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Arg arg) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, fn, arg);
+}
+
 // counter: for a batch, the int that CTAs of a persistent launch claim
 // items from (zeroed here, in stream order); null launches one CTA per item
-int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* counter = nullptr) {
+int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* counter = nullptr,
+                bool pdl = false) {
     if (prec != EMP_PREC_FP64 && prec != EMP_PREC_MIXED)
         return fail(EMP_E_INVALID, "precision %d unknown", prec);
     int L = handle_L(h, prec);
@@ -379,7 +398,8 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
         grid = (int)std::min<int64_t>(items, h->persist_grid[prec][li]);
         CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned), s));
     }
-    fn<<<grid, NT, lay.total, s>>>(a);
+    if (pdl) CUDA_TRY(launch_pdl(fn, dim3(grid), dim3(NT), (size_t)lay.total, s, a));
+    else fn<<<grid, NT, lay.total, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
     if (gp) return launch_gp(h, a, s, prec);
@@ -526,7 +546,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                 int ex = 0;
                 a.a_inv_exact = frexp(st->a, &ex) == 0.5 ? 1.0 / st->a : 0.0;   // a = 2^(ex-1)
             }
-            if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr))) return rc;
+            if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr, !batch))) return rc;
             kcount += h->gp_M > 0 ? 3 : 1;
         }
     }
@@ -595,9 +615,9 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
             h->swap_attr = true;
         }
-        k_swap<true, false><<<1, nth, swap_smem, s>>>(S);
+        CUDA_TRY(launch_pdl(k_swap<true, false>, dim3(1), dim3(nth), swap_smem, s, S));
     } else {
-        k_swap<false, false><<<1, nth, 0, s>>>(S);
+        CUDA_TRY(launch_pdl(k_swap<false, false>, dim3(1), dim3(nth), (size_t)0, s, S));
     }
     g_launches.fetch_add(1);
     ++kcount;
@@ -613,7 +633,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
         const int64_t warps = (int64_t)(st->ntemps - 1) * st->nwalkers;
         const int64_t want = std::max((tot + 255) / 256, (warps + 7) / 8);
         const int grid = (int)std::min<int64_t>(std::max<int64_t>(1, want), 152 * 8);
-        k_record<<<grid, 256, 0, s>>>(R);
+        CUDA_TRY(launch_pdl(k_record, dim3(grid), dim3(256), (size_t)0, s, R));
         g_launches.fetch_add(1);
         ++kcount;
         CUDA_TRY(cudaGetLastError());
