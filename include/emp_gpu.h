@@ -195,7 +195,11 @@ int emp_num_systems(emp_handle* h);
    (logl is left at -inf when the prior is -inf).
    A batch handle (emp_create_batch) evaluates B rows per system: theta
    [S][B][ndim] with ndim the largest free dimension (shorter rows padded),
-   beta and the outputs [S][B].  system_of is reserved and must be NULL. */
+   beta and the outputs [S][B].  system_of is reserved and must be NULL.
+   With a GP model (support/likelihoods/02.like) the likelihood is the
+   celerite one; the handle keeps a row workspace for it, allocated by the
+   first call with more rows than before (make that call outside any stream
+   capture; growing it drops the handle's captured sweep graphs). */
 int emp_logpost(emp_handle* h, const double* theta, int B,
                 const int32_t* system_of, const double* beta,
                 double* logl, double* logprior, double* logp,
