@@ -71,7 +71,7 @@ extern "C" {
 #define EMP_PREC_MIXED  1  /* FP32 Kepler solve + RV sum; float-float phase;
                               compensated FP32 per-lane sums, FP64 across lanes */
 
-/* prior kinds (support/priors/*.prior) */
+/* prior kinds (support/priors/<Name>.prior) */
 #define EMP_PRIOR_UNIFORM   0
 #define EMP_PRIOR_NORMAL    1
 #define EMP_PRIOR_JEFFREYS  2
