@@ -145,6 +145,105 @@ __device__ __forceinline__ float2 ff_split_bits(double x) {
     return make_float2(hi, sign ? -lo : lo);
 }
 
+// float-float helpers of the mixed recursion
+__device__ __forceinline__ FF ff_of(float2 v) { return FF{v.x, v.y}; }
+__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_shfl(FF a, int src, int width) {
+    return FF{__shfl_sync(0xffffffffu, a.hi, src, width), __shfl_sync(0xffffffffu, a.lo, src, width)};
+}
+__device__ __forceinline__ FF ff_shfl_xor(FF a, int m, int width) {
+    return FF{__shfl_xor_sync(0xffffffffu, a.hi, m, width), __shfl_xor_sync(0xffffffffu, a.lo, m, width)};
+}
+__device__ __forceinline__ FF ff_mulr(FF a, FF b) {                 // renormalised product
+    const FF p = ff_mul(a, b);
+    return ff_norm(p.hi, p.lo);
+}
+
+// ---------------------------------------------------------------------------
+// float-float sin/cos and exp for the mixed prep.  FP64 transcendentals cost
+// ~40-60 FP64 instructions each on a pipe that issues one warp instruction
+// per ~64 cycles per sub-partition; here the FP64 part is only the
+// Cody-Waite argument reduction (Cody & Waite 1980; the split constants are
+// pi/2 and ln 2 cut into 33/33/53- and 32/53-bit doubles), and the series
+// run in float-float on the FP32 pipes: Taylor coefficients 1/n! as
+// float-float pairs, the terms that cannot reach 1e-16 of the result in
+// plain FP32.  Relative error ~1e-15 (the recursion needs ~1e-12); for exp
+// below e^-60 the low part falls into the FP32 subnormals (such factors only
+// clear the recursion's memory).
+// ---------------------------------------------------------------------------
+#define EMP_FFC(h, l) FF{h, l}
+__device__ __forceinline__ FF ff_horner(FF q, FF s, FF c) { return ff_add(ff_mul(q, s), c); }
+
+// sin and cos of r, |r| <~ pi/4, r float-float
+__device__ __forceinline__ void ff_sincos_red(FF r, FF& sn, FF& cs) {
+    const FF s = ff_mulr(r, r);
+    const float sh = s.hi;
+    // sin r = r + r s (-1/3! + s (1/5! + s (-1/7! + s (1/9! + s T)))),
+    // T = -1/11! + s/13! - s^2/15! in FP32
+    const float T = fmaf(sh, fmaf(sh, -0x1.ae7f3ep-41f, 0x1.612462p-33f), -0x1.ae6456p-26f);
+    FF q = ff_add(EMP_FFC(0x1.71de3ap-19f, 0x1.55b1ccp-45f), FF{sh * T, 0.f});
+    q = ff_horner(q, s, EMP_FFC(-0x1.a01a02p-13f, 0x1.7f97fap-39f));
+    q = ff_horner(q, s, EMP_FFC(0x1.111112p-7f, -0x1.dddddep-32f));
+    q = ff_horner(q, s, EMP_FFC(-0x1.555556p-3f, 0x1.555556p-28f));
+    sn = ff_add(r, ff_mul(r, ff_mulr(s, q)));
+    // cos r = 1 + s (-1/2 + s (1/4! + s (-1/6! + s (1/8! + s (-1/10! + s U))))),
+    // U = 1/12! - s/14! + s^2/16! in FP32
+    const float U = fmaf(sh, fmaf(sh, 0x1.ae7f3ep-45f, -0x1.93974ap-37f), 0x1.1eed8ep-29f);
+    FF c = ff_add(EMP_FFC(-0x1.27e4fcp-22f, 0x1.10ec14p-47f), FF{sh * U, 0.f});
+    c = ff_horner(c, s, EMP_FFC(0x1.a01a02p-16f, -0x1.7f97fap-42f));
+    c = ff_horner(c, s, EMP_FFC(-0x1.6c16c2p-10f, 0x1.27d27ep-35f));
+    c = ff_horner(c, s, EMP_FFC(0x1.555556p-5f, -0x1.555556p-30f));
+    c = ff_horner(c, s, EMP_FFC(-0.5f, 0.f));
+    cs = ff_add(FF{1.f, 0.f}, ff_mul(s, c));
+}
+
+// (sin x, cos x) of a double x as float-float pairs
+__device__ __forceinline__ void ff_sincos(double x, FF& sn, FF& cs) {
+    if (!(fabs(x) < 1.6e6)) {                          // beyond the 3-part reduction
+        double s, c;
+        sincos(x, &s, &c);
+        sn = ff_of(ff_split_bits(s));
+        cs = ff_of(ff_split_bits(c));
+        return;
+    }
+    const double kd = rint(x * 0.6366197723675814);
+    double r = fma(-kd, 1.5707963267341256, x);
+    r = fma(-kd, 6.077100506303966e-11, r);
+    r = fma(-kd, 2.0222662487959506e-21, r);
+    FF s, c;
+    ff_sincos_red(ff_of(ff_split_bits(r)), s, c);
+    switch (((int)kd) & 3) {
+        case 0: sn = s; cs = c; break;
+        case 1: sn = c; cs = ff_neg(s); break;
+        case 2: sn = ff_neg(s); cs = ff_neg(c); break;
+        default: sn = ff_neg(c); cs = s; break;
+    }
+}
+
+// exp(-y), y >= 0, as a float-float pair (0 below 2^-126)
+__device__ __forceinline__ FF ff_exp_neg(double y) {
+    if (!(y < 87.0)) return FF{0.f, 0.f};
+    const double kd = rint(-y * 1.4426950408889634);
+    double r = fma(-kd, 0.6931471806019545, -y);
+    r = fma(-kd, -4.2009150726810846e-11, r);
+    const FF rf = ff_of(ff_split_bits(r));
+    const float rh = rf.hi;
+    // e^r = 1 + r (1 + r (1/2! + ... + r (1/8! + r T))), T = 1/9! + r/10! + r^2/11! in FP32
+    const float T = fmaf(rh, fmaf(rh, 0x1.ae6456p-26f, 0x1.27e4fcp-22f), 0x1.71de3ap-19f);
+    FF q = ff_add(EMP_FFC(0x1.a01a02p-16f, -0x1.7f97fap-42f), FF{rh * T, 0.f});
+    q = ff_horner(q, rf, EMP_FFC(0x1.a01a02p-13f, -0x1.7f97fap-39f));
+    q = ff_horner(q, rf, EMP_FFC(0x1.6c16c2p-10f, -0x1.27d27ep-35f));
+    q = ff_horner(q, rf, EMP_FFC(0x1.111112p-7f, -0x1.dddddep-32f));
+    q = ff_horner(q, rf, EMP_FFC(0x1.555556p-5f, -0x1.555556p-30f));
+    q = ff_horner(q, rf, EMP_FFC(0x1.555556p-3f, -0x1.555556p-28f));
+    q = ff_horner(q, rf, EMP_FFC(0.5f, 0.f));
+    q = ff_horner(q, rf, EMP_FFC(1.f, 0.f));
+    q = ff_horner(q, rf, EMP_FFC(1.f, 0.f));
+    // times 2^k (k >= -126 since y < 87), exact
+    const float sc = __int_as_float(((int)kd + 127) << 23);
+    return FF{q.hi * sc, q.lo * sc};
+}
+
 // Everything of the recursion that does not depend on its state, for every
 // (row, epoch) in parallel: U_n, V_n and phi_n (one sincos and one exp per
 // component).  Thread (row, g): rows across the warp's lanes (coalesced
@@ -181,6 +280,34 @@ __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
     if (!finite) return;
     const double* t = A.d.t;
     const int n = A.d.n;
+    if constexpr (FFO) {
+        // float-float transcendentals and products (mixed precision)
+        FF fa[M], fb[M];
+#pragma unroll
+        for (int k = 0; k < M; ++k) { fa[k] = ff_of(ff_split_bits(pa[k])); fb[k] = ff_of(ff_split_bits(pb[k])); }
+        for (int i = g; i < n; i += E) {
+            const double ti = t[i];
+            const double dt = i > 0 ? ti - t[i - 1] : 0.0;
+            FF sn[M], cs[M], ph[M];
+            const size_t o = ((size_t)i * A.nwalk + row) * M;
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+                if (k > 0 && ps[k]) { sn[k] = sn[k - 1]; cs[k] = cs[k - 1]; ph[k] = ph[k - 1]; }
+                else {
+                    if (pd[k] != 0.0) ff_sincos(pd[k] * ti, sn[k], cs[k]);
+                    else { sn[k] = FF{0.f, 0.f}; cs[k] = FF{1.f, 0.f}; }
+                    ph[k] = pc[k] != 0.0 ? ff_exp_neg(pc[k] * dt) : FF{1.f, 0.f};
+                }
+                const FF u = ps[k] ? ff_add(ff_mul(fa[k], sn[k]), ff_neg(ff_mul(fb[k], cs[k])))
+                                   : ff_add(ff_mul(fa[k], cs[k]), ff_mul(fb[k], sn[k]));
+                const FF v = pv[k] != 0.0 ? (ps[k] ? sn[k] : cs[k]) : FF{0.f, 0.f};
+                reinterpret_cast<float2*>(A.gp_u)[o + k] = make_float2(u.hi, u.lo);
+                reinterpret_cast<float2*>(A.gp_v)[o + k] = make_float2(v.hi, v.lo);
+                reinterpret_cast<float2*>(A.gp_ph)[o + k] = make_float2(ph[k].hi, ph[k].lo);
+            }
+        }
+        return;
+    }
     for (int i = g; i < n; i += E) {
         const double ti = t[i];
         const double dt = i > 0 ? ti - t[i - 1] : 0.0;
@@ -194,18 +321,9 @@ __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
                 else { sn[k] = 0.0; cs[k] = 1.0; }
                 ph[k] = pc[k] != 0.0 ? exp(-pc[k] * dt) : 1.0;
             }
-            const double u = ps[k] ? pa[k] * sn[k] - pb[k] * cs[k] : pa[k] * cs[k] + pb[k] * sn[k];
-            const double v = pv[k] * (ps[k] ? sn[k] : cs[k]);
-            if constexpr (FFO) {
-                // float-float pairs for the mixed recursion
-                reinterpret_cast<float2*>(A.gp_u)[o + k] = ff_split_bits(u);
-                reinterpret_cast<float2*>(A.gp_v)[o + k] = ff_split_bits(v);
-                reinterpret_cast<float2*>(A.gp_ph)[o + k] = ff_split_bits(ph[k]);
-            } else {
-                A.gp_u[o + k] = u;
-                A.gp_v[o + k] = v;
-                A.gp_ph[o + k] = ph[k];
-            }
+            A.gp_u[o + k] = ps[k] ? pa[k] * sn[k] - pb[k] * cs[k] : pa[k] * cs[k] + pb[k] * sn[k];
+            A.gp_v[o + k] = pv[k] * (ps[k] ? sn[k] : cs[k]);
+            A.gp_ph[o + k] = ph[k];
         }
     }
 }
@@ -374,19 +492,6 @@ static __global__ void __launch_bounds__(256) k_gp_cvt(const double* r, const do
     }
 }
 
-// float-float helpers of the mixed recursion
-__device__ __forceinline__ FF ff_of(float2 v) { return FF{v.x, v.y}; }
-__device__ __forceinline__ FF ff_neg(FF a) { return FF{-a.hi, -a.lo}; }
-__device__ __forceinline__ FF ff_shfl(FF a, int src, int width) {
-    return FF{__shfl_sync(0xffffffffu, a.hi, src, width), __shfl_sync(0xffffffffu, a.lo, src, width)};
-}
-__device__ __forceinline__ FF ff_shfl_xor(FF a, int m, int width) {
-    return FF{__shfl_xor_sync(0xffffffffu, a.hi, m, width), __shfl_xor_sync(0xffffffffu, a.lo, m, width)};
-}
-__device__ __forceinline__ FF ff_mulr(FF a, FF b) {                 // renormalised product
-    const FF p = ff_mul(a, b);
-    return ff_norm(p.hi, p.lo);
-}
 
 // The same recursion in float-float arithmetic (~2^-46 relative per
 // operation) for the mixed precision: FP32 instructions issue ~60 times as
