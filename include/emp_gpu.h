@@ -233,9 +233,10 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model,
    order); logl [B].  Semiseparable recursion with M lanes per row, in FP64
    (EMP_PREC_FP64) or float-float (EMP_PREC_MIXED, the residuals converted
    first); logl = -inf where the covariance is not positive definite.
-   EMP_E_UNSUPPORTED for a handle without a GP.  The log-posterior entries
-   compute the residuals themselves; this one serves callers with their own
-   mean model. */
+   EMP_E_UNSUPPORTED for a handle without a GP.  Uses (and on first need
+   allocates) the handle's GP row workspace, as emp_logpost does.  The
+   log-posterior entries compute the residuals themselves; this one serves
+   callers with their own mean model. */
 int emp_gp_logl(emp_handle* h, const double* theta, int B, const double* resid,
                 const double* err2, double* logl, int precision, void* stream);
 
