@@ -214,3 +214,52 @@ def test_create_batch_rejects_bad_input_before_touching_the_gpu(lib):
     h = C.c_void_p()
     assert lib.emp_create_batch(descs, C.byref(ds), C.byref(h)) == N.EMP_E_SIZE
     assert lib.emp_num_systems(None) == N.EMP_E_INVALID
+
+
+def test_create_rejects_bad_gp_and_hill_fields(lib, peg_arr):
+    """GP and Hill descriptor fields are checked before any device work."""
+    from tests.golden.cases import GP_KERNELS, model_51peg
+    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'])
+    ds, keep = _dataset(d.BJD, d.RV, d.eRV, d.Flag)
+    md = m.descriptor(); md.gp_kind[0] = 7                    # unknown term kind
+    rc, msg = _create(lib, md, ds)
+    assert rc == N.EMP_E_UNSUPPORTED and 'kind' in msg
+    md = m.descriptor(); md.gp_slot[0][1] = md.n_full         # parameter slot out of range
+    rc, msg = _create(lib, md, ds)
+    assert rc == N.EMP_E_INVALID and 'slot' in msg
+    md = m.descriptor(); md.gp_slot[0][4] = 0                 # unused parameter must be -1
+    assert _create(lib, md, ds)[0] == N.EMP_E_INVALID
+    md = m.descriptor(); md.gp_nterms = N.EMP_MAX_GP_TERMS + 1
+    assert _create(lib, md, ds)[0] == N.EMP_E_SIZE
+    md = m.descriptor()                                       # 5 rotation terms: 20 dimensions
+    md.gp_nterms = 5
+    for j in range(5):
+        md.gp_kind[j] = N.EMP_GP_GROT
+        for i in range(5):
+            md.gp_slot[j][i] = md.gp_slot[0][i]
+    rc, msg = _create(lib, md, ds)
+    assert rc == N.EMP_E_UNSUPPORTED and 'dimensions' in msg
+    md = m.descriptor(); md.ma_order = 1; md.ma_slot = 0; md.ma_global = 1
+    rc, msg = _create(lib, md, ds)
+    assert rc == N.EMP_E_UNSUPPORTED and 'MA' in msg
+    # Hill priors
+    m2, d2 = model_51peg(peg_arr, k=2, par=1, hill=1.1)
+    ds2, keep2 = _dataset(d2.BJD, d2.RV, d2.eRV, d2.Flag)
+    md = m2.descriptor(); md.hill_mask = 1 << 3               # over 3 planets, the model has 2
+    assert _create(lib, md, ds2)[0] == N.EMP_E_INVALID
+    md = m2.descriptor(); md.hill_mask = 1 << 1               # planet counts start at 2
+    assert _create(lib, md, ds2)[0] == N.EMP_E_INVALID
+    md = m2.descriptor(); md.hill_starmass = 0.0
+    assert _create(lib, md, ds2)[0] == N.EMP_E_INVALID
+    md = m2.descriptor(); md.kep_param[0] = 7                 # no PAE script for param. 7
+    md.kep_param[1] = 7
+    rc, msg = _create(lib, md, ds2)
+    assert rc == N.EMP_E_UNSUPPORTED and 'Hill' in msg
+
+
+def test_gp_batch_rejected_before_touching_the_gpu(lib, peg_arr):
+    from tests.golden.cases import GP_KERNELS, model_51peg
+    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'])
+    parts = [(d.BJD, d.RV, d.eRV, d.Flag)] * 2
+    rc, msg = _batch(lib, [m, m], parts)
+    assert rc == N.EMP_E_UNSUPPORTED and 'one-system' in msg
