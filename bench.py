@@ -45,10 +45,11 @@ WORKLOADS = {
 }
 SEED = 1234
 
-# DRAM bytes (read + write) of one stretch half-step launch, from the ncu
+# DRAM bytes (read + write) of the roofline's kernel per launch, from the ncu
 # captures summarised in profiles/ (k_logpost_mixed_c2_halfstep.md,
-# k_logpost_mixed_c3_ragged_stretch.md); None where no capture was taken
-NCU_TRAFFIC = {'c2': 607488, 'c3': 581037824}
+# k_logpost_mixed_c3_ragged_stretch.md; for gp the k_gp_prep + k_gp_ff pair of
+# k_gp_celerite_gp_sweep.md); None where no capture was taken
+NCU_TRAFFIC = {'c2': 607488, 'c3': 581037824, 'gp': 247542784}
 
 
 def parse():
