@@ -525,20 +525,21 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
     int pexp = 0;
     bool bad = !isfinite(asum_d);
     // one epoch of the recursion (inputs: this lane's U, V, phi and the row's
-    // residual and err2)
+    // residual and err2); products stay unnormalised where the next operation
+    // is an addition or another product (|lo| stays within ~2 ulp of hi)
     auto epoch = [&](int i, FF Uk, FF Vk, FF Pk, FF ri, FF ei) {
         FF Uj[M];
 #pragma unroll
         for (int j = 0; j < M; ++j) Uj[j] = ff_shfl(Uk, j, M);
         if (i > 0) {
-            const FF dw = ff_mulr(Dp, W);
+            const FF dw = ff_mul(Dp, W);
 #pragma unroll
             for (int j = 0; j < M; ++j) {
                 const FF Wj = ff_shfl(W, j, M);
                 const FF pj = ff_shfl(Pk, j, M);
-                S[j] = ff_mulr(ff_mulr(Pk, pj), ff_add(ff_mul(dw, Wj), S[j]));
+                S[j] = ff_mul(ff_mul(Pk, pj), ff_add(ff_mul(dw, Wj), S[j]));
             }
-            f = ff_mulr(Pk, ff_add(ff_mul(W, zp), f));
+            f = ff_mul(Pk, ff_add(ff_mul(W, zp), f));
         }
         // (S U)_k as a pairwise sum
         FF t[M];
@@ -549,7 +550,7 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
 #pragma unroll
             for (int j = 0; j + w < M; j += 2 * w) t[j] = ff_add(t[j], t[j + w]);
         const FF su = t[0];
-        FF p1 = ff_mulr(Uk, su), p2 = ff_mulr(Uk, f);
+        FF p1 = ff_mul(Uk, su), p2 = ff_mul(Uk, f);
 #pragma unroll
         for (int off = M / 2; off >= 1; off >>= 1) {
             p1 = ff_add(p1, ff_shfl_xor(p1, off, M));
@@ -560,11 +561,11 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
         const FF D = ff_add(ff_add(ei, asum), ff_neg(p1));
         bad = bad || !(D.hi > 0.f);
         const FF iD = ff_recip(D);
-        W = ff_mulr(ff_add(Vk, ff_neg(su)), iD);
+        W = ff_mul(ff_add(Vk, ff_neg(su)), iD);
         const FF z = ff_add(ri, ff_neg(p2));
-        quad = ff_add(quad, ff_mul(ff_mulr(z, z), iD));
+        quad = ff_add(quad, ff_mul(ff_mul(z, z), iD));
         // prod *= D, then its binary exponent moves into pexp (exact scaling)
-        prod = ff_mulr(prod, D);
+        prod = ff_mul(prod, D);
         {
             const int ex = ((__float_as_int(prod.hi) >> 23) & 0xff) - 127;
             const float sc = __int_as_float((127 - ex) << 23);
