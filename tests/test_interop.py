@@ -67,3 +67,12 @@ def test_rotation_term_names_follow_the_reference():
     assert [p.name for p in b] == ['Rotation Term period', 'Rotation Term sigma', 'Rotation Term Q0',
                                    'Rotation Term dQ', 'Rotation Term f']
     assert [p.gp_key for p in b] == ['sigma', 'period', 'Q0', 'dQ', 'f']
+
+
+def test_model_with_hill_from_reference_blocks(peg_arr):
+    m, d = model_51peg(peg_arr, k=3, par=1, hill=1.11)
+    frame = {'BJD': d.BJD, 'RV': d.RV, 'eRV': d.eRV, 'Flag': d.Flag}
+    d2 = data_from_frame(frame, common_t=d.common_t)
+    m2 = model_from_blocks([_ref_like(b) for b in m.blocks], d2)
+    assert bytes(m.descriptor()) == bytes(m2.descriptor())
+    assert m2.descriptor().hill_mask == (1 << 2) | (1 << 3)
