@@ -213,7 +213,9 @@ int validate_model(const emp_model_desc* m) {
     if (m->gp_nterms < 0 || m->gp_nterms > EMP_MAX_GP_TERMS)
         return fail(EMP_E_SIZE, "gp_nterms=%d outside [0, %d]", m->gp_nterms, EMP_MAX_GP_TERMS);
     if (m->gp_nterms > 0) {
-        if (m->ma_order > 0) return fail(EMP_E_UNSUPPORTED, "a GP likelihood with an MA model");
+        // a per-instrument MA under the reference quirk is a no-op (no MA on the device)
+        if (m->ma_order > 0 && (m->ma_global || !m->ma_quirk))
+            return fail(EMP_E_UNSUPPORTED, "a GP likelihood with an MA model");
         int dims = 0;
         for (int j = 0; j < m->gp_nterms; ++j) {
             const int kind = m->gp_kind[j];

@@ -443,8 +443,12 @@ class ReddModel:
         gp = [b for b in self.blocks if b.type_ == 'Celerite2']
         if len(gp) > 1:
             raise ValueError('one Celerite2 block per model')
-        if gp and any(b.type_ == 'MOAV' for b in self.blocks):
-            raise ValueError('a GP likelihood and a MOAV block cannot be combined on this path')
+        # the reference's per-instrument MOAV is a no-op (moav00.model:18-19), so
+        # with the quirk it leaves the GP's residuals alone; a live MA is not
+        # combined with the GP on this path
+        if gp and any(b.type_ == 'MOAV' and (b.is_global or not self.moav_reference_quirk)
+                      for b in self.blocks):
+            raise ValueError('a GP likelihood and a live MOAV block cannot be combined on this path')
         # the MOAV residual is taken after every mean-model block
         seen_moav = False
         for b in self.blocks:

@@ -124,6 +124,23 @@ def test_gp_with_moav_rejected(peg_arr):
     data = peg_data(peg_arr)
     with pytest.raises(ValueError, match='MOAV'):
         ReddModel([MOAVBlock(1, {'order': 1, 'global': True}), CeleriteBlock(GP_KERNELS['grot'])], data)
+    with pytest.raises(ValueError, match='MOAV'):
+        ReddModel([MOAVBlock(1, {'order': 1, 'global': False}), CeleriteBlock(GP_KERNELS['grot'])], data)
+
+
+def test_gp_with_quirk_moav_is_the_gp_alone(peg_arr):
+    # the reference's per-instrument MOAV is a no-op: with the quirk the GP
+    # likelihood equals that of the same model without the MOAV block
+    m0, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'])
+    mq, _ = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'], moav={'order': 1, 'global': False},
+                        quirk=True)
+    o0 = OracleRV(m0.spec(), d.as_dict())
+    oq = OracleRV(mq.spec(), d.as_dict())
+    th0 = np.array([4.231, 55.957, 1.769, 0.087, 0.061, 3.642, 2.961, 2.5, 2.5, 2.5, 2.5])
+    thq = np.concatenate([th0[:7], [0.1, 10.0], th0[7:]])     # MA coefficient and timescale
+    assert abs(oq.my_likelihood(thq) - o0.my_likelihood(th0)) <= 1e-12 * abs(o0.my_likelihood(th0))
+    md = mq.descriptor()
+    assert md.gp_nterms == 1 and md.ma_order == 1 and md.ma_quirk == 1
 
 
 def test_unknown_term_rejected():

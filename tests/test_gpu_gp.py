@@ -180,3 +180,22 @@ def test_gp_unsupported_paths(peg_arr, lib, cuda):
     from astroemperor_gb300.batch import BatchContext
     with pytest.raises(N.EmpError, match='one-system'):
         BatchContext([m, m], 'cuda:0')
+
+
+def test_gp_with_quirk_moav_on_device(peg_arr, lib, cuda):
+    """The reference's per-instrument MOAV is a no-op; with the quirk a GP model
+    carrying it evaluates like the same model without it."""
+    m0, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'])
+    mq, _ = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'], moav={'order': 1, 'global': False},
+                        quirk=True)
+    rng = np.random.default_rng(3)
+    th0 = _p0_near(m0, 1, 12, 4)[0]
+    thq = np.concatenate([th0[:, :7], np.tile([0.1, 10.0], (12, 1)), th0[:, 7:]], axis=1)
+    for prec in (N.EMP_PREC_FP64, N.EMP_PREC_MIXED):
+        a, _ = _eval(Context(m0, 'cuda:0'), th0, prec)
+        b, _ = _eval(Context(mq, 'cuda:0'), thq, prec)
+        np.testing.assert_allclose(b, a, rtol=1e-12)
+    o = OracleRV(mq.spec(), d.as_dict())
+    ref = np.array([o.my_likelihood(x) for x in thq])
+    a, _ = _eval(Context(mq, 'cuda:0'), thq, N.EMP_PREC_FP64)
+    np.testing.assert_allclose(a, ref, rtol=FP64_RTOL)
