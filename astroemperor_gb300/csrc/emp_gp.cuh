@@ -18,13 +18,14 @@
 //
 // k_logpost writes each valid row's residuals and err2 (epoch-major) and the
 // prior; k_gp_prep evaluates, for every (row, epoch) in parallel, the parts of
-// the recursion that do not depend on its state (the sincos and exp); k_gp
-// runs the sequential recursion in FP64 with one lane per state dimension and
-// finishes the mode: log-posterior rows, state slots, or the stretch move's
-// Metropolis test.  FP64 on this GPU issues one warp instruction per ~64
-// cycles per SM sub-partition, so the recursion is bound by the length of its
-// per-epoch FP64 chain: the transcendentals leave it for the parallel kernel,
-// the lanes share a row's S, and log det needs no log per epoch.
+// the recursion that do not depend on its state (the sincos and exp); the
+// recursion runs with one lane per state dimension -- k_gp in FP64, k_gp_ff in
+// float-float for the mixed precision -- and finishes the mode: log-posterior
+// rows, state slots, or the stretch move's Metropolis test.  FP64 on this GPU
+// issues one warp instruction per ~64 cycles per SM sub-partition, so the
+// transcendentals leave the sequential chain for the parallel kernel (and, in
+// the mixed precision, run in float-float on the FP32 pipes), the lanes share
+// a row's S, and log det needs no log per epoch.
 #pragma once
 
 #include "emp_kernels.cuh"
