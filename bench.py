@@ -532,10 +532,11 @@ def main():
                            'has no CUDA-core figure); compute-issue bound, not HBM or tensor',
             'fp64_peak_tflops': f64p.value / 1e12}
     if any(b.type_ == 'Celerite2' for b in model.blocks):
-        # the GP sweep's dominant kernel is k_gp (FP64 recursion, one thread
-        # per walker row): timed alone through emp_gp_logl on the half-step's
-        # rows and their residuals; the mixed k_logpost that writes those
-        # residuals is reported beside it
+        # the GP sweep's dominant kernels are k_gp_prep + k_gp_ff (the mixed
+        # celerite recursion, M lanes per walker row): timed alone through
+        # emp_gp_logl on the half-step's rows and their residuals (with the
+        # conversion of those rows to float-float pairs); the mixed k_logpost
+        # that writes the residuals in a sweep is reported beside it
         mod, e2 = ctx.model_eval(th_half)
         y = torch.as_tensor(data.RV, dtype=torch.float64, device=dev)
         rr = (y[None, :] - mod).t().contiguous()
@@ -555,8 +556,8 @@ def main():
                 'kernel_ms': g_ms,
                 'flop_per_row_epoch': Fg,
                 'peak_source': 'FP64 peak measured on this GPU by the library FMA probe',
-                'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp)',
-                              'kernel_ms_with_k_gp': k_ms, 'launch': roof['launch']}}
+                'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp_ff)',
+                              'kernel_ms_with_gp_kernels': k_ms, 'launch': roof['launch']}}
 
     # ---- end to end through the public sampler with host buffers
     s = s_mixed
