@@ -102,6 +102,7 @@ struct emp_handle {
     cudaStream_t own = nullptr;
     GraphCache gc;               // emp_pt_run
     GraphCache gch;              // emp_pt_run_host
+    cudaStream_t aux = nullptr;  // second stream of the host-state graph
     bool attr_done[2][4][6] = {};
     bool swap_attr = false;
     bool swap_attr_batch = false;
@@ -520,8 +521,17 @@ int check_state(const emp_handle* h, const emp_pt_state* st) {
     return EMP_OK;
 }
 
+// copy of the packed walker state back to the host, overlapped with the swap
+// and record kernels (emp_pt_run_host)
+struct HostCopy {
+    void* host;
+    size_t bytes;
+    cudaStream_t aux;
+    cudaEvent_t ev[2];
+};
+
 int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec,
-                  cudaStream_t s, int* nkern) {
+                  cudaStream_t s, int* nkern, const HostCopy* hc = nullptr) {
     int rc;
     int kcount = 0;
     const bool batch = h->n_sys > 1;
@@ -551,6 +561,15 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
             if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr, !batch))) return rc;
             kcount += h->gp_M > 0 ? 3 : 1;
         }
+    }
+    if (hc) {
+        // the walker state is final after the stretch moves (the swaps
+        // exchange slot ids, the record only reads it): copy it back on a
+        // second stream while the swap and record kernels run
+        CUDA_TRY(cudaEventRecord(hc->ev[0], s));
+        CUDA_TRY(cudaStreamWaitEvent(hc->aux, hc->ev[0], 0));
+        CUDA_TRY(cudaMemcpyAsync(hc->host, st->theta, hc->bytes, cudaMemcpyDeviceToHost, hc->aux));
+        CUDA_TRY(cudaEventRecord(hc->ev[1], hc->aux));
     }
     SwapArgs S{};
     S.T = st->ntemps; S.W = st->nwalkers; S.D = st->ndim; S.nsteps = st->nsteps;
@@ -640,6 +659,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
         ++kcount;
         CUDA_TRY(cudaGetLastError());
     }
+    if (hc) CUDA_TRY(cudaStreamWaitEvent(s, hc->ev[1], 0));    // join the copy back
     if (nkern) *nkern = kcount;
     return EMP_OK;
 }
@@ -915,6 +935,7 @@ int emp_destroy(emp_handle* h) {
     h->gc.reset();
     h->gch.reset();
     if (h->own) cudaStreamDestroy(h->own);
+    if (h->aux) cudaStreamDestroy(h->aux);
     if (h->dbuf) cudaFree(h->dbuf);
     if (h->gp_buf) cudaFree(h->gp_buf);
     delete h;
@@ -1212,7 +1233,29 @@ int capture_sweep(emp_handle* h, GraphCache& gc, const emp_pt_state* st, const e
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
         h->swap_attr_batch = true;
     }
-    CUDA_TRY(cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal));
+    HostCopy hc{};
+    if (host) {
+        if (!h->aux) CUDA_TRY(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+        hc.host = host;
+        hc.bytes = host_bytes;
+        hc.aux = h->aux;
+        CUDA_TRY(cudaEventCreateWithFlags(&hc.ev[0], cudaEventDisableTiming));
+        cudaError_t e1 = cudaEventCreateWithFlags(&hc.ev[1], cudaEventDisableTiming);
+        if (e1 != cudaSuccess) {
+            cudaEventDestroy(hc.ev[0]);
+            return fail(EMP_E_CUDA, "cudaEventCreate: %s", cudaGetErrorString(e1));
+        }
+    }
+    auto drop_events = [&]() {
+        if (host) { cudaEventDestroy(hc.ev[0]); cudaEventDestroy(hc.ev[1]); }
+    };
+    {
+        cudaError_t e0 = cudaStreamBeginCapture(ls, cudaStreamCaptureModeThreadLocal);
+        if (e0 != cudaSuccess) {
+            drop_events();
+            return fail(EMP_E_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e0));
+        }
+    }
     int nk = 0;
     int64_t before = g_launches.load();
     rc = EMP_OK;
@@ -1220,14 +1263,11 @@ int capture_sweep(emp_handle* h, GraphCache& gc, const emp_pt_state* st, const e
         cudaError_t e = cudaMemcpyAsync(st->theta, host, host_bytes, cudaMemcpyHostToDevice, ls);
         if (e != cudaSuccess) rc = fail(EMP_E_CUDA, "state copy in: %s", cudaGetErrorString(e));
     }
-    if (!rc) rc = enqueue_sweep(h, st, has_rec ? &rcopy : nullptr, ls, &nk);
-    if (!rc && host) {
-        cudaError_t e = cudaMemcpyAsync(host, st->theta, host_bytes, cudaMemcpyDeviceToHost, ls);
-        if (e != cudaSuccess) rc = fail(EMP_E_CUDA, "state copy out: %s", cudaGetErrorString(e));
-    }
+    if (!rc) rc = enqueue_sweep(h, st, has_rec ? &rcopy : nullptr, ls, &nk, host ? &hc : nullptr);
     g_launches.store(before);   // captured, not launched
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamEndCapture(ls, &graph);
+    drop_events();
     if (rc) {
         if (graph) cudaGraphDestroy(graph);
         return rc;

@@ -324,7 +324,8 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st,
    the state packed like the device buffers of `st` (theta rows by slot, then
    logl, then logprior; st->logl and st->logprior must follow st->theta that
    way), is copied in, swept and copied back, all inside one CUDA graph
-   cached for (st, rec, host_state).  Launches only: the caller synchronises
+   cached for (st, rec, host_state); the copy back starts after the stretch
+   moves, on a second stream, while the swap and record kernels run.  Launches only: the caller synchronises
    `stream` before reading host_state.  One-system handles. */
 int emp_pt_run_host(emp_handle* h, const emp_pt_state* st,
                     const emp_pt_record* rec, void* host_state, void* stream);
