@@ -42,6 +42,8 @@ WORKLOADS = {
           '1-4 Keplerians, 1-3 instruments',
     'gp': 'RV PT sweep with a celerite GP likelihood: 3 Keplerians, 2 instruments, N=1024, '
           'GonzRotationTerm GP (4 hyperparameters)',
+    'c4grad': 'log-posterior gradients (adjoint kernel) of 65536 multistart points: 5 Keplerians, '
+              '3 instruments, N=4096, per-instrument MA(1)',
 }
 SEED = 1234
 
@@ -163,7 +165,10 @@ def run_reference(args):
         return 0
     if args.config == 'c3':
         return run_reference_ragged(args)
-    model, data, setup, truth = synth.build_model(args.config, seed=SEED)
+    grad = args.config == 'c4grad'
+    model, data, setup, truth = synth.build_model('c4' if grad else args.config, seed=SEED)
+    # a gradient by forward differences costs ndim + 1 log-posterior evaluations
+    per_unit = (model.ndim__ + 1) if grad else 1
     lim = model.limits_free()
     rng = np.random.default_rng(7)
     nc = os.cpu_count() or 1
@@ -181,7 +186,7 @@ def run_reference(args):
             sel = th[:batch]
         el = timer.step(sel)
         if i >= args.warmup:
-            vals.append(len(sel) * data.ndata / el)
+            vals.append(len(sel) * data.ndata / el / per_unit)
     timer.close()
     v = float(np.median(vals)) if vals else float('nan')
     line = {'metric': METRIC, 'impl': 'reference', 'value': v, 'unit': 'evals*epochs/s',
@@ -193,7 +198,9 @@ def run_reference(args):
             'cpu_baseline': {'value': v, 'unit': 'evals*epochs/s', 'cores': nc, 'kind': 'port',
                              'sample': f'per step {batch} reference-faithful walker evaluations '
                                        f'(my_prior+my_likelihood, numpy over epochs) mapped over '
-                                       f'multiprocessing.Pool({nc}); median over steps'},
+                                       f'multiprocessing.Pool({nc}); median over steps'
+                                       + (f'; a gradient by forward differences counted as {per_unit} '
+                                          f'evaluations' if grad else '')},
             'e2e': {'value': v, 'unit': 'evals*epochs/s', 'h2d_bytes_per_step': 0,
                     'd2h_bytes_per_step': 0}}
     print(json.dumps(line))
@@ -413,12 +420,126 @@ def run_reference_ragged(args):
     return 0
 
 
+def main_grad(args):
+    """C4: one step = the log-posterior and its gradient at 65536 points (the
+    multistart MAP's batch) through the adjoint kernel; units = points x epochs."""
+    import ctypes as C
+    import torch
+    from astroemperor_gb300 import _native as N
+    from astroemperor_gb300 import synth
+    from astroemperor_gb300.engine import Context
+    from astroemperor_gb300.replicas import job_rate
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.device('cuda', local if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    model, data, setup, truth = synth.build_model('c4', seed=SEED + rank)
+    n, D = data.ndata, model.ndim__
+    B = 65536
+    lim = model.limits_free()
+    rng = np.random.default_rng(SEED + rank)
+    th = np.clip(truth + 0.02 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(B, D)), lim[:, 0], lim[:, 1])
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        # the reference has no gradient: its CPU path would take D+1 log-posterior
+        # evaluations per point (forward differences)
+        v, ne, el, nc = cpu_baseline(model, data, truth, args.cpu_seconds)
+        cpu = {'value': v / (D + 1), 'unit': 'evals*epochs/s', 'cores': nc, 'kind': 'port',
+               'sample': f'{ne} reference-faithful log-posterior evaluations (my_prior+my_likelihood '
+                         f'per point, numpy over epochs, Pool({nc})) in {el:.1f} s; a gradient by forward '
+                         f'differences costs {D + 1} of them'}
+    lib = N.load()
+    ctx = Context(model, str(dev))
+    t = torch.as_tensor(th, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    steps = min(args.steps, 100)
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            out = ctx.logpost_grad(t, stream=stream)
+    stream.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    clocks = ClockSampler(dev.index or 0)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = lib.emp_launch_count()
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+            out = ctx.logpost_grad(t, stream=stream)
+            evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = lib.emp_launch_count() - l0
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    units = B * n
+    _, t_all, value = job_rate(units * steps, ms / 1e3, device=dev)
+    F = 58 * model.kplan__ + 10 + 7 * ma_order(model)
+    Fg = 3 * F                                                  # forward + adjoint
+    import ctypes as Cc
+    f32, f64p = Cc.c_double(), Cc.c_double()
+    N.call('emp_probe_peaks', Cc.byref(f32), Cc.byref(f64p), stream.cuda_stream)
+    k_ms = ms / steps
+    achieved = Fg * units / (k_ms * 1e-3) / 1e12
+    peak32 = f32.value / 1e12
+    roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s', 'frac': achieved / peak32,
+            'traffic': None, 'algorithmic_bytes': n * 25 + B * (8 * D * 3 + 16),
+            'kernel': 'k_grad<Q=1> (log-posterior and its adjoint gradient)', 'kernel_ms': k_ms,
+            'flop_per_eval_epoch': Fg,
+            'peak_source': 'measured on this GPU by the library FMA probe (MEASURED_PEAKS.json has no '
+                           'CUDA-core figure); F counts forward + adjoint as 3 x the forward FLOP'}
+    # end to end: points in from pinned host memory, gradients out
+    h_th = torch.as_tensor(th, dtype=torch.float64).pin_memory()
+    h_g = torch.empty(B, D, dtype=torch.float64).pin_memory()
+    h_l = torch.empty(B, dtype=torch.float64).pin_memory()
+    e2e_steps = min(steps, 20)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            t.copy_(h_th, non_blocking=True)
+            ll, lp, gl, gp = ctx.logpost_grad(t, stream=stream)
+            h_g.copy_(gl, non_blocking=True)
+            h_l.copy_(ll, non_blocking=True)
+        stream.synchronize()
+    e2e_t = time.perf_counter() - t0
+    e2e = {'value': units * e2e_steps / e2e_t, 'unit': 'evals*epochs/s', 'h2d_bytes_per_step': B * D * 8,
+           'd2h_bytes_per_step': B * (D + 1) * 8,
+           'api': 'Context.logpost_grad (points from pinned host memory in, gradient of logL and logL out)'}
+    if rank == 0:
+        line = {'metric': METRIC, 'value': value, 'unit': 'evals*epochs/s', 'n_gpus': world,
+                'steps': steps, 'warmup': max(args.warmup, 3), 'ms_per_step': k_ms,
+                'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+                'dtype': 'f32+f64 (mixed)', 'data': 'synthetic (seeded generator with the configuration shapes)',
+                'config': {'workload': WORKLOADS['c4grad'], 'points': B, 'epochs': n, 'ndim': D,
+                           'planets': model.kplan__, 'instruments': data.nins, 'ma_order': ma_order(model),
+                           'parameterisation': 1, 'seed': SEED,
+                           'l2': 'flushed between timed steps (256 MiB write, outside the timed events)'},
+                'fp64_plain': None, 'roofline': roof, 'cpu_baseline': cpu, 'e2e': e2e, 'clocks': clk,
+                'gpu_launches': int(launches)}
+        if cpu:
+            line['gpu_over_cpu'] = value / cpu['value']
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
         return run_reference(args)
     if args.config == 'c3':
         return main_ragged(args)
+    if args.config == 'c4grad':
+        return main_grad(args)
 
     import torch
     from astroemperor_gb300 import _native as N
