@@ -15,6 +15,9 @@ Writes
                        with math_utils.cps, executed from the reference's
                        files) at seeded planet sets, to pin the oracle's
                        restatement
+  gp_kat.npz        -- oracle (logL, logprior) of the celerite GP cases (the
+                       recursion, checked against the dense definition when
+                       written), to keep the GP oracle stable across machines
 """
 from __future__ import annotations
 
@@ -49,6 +52,34 @@ def main(ref_root):
     np.savez_compressed(os.path.join(HERE, 'logpost_kat.npz'), **out)
     print('wrote', sorted(k for k in out if k.endswith('__logl')))
     hill_fixture(ref_root)
+    gp_fixture(arr)
+
+
+def gp_fixture(arr):
+    """Oracle GP log-likelihoods of gp_case_models, each checked against the
+    dense-Cholesky definition before it is written."""
+    from oracle import gp
+    from tests.golden.cases import gp_case_models
+    out = {}
+    for name, (m, d, th) in gp_case_models(arr).items():
+        o = OracleRV(m.spec(), d.as_dict())
+        (terms,) = [b['gp_terms'] for b in o.blocks if b['type'] == 'Celerite2']
+        lp = np.array([o.my_prior(t) for t in th])
+        ll = np.full(len(th), -np.inf)
+        for i, t in enumerate(th):
+            if not np.isfinite(lp[i]):
+                continue
+            ll[i] = o.my_likelihood(t)
+            model, err2 = o.my_model(t)
+            full = o.full_theta(t)
+            co = gp.coefficients([(k, [full[j] for j in sl]) for k, sl in terms])
+            dense = gp.dense_loglike(o.X_, o.Y_ - model, err2, co)
+            assert abs(ll[i] - dense) <= 1e-10 * abs(dense), (name, i)
+        out[f'{name}__theta'] = th
+        out[f'{name}__logl'] = ll
+        out[f'{name}__logprior'] = lp
+    np.savez_compressed(os.path.join(HERE, 'gp_kat.npz'), **out)
+    print('gp_kat:', sorted(k for k in out if k.endswith('__logl')))
 
 
 def hill_fixture(ref_root):

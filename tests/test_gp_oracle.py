@@ -173,3 +173,18 @@ def test_compiled_recursion_equals_python(kind, p):
     bad[0] = [-50.0] + list(bad[0])[1:]
     assert gp.semisep_loglike(t, r, diag, bad) == -np.inf
     assert gp.semisep_loglike_c(t, r, diag, bad) == -np.inf
+
+
+def test_oracle_matches_gp_fixture(peg_arr):
+    """The committed GP known-answer vectors (tests/golden/make_golden.py) keep
+    the GP oracle stable across machines and edits."""
+    kat = np.load('tests/golden/gp_kat.npz')
+    cases = gp_case_models(peg_arr)
+    for name, (m, d, th) in cases.items():
+        np.testing.assert_array_equal(th, kat[f'{name}__theta'])
+        o = OracleRV(m.spec(), d.as_dict())
+        lp = np.array([o.my_prior(t) for t in th])
+        np.testing.assert_allclose(lp, kat[f'{name}__logprior'], rtol=1e-13, atol=1e-13)
+        fin = np.isfinite(lp)
+        ll = np.array([o.my_likelihood(t) for t in th[fin]])
+        np.testing.assert_allclose(ll, kat[f'{name}__logl'][fin], rtol=1e-12, err_msg=name)
