@@ -18,6 +18,14 @@ Writes
   gp_kat.npz        -- oracle (logL, logprior) of the celerite GP cases (the
                        recursion, checked against the dense definition when
                        written), to keep the GP oracle stable across machines
+  template_kat.npz  -- my_model / my_likelihood of the known-answer model cases
+                       evaluated by the reference's own model templates
+                       (support/models/*.model, support/likelihoods/00.like),
+                       assembled in the order of emp_model.py:706-781, and its
+                       prior templates (support/priors/*.prior) at seeded
+                       points; the Kepler equation (kepler.py, absent) is
+                       solved by the oracle's solver, so these pin everything
+                       else of the oracle's model, likelihood and priors
 """
 from __future__ import annotations
 
@@ -53,6 +61,104 @@ def main(ref_root):
     print('wrote', sorted(k for k in out if k.endswith('__logl')))
     hill_fixture(ref_root)
     gp_fixture(arr)
+    template_fixture(ref_root, arr)
+
+
+def _template_model_source(model, support):
+    """The reference's my_model text for a model of this package's layer:
+    each block's template formatted with the block's write_args (block_repo.py),
+    in the assembly order of emp_model.py:706-781."""
+    def tpl(name):
+        return open(os.path.join(support, 'models', name)).read()
+    nins = model.data.nins
+    src = ['def my_model(theta):',
+           '    for a in A_:',
+           '        theta = np.insert(theta, a, mod_fixed_[a])',
+           '    model0 = np.zeros(ndat)',
+           '    err20 = YERR_ ** 2']
+    for b in model.blocks:
+        sl = b.slice
+        if b.type_ == 'Keplerian':
+            src.append(tpl(f'kep0{b.parameterisation}.model').format(sl))
+        elif b.type_ == 'Offset':
+            for k in range(1, nins + 1):
+                src.append(tpl('offset00.model').format(k, sl))
+        elif b.type_ in ('Sinusoid', 'MagneticCycle', 'Acceleration'):
+            name = {'Sinusoid': 'sinusoid00.model', 'MagneticCycle': 'magneticcycle00.model',
+                    'Acceleration': 'acc.model'}[b.type_]
+            src.append(tpl(name).format(sl))
+        elif b.type_ == 'MOAV':
+            src.append('    residuals = Y_ - model0')
+            if b.is_global:
+                src.append(tpl('moav01.model').format(nins, sl, b.moav))
+            else:
+                for k in range(1, nins + 1):
+                    src.append(tpl('moav00.model').format(k, sl, b.moav))
+        elif b.type_ == 'Jitter':
+            for k in range(1, nins + 1):
+                src.append(tpl('jitter00.model').format(k, sl))
+        else:
+            raise ValueError(b.type_)
+    src.append('    return model0, err20')
+    return '\n'.join(src) + '\n'
+
+
+def template_fixture(ref_root, arr):
+    """The reference's own templates on the known-answer cases (see module doc)."""
+    import types
+    from oracle.rv import kepler_solve, PRIORS, check_prargs
+    from tests.golden.cases import kat_case_models
+    support = os.path.join(ref_root, 'src', 'astroemperor', 'support')
+    like_src = open(os.path.join(support, 'likelihoods', '00.like')).read()
+    out = {}
+    for name, (m, d, th) in kat_case_models(arr).items():
+        if m.moav_reference_quirk is False and any(b.type_ == 'MOAV' and not b.is_global for b in m.blocks):
+            continue        # the documented per-instrument MA is this package's, not a reference template
+        g = {'np': np, 'kepler': types.SimpleNamespace(solve=kepler_solve),
+             'X_': d.BJD, 'Y_': d.RV, 'YERR_': d.eRV, 'ndat': d.ndata,
+             'A_': list(m.A_), 'mod_fixed_': m.mod_fixed}
+        for k in range(1, d.nins + 1):
+            g[f'mask{k}'] = d.Flag == k
+            g[f'ndat{k}'] = int(np.sum(d.Flag == k))
+        exec(_template_model_source(m, support), g)
+        exec(like_src, g)
+        pick = np.linspace(0, len(th) - 1, 6).astype(int)
+        mod, err, ll = [], [], []
+        with np.errstate(all='ignore'):
+            for i, t in enumerate(th):
+                a, b = g['my_model'](t)
+                if i in pick:
+                    mod.append(a)
+                    err.append(b)
+                ll.append(g['my_likelihood'](t))
+        out[f'{name}__pick'] = pick
+        out[f'{name}__model'] = np.array(mod)
+        out[f'{name}__err2'] = np.array(err)
+        out[f'{name}__logl'] = np.array(ll)
+    # prior templates at seeded points
+    rng = np.random.default_rng(99)
+    for prior in ('Uniform', 'Normal', 'Jeffreys', 'Beta'):
+        from scipy.stats import beta as betapdf          # the reference's model dependency (emp.py:428)
+        gp_ = {'np': np, 'betapdf': betapdf}
+        exec(open(os.path.join(support, 'priors', f'{prior}.prior')).read(), gp_)
+        fn = gp_[prior]
+        xs, vals = [], []
+        for _ in range(200):
+            lo = rng.uniform(0.01, 1.0)
+            hi = lo + rng.uniform(0.1, 3.0)
+            lim = [lo, hi] if prior != 'Beta' else [0.0, 1.0]
+            x = rng.uniform(lim[0] - 0.2, lim[1] + 0.2)
+            pr = {'Normal': [rng.uniform(lo, hi), rng.uniform(0.1, 1.0)], 'Beta': [rng.uniform(0.5, 3.0),
+                  rng.uniform(0.5, 3.0)]}.get(prior)
+            args = check_prargs(prior, lim, pr)
+            with np.errstate(all='ignore'):
+                v = fn(x, lim, args)
+            xs.append([x, lim[0], lim[1]] + (list(pr) if pr else [np.nan, np.nan]))
+            vals.append(v)
+        out[f'prior_{prior}__in'] = np.array(xs)
+        out[f'prior_{prior}__value'] = np.array(vals, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, 'template_kat.npz'), **out)
+    print('template_kat:', sorted(k for k in out if k.endswith('__logl')))
 
 
 def gp_fixture(arr):

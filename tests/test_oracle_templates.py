@@ -1,0 +1,62 @@
+"""The oracle against the reference's own code: my_model / my_likelihood of the
+known-answer cases as the reference's model templates compute them, and its
+prior templates (tests/golden/template_kat.npz, written by
+tests/golden/make_golden.py from support/models/*.model,
+support/likelihoods/00.like and support/priors/*.prior; the Kepler equation,
+a third-party call absent here, solved by the oracle's solver in both).
+
+Tolerances: model and err2 relative 1e-13 (the same operations; numpy's
+pairwise sums and the oracle's vectorised forms differ in the last bits),
+logL relative 1e-12, priors exact to 1e-13.
+"""
+import numpy as np
+import pytest
+
+from oracle.rv import OracleRV, PRIORS, check_prargs
+from tests.golden.cases import kat_case_models
+
+
+@pytest.fixture(scope='module')
+def tkat():
+    return np.load('tests/golden/template_kat.npz')
+
+
+def test_oracle_model_and_likelihood_equal_reference_templates(peg_arr, tkat):
+    cases = kat_case_models(peg_arr)
+    names = sorted({k.split('__')[0] for k in tkat.files if k.endswith('__logl')})
+    assert len(names) >= 14
+    for name in names:
+        m, d, th = cases[name]
+        o = OracleRV(m.spec(), d.as_dict())
+        pick = tkat[f'{name}__pick']
+        with np.errstate(all='ignore'):
+            for j, i in enumerate(pick):
+                mod, err2 = o.my_model(th[i])
+                ref_m, ref_e = tkat[f'{name}__model'][j], tkat[f'{name}__err2'][j]
+                fin = np.isfinite(ref_m)
+                np.testing.assert_allclose(mod[fin], ref_m[fin], rtol=1e-13, atol=1e-11, err_msg=name)
+                np.testing.assert_allclose(err2, ref_e, rtol=1e-13, err_msg=name)
+            ll = np.array([o.my_likelihood(t) for t in th])
+        ref = tkat[f'{name}__logl']
+        fin = np.isfinite(ref)
+        assert fin.sum() >= 10, name
+        np.testing.assert_allclose(ll[fin], ref[fin], rtol=1e-12, err_msg=name)
+
+
+@pytest.mark.parametrize('prior', ['Uniform', 'Normal', 'Jeffreys', 'Beta'])
+def test_oracle_priors_equal_reference_templates(tkat, prior):
+    xin = tkat[f'prior_{prior}__in']
+    want = tkat[f'prior_{prior}__value']
+    fn = PRIORS[prior]
+    got = []
+    for row in xin:
+        x, lo, hi = row[:3]
+        pr = None if np.isnan(row[3]) else [row[3], row[4]]
+        args = check_prargs(prior, [lo, hi], pr)
+        with np.errstate(all='ignore'):
+            got.append(fn(x, [lo, hi], args))
+    got = np.array(got, dtype=np.float64)
+    fin = np.isfinite(want)
+    assert np.array_equal(np.isfinite(got), fin)
+    assert fin.sum() > 20 and (~fin).sum() > 5
+    np.testing.assert_allclose(got[fin], want[fin], rtol=1e-13, atol=1e-13)
