@@ -103,13 +103,78 @@ def _template_model_source(model, support):
     return '\n'.join(src) + '\n'
 
 
+def _reference_check_prargs(src_dir):
+    """The reference's prargs normaliser (emp_model.py, Parameter_Block
+    _check_prargs / _check_additional_prargs), taken from its source and run
+    on duck-typed parameters: returns f(params) normalising in place."""
+    import ast
+    from scipy.stats import norm
+    text = open(os.path.join(src_dir, 'emp_model.py')).read()
+    tree = ast.parse(text)
+    fn = None
+    for node in ast.walk(tree):
+        if isinstance(node, ast.FunctionDef) and node.name == '_check_prargs':
+            fn = node
+            break
+    code = ast.get_source_segment(text, fn)
+    lines = code.split('\n')
+    indent = len(lines[0]) - len(lines[0].lstrip())
+    code = '\n'.join(l[indent:] for l in lines)
+    g = {'np': np, 'norm': norm}
+    exec(code, g)
+    return lambda params: g['_check_prargs'](list(params))
+
+
+def _template_prior_source(model, src_dir, normalise):
+    """The reference's my_prior text (emp.py:182-254) for a model of this
+    package's layer: one prior call per free parameter with the normalised
+    prargs, the block's -inf exit, then the derived priors (Amp, Ecc, Hill)."""
+    import copy
+    support = os.path.join(src_dir, 'support')
+    C_ = list(model.C_)
+    out = ['def my_prior(theta):', '    for a in A_:', '        theta = np.insert(theta, a, mod_fixed_[a])',
+           '    lp = 0.']
+    count = 0
+    for b in model.blocks:
+        free = [copy.copy(p) for p in b if p.fixed is None]
+        normalise(free)
+        for p in free:
+            out.append(f'    lp += {p.prior}(theta[{C_[count]}], {p.limits}, {p.prargs})')
+            count += 1
+        out.append('    if lp == -np.inf:\n        return lp')
+        extra = [copy.copy(p) for p in getattr(b, 'additional_parameters', []) if getattr(p, 'has_prior', False)]
+        normalise(extra)
+        for p in extra:
+            if p.name[:3] == 'Amp':
+                out.append(f'    x = theta[{b.slice}][1]**2 + theta[{b.slice}][2]**2')
+            elif p.name[:3] == 'Ecc':
+                out.append(f'    x = theta[{b.slice}][3]**2 + theta[{b.slice}][4]**2')
+            elif p.name == 'Hill' and p.prargs[0] > 1:
+                out.append(f'    b_len = {len(b)}\n    kplanets = {p.prargs[0]}')
+                out.append(open(os.path.join(support, 'PAE', f'0{b.parameterisation}.pae')).read())
+            else:
+                continue
+            out.append(f'    lp += {p.prior}(x, {p.limits}, {p.prargs})')
+    out.append('    return lp')
+    return '\n'.join(out) + '\n'
+
+
 def template_fixture(ref_root, arr):
     """The reference's own templates on the known-answer cases (see module doc)."""
     import types
     from oracle.rv import kepler_solve, PRIORS, check_prargs
     from tests.golden.cases import kat_case_models
-    support = os.path.join(ref_root, 'src', 'astroemperor', 'support')
+    import importlib.util
+    from scipy.stats import beta as betapdf          # the reference's model dependency (emp.py:428)
+    src_dir = os.path.join(ref_root, 'src', 'astroemperor')
+    support = os.path.join(src_dir, 'support')
     like_src = open(os.path.join(support, 'likelihoods', '00.like')).read()
+    normalise = _reference_check_prargs(src_dir)
+    spec = importlib.util.spec_from_file_location('_ref_math_utils', os.path.join(src_dir, 'math_utils.py'))
+    mu = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mu)
+    prior_defs = ''.join(open(os.path.join(support, 'priors', f)).read() + '\n'
+                         for f in sorted(os.listdir(os.path.join(support, 'priors'))))
     out = {}
     for name, (m, d, th) in kat_case_models(arr).items():
         if m.moav_reference_quirk is False and any(b.type_ == 'MOAV' and not b.is_global for b in m.blocks):
@@ -122,6 +187,9 @@ def template_fixture(ref_root, arr):
             g[f'ndat{k}'] = int(np.sum(d.Flag == k))
         exec(_template_model_source(m, support), g)
         exec(like_src, g)
+        g.update({'betapdf': betapdf, 'cps': mu.cps})
+        exec(prior_defs, g)
+        exec(_template_prior_source(m, src_dir, normalise), g)
         pick = np.linspace(0, len(th) - 1, 6).astype(int)
         mod, err, ll = [], [], []
         with np.errstate(all='ignore'):
@@ -135,6 +203,8 @@ def template_fixture(ref_root, arr):
         out[f'{name}__model'] = np.array(mod)
         out[f'{name}__err2'] = np.array(err)
         out[f'{name}__logl'] = np.array(ll)
+        with np.errstate(all='ignore'):
+            out[f'{name}__logprior'] = np.array([g['my_prior'](t) for t in th], dtype=np.float64)
     # prior templates at seeded points
     rng = np.random.default_rng(99)
     for prior in ('Uniform', 'Normal', 'Jeffreys', 'Beta'):

@@ -1,13 +1,15 @@
-"""The oracle against the reference's own code: my_model / my_likelihood of the
-known-answer cases as the reference's model templates compute them, and its
-prior templates (tests/golden/template_kat.npz, written by
+"""The oracle against the reference's own code: my_model / my_likelihood /
+my_prior of the known-answer cases as the reference's templates compute them
+(my_prior assembled as emp.py:182-254 writes it, with the reference's own
+prargs normaliser and Hill/PAE code), and its prior templates
+(tests/golden/template_kat.npz, written by
 tests/golden/make_golden.py from support/models/*.model,
 support/likelihoods/00.like and support/priors/*.prior; the Kepler equation,
 a third-party call absent here, solved by the oracle's solver in both).
 
 Tolerances: model and err2 relative 1e-13 (the same operations; numpy's
 pairwise sums and the oracle's vectorised forms differ in the last bits),
-logL relative 1e-12, priors exact to 1e-13.
+logL relative 1e-12, priors exact to 1e-13, my_prior bit for bit.
 """
 import numpy as np
 import pytest
@@ -60,3 +62,18 @@ def test_oracle_priors_equal_reference_templates(tkat, prior):
     assert np.array_equal(np.isfinite(got), fin)
     assert fin.sum() > 20 and (~fin).sum() > 5
     np.testing.assert_allclose(got[fin], want[fin], rtol=1e-13, atol=1e-13)
+
+
+def test_oracle_my_prior_equals_reference_assembly(peg_arr, tkat):
+    cases = kat_case_models(peg_arr)
+    names = sorted({k.split('__')[0] for k in tkat.files if k.endswith('__logprior')})
+    assert '51peg_k3_hill_p0' in names and '51peg_k1_p7' in names
+    for name in names:
+        m, d, th = cases[name]
+        o = OracleRV(m.spec(), d.as_dict())
+        with np.errstate(all='ignore'):
+            lp = np.array([o.my_prior(t) for t in th])
+        ref = tkat[f'{name}__logprior']
+        np.testing.assert_array_equal(np.isfinite(lp), np.isfinite(ref), err_msg=name)
+        fin = np.isfinite(ref)
+        np.testing.assert_array_equal(lp[fin], ref[fin], err_msg=name)
