@@ -26,6 +26,10 @@ Writes
                        points; the Kepler equation (kepler.py, absent) is
                        solved by the oracle's solver, so these pin everything
                        else of the oracle's model, likelihood and priors
+  smartsetter_kat.json -- default limits / priors / prargs of every block type
+                       as the reference's SmartSetter methods (block_repo.py,
+                       run from its source on a small column shim) set them
+                       for the 51 Peg data and the two-instrument C2 data
 """
 from __future__ import annotations
 
@@ -39,7 +43,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle.rv import OracleRV, preprocess  # noqa: E402
-from tests.golden.cases import kat_cases  # noqa: E402
+from tests.golden.cases import kat_cases, peg_data  # noqa: E402
 
 
 def main(ref_root):
@@ -62,6 +66,90 @@ def main(ref_root):
     hill_fixture(ref_root)
     gp_fixture(arr)
     template_fixture(ref_root, arr)
+    smartsetter_fixture(ref_root, arr)
+
+
+class _Col:
+    """The few pandas Series operations SmartSetter uses."""
+
+    def __init__(self, v):
+        self.v = np.asarray(v, dtype=float)
+
+    def std(self, ddof=1):
+        return float(np.std(self.v, ddof=ddof))
+
+    def max(self):
+        return float(np.max(self.v))
+
+    def min(self):
+        return float(np.min(self.v))
+
+    def abs(self):
+        return _Col(np.abs(self.v))
+
+    def __eq__(self, other):
+        return self.v == other
+
+
+class _Frame:
+    def __init__(self, cols):
+        self.cols = {k: np.asarray(v) for k, v in cols.items()}
+
+    def __getitem__(self, key):
+        if isinstance(key, str):
+            return _Col(self.cols[key])
+        return _Frame({c: v[key] for c, v in self.cols.items()})
+
+
+def smartsetter_fixture(ref_root, arr):
+    """The reference's SmartSetter limit methods run from block_repo.py's source."""
+    import ast
+    import json
+    import types
+    from astroemperor_gb300 import synth
+    text = open(os.path.join(ref_root, 'src', 'astroemperor', 'block_repo.py')).read()
+    tree = ast.parse(text)
+    cls = next(n for n in ast.walk(tree) if isinstance(n, ast.ClassDef) and n.name == 'SmartSetter')
+    names = ['__init__', 'set_Keplerian', 'set_Offset', 'set_Jitter', 'set_MOAV', 'set_Acceleration',
+             'set_Sinusoid', 'set_MagneticCycle']
+    parts = [ast.get_source_segment(text, n) for n in cls.body
+             if isinstance(n, ast.FunctionDef) and n.name in names]
+    src = 'class RefSmartSetter(object):\n' + '\n'.join('    ' + l for p in parts for l in p.split('\n'))
+    g = {'np': np}
+    exec(src, g)
+    Ref = g['RefSmartSetter']
+    # the additional-parameter helpers only attach derived parameters
+    Ref.ecc_w_add_additional = lambda self, b, **kw: None
+    Ref.per_add_additional = lambda self, b, **kw: None
+
+    def clean(x):
+        if isinstance(x, (list, tuple)):
+            return [clean(v) for v in x]
+        if x is None:
+            return None
+        return float(x)
+
+    out = {}
+    _, d2, _, _ = synth.build_model('c2', seed=1234)
+    for dname, d in (('51peg', peg_data(arr)), ('c2', d2)):
+        ref = Ref(_Frame({'BJD': d.BJD, 'RV': d.RV, 'eRV': d.eRV, 'Flag': d.Flag}))
+        res = {}
+        for par in (0, 1, 2, 3, 4, 6, 7):
+            b = types.SimpleNamespace(parameterisation=par, astrometry_bool=False, number_=1)
+            res[f'Keplerian{par}'] = ref.set_Keplerian(b, prargs=[[0, 1], [0, 0.1]], starmass=None,
+                                                       dynamics=False, kplan=1, dynamics_already_included=False)
+        nins = d.nins
+        res['Offset'] = ref.set_Offset(types.SimpleNamespace(number_=nins))
+        res['Jitter'] = ref.set_Jitter(types.SimpleNamespace(number_=nins), [0, 1], [5, 5])
+        res['MOAV2'] = ref.set_MOAV(types.SimpleNamespace(number_=nins, moav=2))
+        res['Acceleration2'] = ref.set_Acceleration(types.SimpleNamespace(number_=2))
+        res['Sinusoid'] = ref.set_Sinusoid(types.SimpleNamespace(number_=1))
+        res['MagneticCycle'] = ref.set_MagneticCycle(types.SimpleNamespace(number_=1))
+        out[dname] = {k: {'limits': clean(v[0]), 'priors': list(v[1]), 'prargs': clean(v[2])}
+                      for k, v in res.items()}
+    with open(os.path.join(HERE, 'smartsetter_kat.json'), 'w') as f:
+        json.dump(out, f, indent=1)
+    print('smartsetter_kat:', {k: len(v) for k, v in out.items()})
 
 
 def _template_model_source(model, support):
