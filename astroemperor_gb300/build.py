@@ -3,13 +3,18 @@
 Each ``csrc/*.cu`` translation unit is compiled by its own ``nvcc`` process
 (in parallel) and the objects are linked into
 ``astroemperor_gb300/_lib/libemp_gpu.so``.  A build is skipped when the
-library is newer than every source and header.
+library was built from the same sources: a SHA-256 over every source and
+header, the compiler flags and the machine type, written next to the
+library, must match (file times are not trusted: a copied tree keeps a
+library built elsewhere).  ``build`` prints whether it compiled.
 """
 from __future__ import annotations
 
 import concurrent.futures as cf
 import glob
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -38,21 +43,39 @@ def _deps():
     return _sources() + glob.glob(os.path.join(CSRC, '*.cuh')) + glob.glob(os.path.join(INCLUDE, '*.h'))
 
 
-def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+STAMP = LIB + '.sha256'
+BASE_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC']
+
+
+def source_hash(extra_flags=None) -> str:
+    """SHA-256 of the sources, headers, flags and machine type."""
+    h = hashlib.sha256()
+    for p in sorted(_deps()):
+        h.update(os.path.relpath(p, ROOT).encode())
+        with open(p, 'rb') as f:
+            h.update(f.read())
+    h.update(' '.join(ARCH + BASE_FLAGS + list(extra_flags or [])).encode())
+    h.update(platform.machine().encode())
+    return h.hexdigest()
+
+
+def up_to_date(extra_flags=None) -> bool:
+    if not (os.path.exists(LIB) and os.path.exists(STAMP)):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(p) <= t for p in _deps())
+    with open(STAMP) as f:
+        return f.read().strip() == source_hash(extra_flags)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
-    """Compile and link; returns the library path."""
-    if not force and up_to_date():
+def build(force: bool = False, verbose: bool = False, extra_flags=None, quiet: bool = False) -> str:
+    """Compile and link unless the library matches the sources; returns its path."""
+    digest = source_hash(extra_flags)
+    if not force and up_to_date(extra_flags):
+        if not quiet:
+            print(f'libemp_gpu.so up to date (sources {digest[:12]})')
         return LIB
     nvcc = nvcc_path()
     os.makedirs(OUTDIR, exist_ok=True)
-    flags = ARCH + ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC',
-                    '-I', INCLUDE, '-I', CSRC] + list(extra_flags or [])
+    flags = ARCH + BASE_FLAGS + ['-I', INCLUDE, '-I', CSRC] + list(extra_flags or [])
     objs = []
     cmds = []
     for src in _sources():
@@ -76,11 +99,15 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
         sys.stderr.write(' '.join(link) + '\n' + p.stdout + p.stderr)
         raise RuntimeError('link of libemp_gpu.so failed')
     os.replace(LIB + '.tmp', LIB)
+    with open(STAMP, 'w') as f:
+        f.write(digest + '\n')
     for o in objs:
         try:
             os.remove(o)
         except OSError:
             pass
+    if not quiet:
+        print(f'libemp_gpu.so compiled (sources {digest[:12]}, {platform.machine()})')
     return LIB
 
 

@@ -32,21 +32,32 @@ struct Work {
     int2* pairs;          // [T*W] accepted (slot_a, slot_b) of pair t at [t*W + k]
 };
 
-__host__ __device__ inline size_t work_bytes(int T, int W) {
-    return 8 * (size_t)kMaxTemps + 16 + 4 * (size_t)kMaxTemps + 4 * (size_t)kMaxTemps + 16 + 16 +
-           8 * (size_t)T * (size_t)W;
+// byte offsets of the Work fields in the workspace; the header (everything
+// before the swap log) is cleared before a sweep that starts from fresh memory
+constexpr size_t kWorkOffBetas = 0;
+constexpr size_t kWorkOffRows = kWorkOffBetas + 8 * (size_t)kMaxTemps;
+constexpr size_t kWorkOffPairCount = kWorkOffRows + 16;
+constexpr size_t kWorkOffSmd = kWorkOffPairCount + 4 * (size_t)kMaxTemps;
+constexpr size_t kWorkOffTicket = kWorkOffSmd + 4 * (size_t)kMaxTemps;
+constexpr size_t kWorkOffNrecNone = kWorkOffTicket + 16;
+constexpr size_t kWorkOffPairs = kWorkOffNrecNone + 16;
+constexpr size_t kWorkHeaderBytes = kWorkOffPairs;
+static_assert(kWorkOffPairs % 8 == 0, "the swap log needs 8-byte alignment");
+
+__host__ __device__ constexpr size_t work_bytes(int T, int W) {
+    return kWorkHeaderBytes + 8 * (size_t)T * (size_t)W;
 }
 
 __host__ __device__ inline Work carve_work(void* base) {
     char* p = static_cast<char*>(base);
     Work w;
-    w.betas_used = reinterpret_cast<double*>(p); p += 8 * kMaxTemps;
-    w.rows = reinterpret_cast<int64_t*>(p);      p += 16;
-    w.pair_count = reinterpret_cast<int*>(p);    p += 4 * kMaxTemps;
-    w.smd_acc = reinterpret_cast<float*>(p);     p += 4 * kMaxTemps;
-    w.ticket = reinterpret_cast<unsigned int*>(p); p += 16;
-    w.nrec_none = reinterpret_cast<int64_t*>(p); p += 16;
-    w.pairs = reinterpret_cast<int2*>(p);
+    w.betas_used = reinterpret_cast<double*>(p + kWorkOffBetas);
+    w.rows = reinterpret_cast<int64_t*>(p + kWorkOffRows);
+    w.pair_count = reinterpret_cast<int*>(p + kWorkOffPairCount);
+    w.smd_acc = reinterpret_cast<float*>(p + kWorkOffSmd);
+    w.ticket = reinterpret_cast<unsigned int*>(p + kWorkOffTicket);
+    w.nrec_none = reinterpret_cast<int64_t*>(p + kWorkOffNrecNone);
+    w.pairs = reinterpret_cast<int2*>(p + kWorkOffPairs);
     return w;
 }
 

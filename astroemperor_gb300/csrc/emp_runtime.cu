@@ -328,6 +328,25 @@ int prepare_eval(emp_handle* h, int prec) {
     return EMP_OK;
 }
 
+// Everything a sweep sets up on the device once per handle (the stretch
+// kernel's attributes and persistent grid, the swap kernel's shared-memory
+// limit), done before the sweep's first launch.
+int prepare_sweep(emp_handle* h, int prec) {
+    int rc = prepare_eval(h, prec);
+    if (rc) return rc;
+    if (!h->swap_attr) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+        h->swap_attr = true;
+    }
+    if (!h->swap_attr_batch) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+        h->swap_attr_batch = true;
+    }
+    return EMP_OK;
+}
+
 void gp_args(const emp_handle* h, KArgs& a);
 int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec);
 
@@ -1140,24 +1159,27 @@ int emp_pt_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec
 // ---------------------------------------------------------------------------
 // Sweep without any allocation by the caller or the library.
 //
-// Some callers cannot call cudaMalloc at all: code that runs while a larger
-// application graph is being captured (allocation is illegal inside stream
-// capture), and host programs whose device memory is one fixed arena handed
-// out by their own allocator.  emp_pt_sweep_static serves them: the sweep's
-// workspace (the swap log, the per-sweep rows, the ladder of the running
-// sweep) lives in the file-scope array below instead of a caller buffer.
+// Some callers cannot call cudaMalloc at all: host programs whose device
+// memory is one fixed arena handed out by their own allocator (a second
+// allocator would fragment or overcommit it), and processes that forbid any
+// allocation once they are running (real-time loops, allocation-audited
+// services).  emp_pt_sweep_static serves them: the sweep's workspace (the
+// swap log, the per-sweep rows, the ladder of the running sweep) lives in
+// the file-scope array below instead of a caller buffer.
 //
 // The array holds one PT state of up to kStaticMaxWalkers = ntemps*nwalkers
 // walkers (about 260 KB); every GPU that loads this library keeps it until
 // the process exits.  All calls share it and it keeps the last call's
 // contents, so each call first clears the part that must start at zero;
 // calls that overlap on the GPU (other streams, other threads) race on it.
+// The first call on each device looks the array's device address up
+// (cudaGetSymbolAddress, with that device current) and sets the kernels'
+// attributes; that first call should come before any stream capture.
 // ---------------------------------------------------------------------------
-static const int kStaticMaxWalkers = 32768;
-static const size_t kStaticHeaderBytes = 8 * (size_t)kMaxTemps + 16 + 4 * (size_t)kMaxTemps +
-                                         4 * (size_t)kMaxTemps + 16 + 16;
-static const size_t kStaticWorkBytes =
-    ((kStaticHeaderBytes + 8 * (size_t)kStaticMaxWalkers) + 255) & ~(size_t)255;
+static constexpr int kStaticMaxWalkers = 32768;
+static constexpr size_t kStaticHeaderBytes = work_bytes(0, 0);
+static constexpr size_t kStaticWorkBytes = (work_bytes(1, kStaticMaxWalkers) + 255) & ~(size_t)255;
+static_assert(kStaticHeaderBytes == kWorkHeaderBytes, "static workspace header out of step with Work");
 static __device__ __align__(256) unsigned char g_static_work[kStaticWorkBytes];
 
 static std::mutex g_static_mu;
@@ -1199,6 +1221,7 @@ extern "C" int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st, const 
     if (h->gp_M > 0 && h->gp_rows < walkers)
         return fail(EMP_E_UNSUPPORTED, "a GP model needs its row workspace (emp_pt_evaluate or emp_pt_sweep "
                     "allocates it) before the allocation-free sweep");
+    if ((rc = prepare_sweep(h, local.precision))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     CUDA_TRY(cudaMemsetAsync(ws, 0, kStaticHeaderBytes, s));
     return enqueue_sweep(h, &local, rec, s, nullptr);
@@ -1222,17 +1245,7 @@ int capture_sweep(emp_handle* h, GraphCache& gc, const emp_pt_state* st, const e
     const bool has_rec = rec != nullptr;
     if (has_rec) rcopy = *rec;
     gc.reset();
-    if ((rc = prepare_eval(h, st->precision))) return rc;
-    if (!h->swap_attr) {
-        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
-        h->swap_attr = true;
-    }
-    if (!h->swap_attr_batch) {
-        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, true>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
-        h->swap_attr_batch = true;
-    }
+    if ((rc = prepare_sweep(h, st->precision))) return rc;
     HostCopy hc{};
     if (host) {
         if (!h->aux) CUDA_TRY(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));

@@ -562,8 +562,15 @@ class PTSampler:
         from .stats import stepping_stone
         return stepping_stone(self.betas, self.get_log_like(discard=discard))
 
-    # reddemcee's hybrid estimator is not reproduced: thermodynamic integration
-    get_evidence_hybrid = get_evidence_ti
+    def get_evidence_hybrid(self, discard=0):
+        """reddemcee's 'hybrid' estimator (EMPEROR's default
+        ``evidence_method``, ``emp.py:129``) is defined in reddemcee's own
+        source, which the reference does not vendor; it is refused rather
+        than replaced.  EMPEROR's postprocess catches the error and falls
+        back to thermodynamic integration (``emp.py:1443-1445``); call
+        ``get_evidence_ti`` or ``get_evidence_ss`` directly."""
+        raise NotImplementedError("reddemcee's hybrid evidence estimator is not available on the GPU "
+                                  "engine; use get_evidence_ti or get_evidence_ss")
 
     def run_adaptation_batches(self, p1, adaptation_batches, adaptation_nsweeps, nsweeps, nsteps=1,
                                tol0=10, tau_diff_to_converge=0.1):

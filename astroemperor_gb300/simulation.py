@@ -45,7 +45,12 @@ class Simulation:
         self.switch_jitter = True
         self.switch_first_run = True
         self.moav = {'order': 0, 'global': False}
-        self.moav_reference_quirk = False
+        # None: as the reference computes it -- its per-instrument MA template
+        # writes into a masked copy and leaves the model unchanged
+        # (moav00.model:18-19), its global one is live (moav01.model).  False
+        # opts in to the documented per-instrument recurrence; True forces the
+        # no-op form.
+        self.moav_reference_quirk = None
         self.switch_celerite = False
         self.my_kernel = {'terms': ['RealTerm'], 'params': [{'a': None, 'c': None}]}
         self.sinusoid = 0
@@ -59,6 +64,12 @@ class Simulation:
         self.switch_dynamics = False
         self.dynamics_already_included = False
         self.cores__ = 1
+        # emp.py:104-112: point estimate and the between-run limit constraint
+        self.use_fit = 'max_post'
+        self.constrain = {'method': 'range', 'sigma': 3, 'types': ['Keplerian', 'Jitter'],
+                          'tol': 1e-4, 'known_methods': ['sigma', 'range', 'None']}
+        self.switch_evidence = True
+        self.evidence = (0.0, 0.0)
         self.engine__ = None
         self.engine_config = {}
         self.run_config = {}
@@ -195,9 +206,14 @@ class Simulation:
             if ap in self.conds:
                 self.conds.remove(ap)
 
+    def moav_quirk(self) -> bool:
+        """Whether the per-instrument MA runs as the reference's no-op."""
+        if self.moav_reference_quirk is None:
+            return not self.moav['global']
+        return bool(self.moav_reference_quirk)
+
     def update_model(self):
-        self.model = ReddModel(self.blocks__, self.my_data,
-                               moav_reference_quirk=self.moav_reference_quirk)
+        self.model = ReddModel(self.blocks__, self.my_data, moav_reference_quirk=self.moav_quirk())
 
     # ------------------------------------------------------------ init walkers
     def set_init(self, rng=np.random):
@@ -281,37 +297,91 @@ class Simulation:
         self.time_run = time.time() - t0
 
     def postprocess(self):
-        """The statistics of emp.py:1324-1210 that need only the samples."""
+        """emp.py:1324-1340 without the plots and logs: samples, evidence, the
+        point estimates of ``_get_fit_reddemcee`` (emp.py:1467-1496), the
+        statistics of ``_calculate_statistics`` (emp.py:1546-1557,
+        1187-1210) and the per-parameter values of ``_set_p_values``
+        (emp.py:1560-1566, 1721-1767)."""
+        from .stats import hdi_of_chain
         d = dict(discard=self.reddemcee_discard, thin=self.reddemcee_thin, flat=True)
         self.chain = self.sampler.get_chain(**d)
         self.likes = self.sampler.get_log_like(**d)
         self.posts = self.sampler.get_log_prob(**d)
+        if self.switch_evidence:
+            # emp.py:1431-1446: the configured estimator, then TI, then TI
+            # without the PCHIP interpolation
+            method = getattr(self, 'evidence_method', 'hybrid')
+            try:
+                z = getattr(self.sampler, f'get_evidence_{method}')(discard=self.reddemcee_discard)[:2]
+                if z[0] == -np.inf:
+                    z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard)[:2]
+                if z[0] == -np.inf:
+                    z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard, pchip=False)[:2]
+            except Exception:
+                z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard, pchip=False)[:2]
+            self.evidence = (z[0], z[1])
+        ch0 = self.chain[0]
         self.best_loc_post = int(np.argmax(self.posts[0]))
         self.best_loc_like = int(np.argmax(self.likes[0]))
-        self.fit_max = self.chain[0][self.best_loc_post]
-        self.fit_like = self.chain[0][self.best_loc_like]
-        self.fit_median = np.median(self.chain[0], axis=0)
+        # the "maximum likelihood" the reference reports, and the one its BIC
+        # uses, is the likelihood of the maximum-posterior sample
         self.post_max = float(self.posts[0][self.best_loc_post])
-        self.like_max = float(self.likes[0][self.best_loc_like])
-        # emp.py:1431-1446: the configured estimator, then TI, then TI without
-        # the PCHIP interpolation
-        method = getattr(self, 'evidence_method', 'hybrid')
-        try:
-            z = getattr(self.sampler, f'get_evidence_{method}')(discard=self.reddemcee_discard)[:2]
-            if z[0] == -np.inf:
-                z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard)[:2]
-            if z[0] == -np.inf:
-                z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard, pchip=False)[:2]
-        except Exception:
-            z = self.sampler.get_evidence_ti(discard=self.reddemcee_discard, pchip=False)[:2]
-        self.evidence = (z[0], z[1])
-        resid, err2 = self.residuals(self.fit_max)
+        self.like_max = float(self.likes[0][self.best_loc_post])
+        self.prior_max_post = self.post_max - self.like_max
+        self.sigmas = np.std(ch0, axis=0)
+        self.fit_max = ch0[self.best_loc_post]
+        self.fit_mean = np.mean(ch0, axis=0)
+        self.fit_median = np.median(ch0, axis=0)
+        self.fit_low1, self.fit_high1 = hdi_of_chain(ch0, 0.36).T
+        self.fit_low2, self.fit_high2 = hdi_of_chain(ch0, 0.90).T
+        self.fit_low3, self.fit_high3 = hdi_of_chain(ch0, 0.95).T
+        self.fit_maxlike = ch0[self.best_loc_like]
+        self.fit_like = self.fit_maxlike
+        self.ajuste = {'max_post': self.fit_max, 'max_like': self.fit_maxlike, 'mean': self.fit_mean,
+                       'median': self.fit_median}.get(self.use_fit, self.fit_max)
+        resid, err2 = self.residuals(self.ajuste)
         st = model_stats(resid, err2, self.model.ndim__, self.like_max,
                          flags=self.my_data.Flag, nins=self.nins__)
         for k, v in st.items():
             setattr(self, k, v)
+        # emp.py:1202, 1548: DIC from the likelihood at the posterior mean
+        self.dic_aux = float(np.var(-2 * self.likes[0]))
+        self.DIC = -2 * self.log_like_at(self.fit_mean) + self.dic_aux
+        self.Evidence = self.evidence[0]
+        self.post_true = self.post_max - self.Evidence
+        self.BayesFactor = self.like_max - self.Evidence
+        self._set_p_values()
         self.history.append({'k': self.kplanets__, 'like_max': self.like_max,
-                             'post_max': self.post_max, 'BIC': self.BIC, 'fit': self.fit_max})
+                             'post_max': self.post_max, 'BIC': self.BIC, 'fit': self.fit_max,
+                             'evidence': self.evidence})
+
+    def _set_p_values(self):
+        """emp.py:1560-1566, 1721-1767: value, sigma, HDI bounds and the
+        1-sigma ``value_range`` of every free parameter; fixed ones get
+        their value and NaN spreads."""
+        j = 0
+        for b in self.blocks__:
+            for p in b:
+                if p.fixed is not None:
+                    p.sigma = np.nan
+                    p.value_max = p.value_mean = p.value_median = p.value_max_lk = p.value
+                    for lvl in (1, 2, 3):
+                        setattr(p, f'value_low{lvl}', np.nan)
+                        setattr(p, f'value_high{lvl}', np.nan)
+                    p.value_range = [np.nan, np.nan]
+                    continue
+                p.cpointer = j
+                p.value = float(self.ajuste[j])
+                p.sigma = float(self.sigmas[j])
+                p.value_max, p.value_mean = float(self.fit_max[j]), float(self.fit_mean[j])
+                p.value_median, p.value_max_lk = float(self.fit_median[j]), float(self.fit_maxlike[j])
+                for lvl in (1, 2, 3):
+                    setattr(p, f'value_low{lvl}', float(getattr(self, f'fit_low{lvl}')[j]))
+                    setattr(p, f'value_high{lvl}', float(getattr(self, f'fit_high{lvl}')[j]))
+                a = p.value_low1 if p.value_low1 < p.value_max else p.value_max - p.sigma
+                c = p.value_high1 if p.value_high1 > p.value_max else p.value_max + p.sigma
+                p.value_range = [max(a, p.limits[0]), min(c, p.limits[1])]
+                j += 1
 
     def residuals(self, theta):
         """(Y - model, err2) at theta, from the device my_model (for stats)."""
@@ -321,22 +391,77 @@ class Simulation:
         model0, err2 = ctx.model_eval(th)
         return self.my_data.RV - model0[0].cpu().numpy(), err2[0].cpu().numpy()
 
+    def log_like_at(self, theta):
+        """my_likelihood(theta) on the device (FP64)."""
+        import torch
+        ctx = self.sampler.ctx
+        th = torch.as_tensor(np.atleast_2d(theta), dtype=torch.float64, device=ctx.device)
+        ll, _ = ctx.logpost(th, precision=0)
+        return float(ll[0].item())
+
+    # ------------------------------------------------------- between runs
+    def _set_init_pos(self):
+        """emp.py:2671-2675: the next run starts the Keplerians inside their
+        1-sigma ranges."""
+        for b in self.blocks__:
+            if b.type_ == 'Keplerian':
+                for p in b:
+                    if p.fixed is None:
+                        p.init_pos = list(p.value_range)
+
+    def _constrain_next_run(self):
+        """emp.py:2707-2783 ('sigma' and 'range'; 'GM' needs the Gaussian
+        mixture fits, which are not on this path): narrow the limits of the
+        Keplerian and jitter parameters for the next run by conditions."""
+        method = self.constrain['method']
+        if method == 'None':
+            return
+        if method not in ('sigma', 'range'):
+            raise ValueError(f'constrain method {method!r} is not on this path')
+        nsig = self.constrain['sigma']
+        for b in self.blocks__:
+            if b.type_ not in self.constrain['types']:
+                continue
+            for p in b:
+                if p.fixed is not None:
+                    continue
+                if method == 'sigma':
+                    limf, limc = p.value - nsig * p.sigma, p.value + nsig * p.sigma
+                else:
+                    limf, limc = getattr(p, f'value_low{nsig}'), getattr(p, f'value_high{nsig}')
+                limc = min(limc, p.limits[1])
+                if limf < p.limits[0] or b.type_ == 'Jitter':
+                    limf = p.limits[0]
+                if (limc - limf) / abs(p.value) >= self.constrain['tol']:
+                    self.add_condition([p.name, 'limits', [limf, limc]])
+
+    def _check_continue_run(self, old_crit):
+        """emp.py:2654-2668: False while the criterion improved by more than
+        the tolerance and runs remain."""
+        new = getattr(self, self._crit_current)
+        if not (old_crit - new > self._crit_tolerance):
+            return False
+        return self.k_start <= self.k_end
+
     def autorun(self, k_start=0, k_end=10):
-        """emp.py:2414-2456 with the BIC comparison (emp.py:1145-1156)."""
+        """emp.py:2414-2456: runs of k_start..k_end Keplerians while the BIC
+        improves by more than ``_crit_tolerance`` (emp.py:1145-1156); between
+        runs the Keplerians start inside the last run's ranges and the
+        Keplerian and jitter limits are narrowed (``constrain``)."""
         assert k_start <= k_end, f'Invalid keplerian starting point: ({k_start}, {k_end})'
         self.k_start, self.k_end = k_start, k_end
-        old_bic = np.inf
         while self.k_start <= self.k_end:
             if self.switch_first_run:
                 self._autorun_add_RV_ins()
                 for _ in range(self.k_start):
                     self.add_keplerian()
                 self.switch_first_run = False
+            old = getattr(self, self._crit_current)
             self.run()
             self.postprocess()
             self.k_start += 1
-            if not (old_bic - self.BIC > self._crit_tolerance):
+            if not self._check_continue_run(old):
                 break
-            old_bic = self.BIC
-            if self.k_start <= self.k_end:
-                self.add_keplerian()
+            self._set_init_pos()
+            self._constrain_next_run()
+            self.add_keplerian()

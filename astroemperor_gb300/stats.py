@@ -137,14 +137,38 @@ def stepping_stone(betas, log_like):
     return float(logz), float(np.sqrt(var))
 
 
+def hdi_of_samples(samples, cred_mass=0.9):
+    """Shortest interval holding ``cred_mass`` of the samples
+    (``src/astroemperor/math_utils.py:72-85``): over the sorted samples, the
+    window of floor(cred_mass * n) steps with the least width."""
+    s = np.sort(np.asarray(samples, dtype=np.float64))
+    n = len(s)
+    k = int(np.floor(cred_mass * n))
+    widths = s[k:] - s[: n - k]
+    i = int(np.argmin(widths))
+    return s[i], s[i + k]
+
+
+def hdi_of_chain(chain, cred_mass=0.9):
+    """``hdi_of_samples`` per column of a flat chain [n, ndim] -> [ndim, 2]
+    (``math_utils.py:88-105``)."""
+    chain = np.asarray(chain, dtype=np.float64)
+    return np.array([hdi_of_samples(chain[:, j], cred_mass) for j in range(chain.shape[1])])
+
+
 def model_stats(residuals, err2, ndim, like_max, flags=None, nins=1):
     n = len(residuals)
     out = {}
     out['chi2'] = float(np.sum(residuals ** 2 / err2))
     out['chi2_red'] = out['chi2'] / (n - ndim)
     out['RMSE'] = float(np.sqrt(np.sum(residuals ** 2) / n))
+    out['dof'] = n - ndim
     if flags is not None:
         out['RMSi'] = [float(np.sqrt(np.mean(residuals[flags == i + 1] ** 2))) for i in range(nins)]
+        # emp.py:1195-1197 weighs each instrument by len(FLAGS_ == k) / RMSi**2,
+        # where the length is that of the whole boolean mask (n for every k)
+        w = np.array([n / r ** 2 for r in out['RMSi']])
+        out['Weights'] = w / np.sum(w)
     out['AIC'] = 2 * ndim - 2 * like_max
     out['BIC'] = np.log(n) * ndim - 2 * like_max
     out['HQIC'] = 2 * ndim * np.log(np.log(n)) - 2 * like_max

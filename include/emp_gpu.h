@@ -303,13 +303,14 @@ int emp_pt_sweep(emp_handle* h, const emp_pt_state* st,
                  const emp_pt_record* rec, void* stream);
 
 /* No counterpart in the reference.  Same as emp_pt_sweep, for callers that
-   cannot allocate device memory (inside the capture of a larger CUDA graph,
-   or with all device memory owned by their own arena): the workspace comes
-   from a static device array of the library (st->work is ignored), so
-   neither the caller nor the library allocates.  Limit: ntemps*nwalkers <=
-   32768 (EMP_E_SIZE beyond).  The first call on each device looks the array
-   up and must come before any stream capture; calls share the array, so
-   calls that overlap on the GPU race. */
+   cannot allocate device memory (all device memory owned by their own
+   arena allocator, or no allocation allowed once the process runs): the
+   workspace comes from a static device array of the library (st->work is
+   ignored), so neither the caller nor the library allocates.  Limit:
+   ntemps*nwalkers <= 32768 (EMP_E_SIZE beyond).  The first call on each
+   device looks the array up and sets the kernels' attributes, and should
+   come before any stream capture; calls share the array (each clears what
+   must start at zero), so calls that overlap on the GPU race. */
 int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st,
                         const emp_pt_record* rec, void* stream);
 

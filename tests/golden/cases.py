@@ -159,8 +159,8 @@ def kat_case_models(arr):
     rng = np.random.default_rng(20240601)
     cases = {}
 
-    def add(name, model, data, center=None):
-        th = draw_thetas(model, rng, center=center)
+    def add(name, model, data, center=None, spread=0.02):
+        th = draw_thetas(model, rng, center=center, spread=spread)
         cases[name] = (model, data, th)
 
     m, d = model_51peg(arr, k=0)
@@ -189,4 +189,13 @@ def kat_case_models(arr):
     add('51peg_k2_hill', m, d)
     m, d = model_51peg(arr, k=3, par=0, hill=1.11)
     add('51peg_k3_hill_p0', m, d)
+    # documented per-instrument MA(2) on one instrument (equal to the
+    # reference's live global template on the whole series)
+    m, d = model_51peg(arr, k=1, par=1, moav={'order': 2, 'global': False})
+    add('51peg_ma2_inst', m, d, center=PEG_MAP_P1 + [0.15, 10.0, 0.1, 12.0])
+    # the throughput-scale workload's shape: 7 Keplerians, 4 instruments with
+    # documented per-instrument MA(2), N = 16384 over 10000 d (8 epoch tiles
+    # of 2048 on the device)
+    m, d, setup, truth = synth.build_model('c5', seed=5)
+    add('c5_ma2', m, d, center=truth, spread=1e-4)
     return cases

@@ -25,7 +25,11 @@ Writes
                        prior templates (support/priors/*.prior) at seeded
                        points; the Kepler equation (kepler.py, absent) is
                        solved by the oracle's solver, so these pin everything
-                       else of the oracle's model, likelihood and priors
+                       else of the oracle's model, likelihood and priors.
+                       The documented per-instrument MA (which the reference's
+                       own per-instrument template does not compute) is pinned
+                       to its live global template moav01.model run on each
+                       instrument's time-ordered subsequence
   smartsetter_kat.json -- default limits / priors / prargs of every block type
                        as the reference's SmartSetter methods (block_repo.py,
                        run from its source on a small column shim) set them
@@ -159,6 +163,7 @@ def _template_model_source(model, support):
     def tpl(name):
         return open(os.path.join(support, 'models', name)).read()
     nins = model.data.nins
+    helpers = []
     src = ['def my_model(theta):',
            '    for a in A_:',
            '        theta = np.insert(theta, a, mod_fixed_[a])',
@@ -179,16 +184,28 @@ def _template_model_source(model, support):
             src.append('    residuals = Y_ - model0')
             if b.is_global:
                 src.append(tpl('moav01.model').format(nins, sl, b.moav))
-            else:
+            elif model.moav_reference_quirk:
                 for k in range(1, nins + 1):
                     src.append(tpl('moav00.model').format(k, sl, b.moav))
+            else:
+                # the documented per-instrument MA (docs/user-guide/ug-the-model.md):
+                # the reference's live template moav01 run on each instrument's
+                # time-ordered subsequence with that instrument's coefficients
+                for k in range(1, nins + 1):
+                    q0 = sl.start + 2 * b.moav * (k - 1)
+                    body = tpl('moav01.model').format(nins, f'{q0}:{q0 + 2 * b.moav}', b.moav)
+                    helpers.append(f'def _ma_run{k}(theta, X_, residuals, model0, ndat):\n{body}\n'
+                                   '    return model0, residuals\n')
+                    src.append(f'    model0[mask{k}], residuals[mask{k}] = _ma_run{k}('
+                               f'theta, X_[mask{k}], residuals[mask{k}].copy(), model0[mask{k}].copy(), '
+                               f'ndat{k})')
         elif b.type_ == 'Jitter':
             for k in range(1, nins + 1):
                 src.append(tpl('jitter00.model').format(k, sl))
         else:
             raise ValueError(b.type_)
     src.append('    return model0, err20')
-    return '\n'.join(src) + '\n'
+    return ''.join(helpers) + '\n'.join(src) + '\n'
 
 
 def _reference_check_prargs(src_dir):
@@ -265,8 +282,6 @@ def template_fixture(ref_root, arr):
                          for f in sorted(os.listdir(os.path.join(support, 'priors'))))
     out = {}
     for name, (m, d, th) in kat_case_models(arr).items():
-        if m.moav_reference_quirk is False and any(b.type_ == 'MOAV' and not b.is_global for b in m.blocks):
-            continue        # the documented per-instrument MA is this package's, not a reference template
         g = {'np': np, 'kepler': types.SimpleNamespace(solve=kepler_solve),
              'X_': d.BJD, 'Y_': d.RV, 'YERR_': d.eRV, 'ndat': d.ndata,
              'A_': list(m.A_), 'mod_fixed_': m.mod_fixed}
@@ -278,7 +293,8 @@ def template_fixture(ref_root, arr):
         g.update({'betapdf': betapdf, 'cps': mu.cps})
         exec(prior_defs, g)
         exec(_template_prior_source(m, src_dir, normalise), g)
-        pick = np.linspace(0, len(th) - 1, 6).astype(int)
+        # the per-epoch model of the large cases is pinned through logL only
+        pick = np.linspace(0, len(th) - 1, 6).astype(int) if d.ndata <= 4096 else np.zeros(0, int)
         mod, err, ll = [], [], []
         with np.errstate(all='ignore'):
             for i, t in enumerate(th):
@@ -376,4 +392,6 @@ def hill_fixture(ref_root):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) != 2:
+        sys.exit('usage: python tests/golden/make_golden.py <root of the astroemperor source tree>')
+    main(sys.argv[1])

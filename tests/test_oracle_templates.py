@@ -77,3 +77,34 @@ def test_oracle_my_prior_equals_reference_assembly(peg_arr, tkat):
         np.testing.assert_array_equal(np.isfinite(lp), np.isfinite(ref), err_msg=name)
         fin = np.isfinite(ref)
         np.testing.assert_array_equal(lp[fin], ref[fin], err_msg=name)
+
+
+@pytest.mark.parametrize('quirk,case', [(None, 'c2_ma1_quirk'), (False, 'c2_ma1')])
+def test_simulation_ma_default_follows_the_reference(peg_arr, tkat, quirk, case):
+    """A Simulation with per-instrument MA(1) computes what the reference's
+    generated my_likelihood computes (its per-instrument template is a
+    no-op); ``moav_reference_quirk = False`` opts in to the documented
+    recurrence, pinned to the reference's live template run per instrument."""
+    from astroemperor_gb300 import synth
+    from astroemperor_gb300.simulation import Simulation
+    instruments, _ = synth.make_system('c2', seed=7)
+    sim = Simulation()
+    sim.load_arrays(instruments, ['INS1', 'INS2'])
+    sim.keplerian_parameterisation = 1
+    sim.moav = {'order': 1, 'global': False}
+    if quirk is not None:
+        sim.moav_reference_quirk = quirk
+    sim._autorun_add_RV_ins()
+    for _ in range(3):
+        sim.add_keplerian()
+    sim.apply_conditions()
+    sim.update_model()
+    assert sim.model.moav_reference_quirk is (quirk is None)
+    m, d, th = kat_case_models(peg_arr)[case]
+    assert [p.name for p in sim.model.free_parameters()] == [p.name for p in m.free_parameters()]
+    o = OracleRV(sim.model.spec(), sim.my_data.as_dict())
+    ref = tkat[f'{case}__logl']
+    fin = np.isfinite(ref)
+    with np.errstate(all='ignore'):
+        ll = np.array([o.my_likelihood(t) for t in th[fin]])
+    np.testing.assert_allclose(ll, ref[fin], rtol=1e-12)
