@@ -7,8 +7,8 @@
 * posterior: the mixed-precision sampler on 51 Peg recovers the fit the
   reference recorded (tests/01_51peg_basic.ipynb), and with an independent
   random stream its cold-chain quantiles (51 Peg and the C2 model) agree
-  with the oracle sampler's within 4 Monte-Carlo standard errors from the
-  chains' effective sample sizes.
+  with the oracle sampler's within 4 Monte-Carlo standard errors (batch
+  means).
 """
 import numpy as np
 import pytest
@@ -150,18 +150,15 @@ def test_adaptation_batches_driver_freezes_the_ladder(peg_arr, lib, cuda):
     assert np.isfinite(s.get_evidence_ss()[0]) and np.isfinite(s.get_evidence_ti()[0])
 
 
-def _quantile_se(x_sw, q):
-    """Monte-Carlo standard error of the q-quantile of a chain x[steps, walkers]:
-    sqrt(q (1 - q) / ESS) / f(x_q), with ESS = steps * walkers / tau (tau the
-    integrated autocorrelation time) and the density f from the quantiles at
-    q -+ 0.05."""
-    from astroemperor_gb300.stats import integrated_time
-    tau = max(float(integrated_time(x_sw[:, :, None], tol=0)[0]), 1.0)
-    ess = x_sw.size / tau
-    x = x_sw.reshape(-1)
-    lo, hi = np.quantile(x, max(q - 0.05, 0.001)), np.quantile(x, min(q + 0.05, 0.999))
-    dens = (min(q + 0.05, 0.999) - max(q - 0.05, 0.001)) / (hi - lo)
-    return np.sqrt(q * (1 - q) / ess) / dens, ess
+def _quantile_se(x_sw, q, nb=10):
+    """Monte-Carlo standard error of the q-quantile of a chain x[steps, walkers]
+    by batch means: the chain cut into ``nb`` contiguous blocks of sweeps,
+    the quantile of each block, their standard deviation over sqrt(nb)
+    (valid when a block is much longer than the autocorrelation time; the
+    blocks here are 600 sweeps against times of tens to a few hundred)."""
+    blocks = np.array_split(x_sw, nb, axis=0)
+    bq = np.array([np.quantile(b.reshape(-1), q) for b in blocks])
+    return float(np.std(bq, ddof=1) / np.sqrt(nb))
 
 
 def _compare_quantiles(cpu, gpu, cols, names, nsig=4.0):
@@ -169,71 +166,67 @@ def _compare_quantiles(cpu, gpu, cols, names, nsig=4.0):
     for j in cols:
         for q in (0.16, 0.5, 0.84):
             a, b = np.quantile(cpu[:, :, j], q), np.quantile(gpu[:, :, j], q)
-            se_a, ess_a = _quantile_se(cpu[:, :, j], q)
-            se_b, ess_b = _quantile_se(gpu[:, :, j], q)
-            bound = nsig * np.hypot(se_a, se_b)
-            print(f'{names[j]} q={q}: oracle {a:.6g} device {b:.6g} |d| {abs(a - b):.3g} '
-                  f'bound {bound:.3g} (ESS {ess_a:.0f}, {ess_b:.0f})')
+            bound = nsig * np.hypot(_quantile_se(cpu[:, :, j], q), _quantile_se(gpu[:, :, j], q))
+            print(f'{names[j]} q={q}: oracle {a:.8g} device {b:.8g} |d| {abs(a - b):.3g} bound {bound:.3g}')
             assert abs(a - b) <= bound, (names[j], q, a, b, bound)
+
+
+def _device_fp64(ctx):
+    """Batch log-posterior with the FP64 kernel (equal to the numpy oracle
+    to 1e-11 on the golden cases), for the oracle sampler: the numpy path
+    would take minutes for these chain lengths."""
+    def f(th):
+        t = torch.as_tensor(np.atleast_2d(th), dtype=torch.float64, device='cuda:0')
+        ll, lp = ctx.logpost(t, precision=N.EMP_PREC_FP64)
+        return ll.cpu().numpy(), lp.cpu().numpy()
+    return f
+
+
+def _independent_runs(m, ctx, p0, betas, S, seed_cpu, seed_gpu):
+    T, W = p0.shape[:2]
+    ora = OraclePT(_device_fp64(ctx), T, W, m.ndim__, betas, adapt=False, rng='numpy', seed=seed_cpu)
+    ora.set_positions(p0)
+    ora.run(S)
+    cpu = np.array(ora.chain)[S // 4:, 0]
+    gpu = PTSampler(W, m.ndim__, m, ntemps=T, betas=betas, precision='mixed', seed=seed_gpu, context=ctx)
+    gpu.select_adjustment('00')
+    gpu.run_mcmc(p0, nsweeps=S)
+    return cpu, gpu.get_chain(discard=S // 4)[0]
 
 
 def test_posterior_quantiles_match_the_oracle_sampler(peg_arr, lib, cuda):
     """Independent random streams (numpy generator in the oracle sampler,
-    Philox on the device): the cold-chain 16/50/84 % quantiles of 51 Peg k=1
-    agree within 4 Monte-Carlo standard errors of their difference (each
-    error from the chain's effective sample size)."""
+    Philox on the device, mixed precision on the device): the cold-chain
+    16/50/84 % quantiles of 51 Peg k=1 agree within 4 Monte-Carlo standard
+    errors of their difference."""
+    from astroemperor_gb300.engine import Context
     m, d = model_51peg(peg_arr, k=1, par=1)
-    T, W, S = 2, 32, 1500
-    betas = [1.0, 0.2]
+    ctx = Context(m, 'cuda:0')
+    T, W, S = 2, 64, 8000
     rng = np.random.default_rng(11)
     lim = m.limits_free()
     p0 = rng.uniform(lim[:, 0], lim[:, 1], size=(T, W, m.ndim__))
     p0[..., 0] = rng.uniform(4.225, 4.235, size=(T, W))
     p0[..., 1] = rng.uniform(52, 58, size=(T, W))
     p0[..., 3:5] *= 0.3
-    o = OracleRV(m.spec(), d.as_dict())
-    ora = OraclePT(_oracle_logpost(o), T, W, m.ndim__, betas, adapt=False, rng='numpy', seed=3)
-    ora.set_positions(p0)
-    ora.run(S)
-    cpu = np.array(ora.chain)[S // 2:, 0]
-    gpu = PTSampler(W, m.ndim__, m, ntemps=T, betas=betas, precision='mixed', seed=12345)
-    gpu.select_adjustment('00')
-    gpu.run_mcmc(p0, nsweeps=S)
-    g = gpu.get_chain(discard=S // 2)[0]
+    cpu, g = _independent_runs(m, ctx, p0, [1.0, 0.2], S, 3, 12345)
     names = [p.name for p in m.free_parameters()]
     _compare_quantiles(cpu, g, (0, 1, 5, 6), names)       # period, amplitude, offset, jitter
 
 
 def test_posterior_quantiles_match_the_oracle_sampler_c2(lib, cuda):
     """The same check on the two-instrument MA(1) model of the C2 workload
-    (3 Keplerians, 23 dimensions).  The oracle sampler evaluates its
-    proposals with the FP64 kernel (equal to the numpy oracle to 1e-11 on
-    the golden cases; the numpy path would take minutes here), while the
-    device sampler runs in mixed precision with its own random stream."""
+    (3 Keplerians, 23 dimensions)."""
     from astroemperor_gb300 import synth
     from astroemperor_gb300.engine import Context
     m, d, _, truth = synth.build_model('c2', seed=1234)
     ctx = Context(m, 'cuda:0')
-
-    def fp64(th):
-        t = torch.as_tensor(np.atleast_2d(th), dtype=torch.float64, device='cuda:0')
-        ll, lp = ctx.logpost(t, precision=N.EMP_PREC_FP64)
-        return ll.cpu().numpy(), lp.cpu().numpy()
-
-    T, W, S = 2, 64, 2000
-    betas = [1.0, 0.3]
+    T, W, S = 2, 64, 8000
     rng = np.random.default_rng(5)
     lim = m.limits_free()
     p0 = np.clip(truth + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, m.ndim__)),
                  lim[:, 0], lim[:, 1])
-    ora = OraclePT(fp64, T, W, m.ndim__, betas, adapt=False, rng='numpy', seed=17)
-    ora.set_positions(p0)
-    ora.run(S)
-    cpu = np.array(ora.chain)[S // 2:, 0]
-    gpu = PTSampler(W, m.ndim__, m, ntemps=T, betas=betas, precision='mixed', seed=99, context=ctx)
-    gpu.select_adjustment('00')
-    gpu.run_mcmc(p0, nsweeps=S)
-    g = gpu.get_chain(discard=S // 2)[0]
+    cpu, g = _independent_runs(m, ctx, p0, [1.0, 0.3], S, 17, 99)
     names = [p.name for p in m.free_parameters()]
     cols = [names.index(n) for n in ('Period 1', 'Amplitude 1', 'Amplitude 3', 'Offset 2', 'Jitter 1',
                                      'MACoefficient 1 Order 1')]
