@@ -12,7 +12,7 @@ import os
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, '_lib', 'libemp_gpu.so')
 
-EMP_ABI_VERSION = 3
+EMP_ABI_VERSION = 4
 EMP_MAX_PARAMS = 160
 EMP_MAX_PLANETS = 16
 EMP_MAX_INS = 16
@@ -38,8 +38,9 @@ EMP_TERM_CYCLE_2 = 10
 
 EMP_PREC_FP64 = 0
 EMP_PREC_MIXED = 1
+EMP_LAUNCH_GRAD = 2
 
-PRIOR_KIND = {'Uniform': 0, 'Normal': 1, 'Jeffreys': 2, 'Beta': 3, 'None': 4}
+PRIOR_KIND = {'Uniform': 0, 'Normal': 1, 'Jeffreys': 2, 'Beta': 3, 'None': 4, 'Isotropic': 5}
 EMP_PRIOR_NONE = 4
 
 
@@ -71,7 +72,16 @@ class EmpModelDesc(C.Structure):
         ('gp_kind', C.c_int32 * EMP_MAX_GP_TERMS),
         ('gp_slot', (C.c_int32 * 5) * EMP_MAX_GP_TERMS),
         ('hill_mask', C.c_int32), ('_pad3', C.c_int32), ('hill_starmass', C.c_double),
+        ('am_on', C.c_int32), ('am_offset_slot', C.c_int32), ('am_jitter_slot', C.c_int32),
+        ('_pad4', C.c_int32),
     ]
+
+
+class EmpAmDesc(C.Structure):
+    _fields_ = [('n_hipp', C.c_int32), ('n_gost', C.c_int32),
+                ('catalogs', C.c_void_p), ('inv_cov', C.c_void_p), ('log_det_cov', C.c_void_p),
+                ('astro_gost', C.c_void_p), ('hipp', C.c_void_p), ('gost', C.c_void_p),
+                ('gsv', C.c_void_p), ('common_t', C.c_double)]
 
 
 class EmpDatasetDesc(C.Structure):
@@ -115,6 +125,7 @@ SIGNATURES = {
                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     'emp_logpost_grad': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    'emp_set_astrometry': (C.c_int, [C.c_void_p, C.POINTER(EmpAmDesc)]),
     'emp_model_eval': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     'emp_gp_logl': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                               C.c_int, C.c_void_p]),
@@ -129,6 +140,10 @@ SIGNATURES = {
     'emp_pt_work_bytes': (C.c_int64, [C.c_int, C.c_int, C.c_int]),
     'emp_set_launch': (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     'emp_get_launch': (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    'emp_ladder_sums': (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                  C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
+    'emp_autocorr': (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                               C.c_void_p, C.c_void_p]),
     'emp_probe_peaks': (C.c_int, [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p]),
     'emp_launch_count': (C.c_int64, []),
     'emp_last_error_string': (C.c_char_p, []),

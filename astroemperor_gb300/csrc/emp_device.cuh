@@ -113,6 +113,22 @@ struct GPMeta {
     int t;                     // temperature index
 };
 
+// threads of a k_am CTA: four walker rows, one warp each
+constexpr int kAmThreads = 128;
+
+// astrometric data on the device (emp_am_desc, emp_set_astrometry)
+struct AmDev {
+    int n_hipp, n_gost;
+    const double* catalogs;    // [3][7]
+    const double* inv_cov;     // [3][5][5]
+    const double* log_det_cov; // [3]
+    const double* astro_gost;  // [2][5]
+    const double* hipp;        // [7][n_hipp]
+    const double* gost;        // [4][n_gost]
+    const double* gsv;         // [2][5][n_gost]
+    double common_t;
+};
+
 struct KArgs {
     const emp_model_desc* md;
     DevData d;
@@ -160,6 +176,11 @@ struct KArgs {
     double* gp_v;
     double* gp_ph;
     double* gp_asum;           // [nwalk] k(0) of each row's kernel (NaN: bad coefficients)
+    // joint RV + astrometry (md->am_on): in stretch mode the kernel writes
+    // the proposal, its meta (gp_prop, gp_meta) and its RV logL (am_rv); k_am
+    // adds the astrometric term and finishes every mode
+    double* am_rv;             // [nwalk] (stretch)
+    AmDev am;
 };
 
 

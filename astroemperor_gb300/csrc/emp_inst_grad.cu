@@ -9,9 +9,6 @@ template <int Q>
 static GFn pick_grad(int lidx) {
     switch (lidx) {
         case 0: return k_grad<Q, 32, 128>;
-        case 1: return k_grad<Q, 64, 128>;
-        case 2: return k_grad<Q, 128, 128>;
-        case 3: return k_grad<Q, 256, 256>;
         default: return nullptr;
     }
 }

@@ -50,7 +50,14 @@ __device__ __forceinline__ double prior_var_term(const emp_prior& p, double x) {
         return -0.5 * z * z - p.a2;
     }
     if (p.kind == EMP_PRIOR_BETA) return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
+    if (p.kind == EMP_PRIOR_ISOTROPIC) return log(0.5 * sin(x)) - p.a0;
     return 0.0;
+}
+
+// priors whose value varies with the parameter (the others are constants
+// summed on the host)
+__device__ __forceinline__ bool prior_varies(int kind) {
+    return kind == EMP_PRIOR_NORMAL || kind == EMP_PRIOR_BETA || kind == EMP_PRIOR_ISOTROPIC;
 }
 
 __device__ __forceinline__ double derived_x(const double* th, int k) {
@@ -956,7 +963,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             const emp_prior& p = md->prior[d];
             const double x = thp[d];
             if (!in_support(x, p.lo, p.hi)) flag[0] = 1;
-            else if (p.kind == EMP_PRIOR_NORMAL || p.kind == EMP_PRIOR_BETA) pterm[d] = prior_var_term(p, x);
+            else if (prior_varies(p.kind)) pterm[d] = prior_var_term(p, x);
         }
         for (int q2 = r; q2 < 2 * n_planets; q2 += L) {
             const int p = q2 >> 1, k = q2 & 1;
@@ -964,7 +971,7 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             if (dp.kind == EMP_PRIOR_NONE) continue;
             const double x = derived_x(full + md->kep_slot[p], k);
             if (!in_support(x, dp.lo, dp.hi)) flag[0] = 1;
-            else if (dp.kind == EMP_PRIOR_NORMAL || dp.kind == EMP_PRIOR_BETA)
+            else if (prior_varies(dp.kind))
                 pterm[n_free + q2] = prior_var_term(dp, x);
         }
         for (int p = r; p < n_planets; p += L) {
@@ -1300,6 +1307,20 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
             }
         }
         if (active && A.mode == kModeStretch) {
+            double* dst = A.gp_prop + (size_t)wk * ds;
+            for (int d = r; d < n_free; d += L) dst[d] = thp[d];
+        }
+    } else if (A.am_rv != nullptr && A.mode == kModeStretch) {
+        // joint astrometry: the proposal, its prior and its RV logL for k_am,
+        // which adds the astrometric term and makes the Metropolis test
+        if (active && r == 0) {
+            GPMeta m;
+            m.lp = lp; m.z = z; m.uword = uword; m.slot = slot_j;
+            m.pos = t_idx * A.W + j_idx; m.t = t_idx;
+            A.gp_meta[wk] = m;
+            A.am_rv[wk] = logl;
+        }
+        if (active) {
             double* dst = A.gp_prop + (size_t)wk * ds;
             for (int d = r; d < n_free; d += L) dst[d] = thp[d];
         }

@@ -28,6 +28,7 @@ KFn get_kernel_mixed(int q, int lidx);
 using GFn = void (*)(GArgs);
 GFn get_kernel_grad(int q, int lidx);
 KFn get_kernel_gp(int M, int prep, int ff);
+KFn get_kernel_am();
 }  // namespace emp
 
 using namespace emp;
@@ -120,6 +121,21 @@ struct emp_handle {
     double* gp_ph = nullptr;
     double* gp_asum = nullptr;
     int sms = 0;
+    // adjoint kernel: epoch tile (0: chosen per call) and the residual buffer
+    // of MA models whose series spans several tiles (grown on demand)
+    int grad_tile = 0;
+    void* grad_buf = nullptr;
+    size_t grad_bytes = 0;
+    // joint astrometry (md.am_on): the data on the device, and per walker
+    // row of a stretch half-step the proposal, its meta and its RV logL
+    bool am_set = false;
+    AmDev am{};
+    void* am_buf = nullptr;
+    void* am_rows_buf = nullptr;
+    int64_t am_rows = 0;
+    double* am_rv = nullptr;
+    double* am_prop = nullptr;
+    GPMeta* am_meta = nullptr;
 };
 
 // dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
@@ -132,7 +148,7 @@ static const int kGPBlock = 32;
 namespace {
 
 int validate_prior(const emp_prior& p, const char* what, int i) {
-    if (p.kind < EMP_PRIOR_UNIFORM || p.kind > EMP_PRIOR_NONE)
+    if (p.kind < EMP_PRIOR_UNIFORM || p.kind > EMP_PRIOR_ISOTROPIC)
         return fail(EMP_E_INVALID, "%s %d: unknown prior kind %d", what, i, p.kind);
     if (p.kind == EMP_PRIOR_NONE) return EMP_OK;
     if (!(p.lo <= p.hi)) return fail(EMP_E_INVALID, "%s %d: limits not ordered", what, i);
@@ -210,6 +226,17 @@ int validate_model(const emp_model_desc* m) {
                 return fail(EMP_E_UNSUPPORTED, "Hill prior: term %d has parameterisation %d (0-4, 6 read "
                             "as the reference reads them)", p, par);
         }
+    }
+    if (m->am_on) {
+        // every Keplerian an astrometric one: parameterisation 0 with inclination and node
+        for (int p = 0; p < m->n_planets; ++p)
+            if (m->kep_param[p] != 0 || m->kep_slot[p] + 7 > m->n_full)
+                return fail(EMP_E_UNSUPPORTED, "astrometry: term %d is not a 7-slot parameterisation-0 Keplerian", p);
+        if (m->am_offset_slot < 0 || m->am_jitter_slot < 0)
+            return fail(EMP_E_INVALID, "astrometry without offset or jitter slots");
+        if ((rc = chk(m->am_offset_slot, 5, "astrometric offset"))) return rc;
+        if ((rc = chk(m->am_jitter_slot, 2, "astrometric jitter"))) return rc;
+        if (m->gp_nterms > 0) return fail(EMP_E_UNSUPPORTED, "a GP likelihood with astrometry");
     }
     if (m->gp_nterms < 0 || m->gp_nterms > EMP_MAX_GP_TERMS)
         return fail(EMP_E_SIZE, "gp_nterms=%d outside [0, %d]", m->gp_nterms, EMP_MAX_GP_TERMS);
@@ -410,6 +437,19 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
         gp = true;
         gp_args(h, a);
     }
+    const bool am = h->md.am_on != 0;
+    if (am) {
+        if (!h->am_set) return fail(EMP_E_INVALID, "the model has astrometry but emp_set_astrometry was not called");
+        a.am = h->am;
+        if (a.mode == kModeStretch) {
+            if (a.nwalk > h->am_rows)
+                return fail(EMP_E_INVALID, "astrometry rows hold %lld walkers, launch has %d", (long long)h->am_rows,
+                            a.nwalk);
+            a.am_rv = h->am_rv;
+            a.gp_meta = h->am_meta;
+            a.gp_prop = h->am_prop;
+        }
+    }
     a.cps = (a.nwalk + G - 1) / G;
     const int64_t items = (int64_t)a.cps * h->n_sys;
     if (items > 0x7fffffff) return fail(EMP_E_SIZE, "%lld CTA items exceed 2^31-1", (long long)items);
@@ -425,6 +465,39 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
     if (gp) return launch_gp(h, a, s, prec);
+    if (am) {
+        const int rows_per_cta = kAmThreads / 32;
+        get_kernel_am()<<<(a.nwalk + rows_per_cta - 1) / rows_per_cta, kAmThreads, 0, s>>>(a);
+        g_launches.fetch_add(1);
+        CUDA_TRY(cudaGetLastError());
+    }
+    return EMP_OK;
+}
+
+// Stretch buffers of the astrometric term for up to `rows` walker rows
+// (proposal, meta, RV logL); allocated outside any capture, growing drops
+// the captured sweep graphs.
+int am_reserve(emp_handle* h, int64_t rows) {
+    if (!h->md.am_on || rows <= h->am_rows) return EMP_OK;
+    const size_t D = (size_t)std::max(h->lay[1], 1);
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t b_prop = up(8 * D * (size_t)rows), b_meta = up(sizeof(GPMeta) * (size_t)rows);
+    const size_t b_rv = up(8 * (size_t)rows);
+    h->gc.reset();
+    h->gch.reset();
+    if (h->am_rows_buf) {
+        cudaFree(h->am_rows_buf);
+        h->am_rows_buf = nullptr;
+        h->am_rows = 0;
+    }
+    void* b = nullptr;
+    CUDA_TRY(cudaMalloc(&b, b_prop + b_meta + b_rv));
+    unsigned char* c = (unsigned char*)b;
+    h->am_rows_buf = b;
+    h->am_prop = (double*)c;
+    h->am_meta = (GPMeta*)(c + b_prop);
+    h->am_rv = (double*)(c + b_prop + b_meta);
+    h->am_rows = rows;
     return EMP_OK;
 }
 
@@ -578,7 +651,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                 a.a_inv_exact = frexp(st->a, &ex) == 0.5 ? 1.0 / st->a : 0.0;   // a = 2^(ex-1)
             }
             if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr, !batch))) return rc;
-            kcount += h->gp_M > 0 ? 3 : 1;
+            kcount += h->gp_M > 0 ? 3 : (h->md.am_on ? 2 : 1);
         }
     }
     if (hc) {
@@ -691,6 +764,12 @@ bool same_rec(const emp_pt_record& a, const emp_pt_record& b) {
 }
 
 }  // namespace
+
+namespace emp {
+// error reporting for the other translation units (same last-error string)
+int stats_fail(int code, const char* msg) { return fail(code, "%s", msg); }
+void count_launch() { g_launches.fetch_add(1); }
+}  // namespace emp
 
 extern "C" {
 
@@ -814,6 +893,8 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
         if ((rc = check_system(m, data, s, &nsys[s]))) return rc;
         if (S > 1 && m->gp_nterms > 0)
             return fail(EMP_E_UNSUPPORTED, "system %d: GP likelihoods take a one-system handle", s);
+        if (S > 1 && m->am_on)
+            return fail(EMP_E_UNSUPPORTED, "system %d: astrometric likelihoods take a one-system handle", s);
         total += nsys[s];
         lay[0] = std::max(lay[0], m->n_full);
         lay[1] = std::max(lay[1], m->n_free);
@@ -957,12 +1038,23 @@ int emp_destroy(emp_handle* h) {
     if (h->aux) cudaStreamDestroy(h->aux);
     if (h->dbuf) cudaFree(h->dbuf);
     if (h->gp_buf) cudaFree(h->gp_buf);
+    if (h->grad_buf) cudaFree(h->grad_buf);
+    if (h->am_buf) cudaFree(h->am_buf);
+    if (h->am_rows_buf) cudaFree(h->am_rows_buf);
     delete h;
     return EMP_OK;
 }
 
 int emp_set_launch(emp_handle* h, int precision, int lanes_per_walker, int tile_epochs) {
     if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (precision == EMP_LAUNCH_GRAD) {
+        if (lanes_per_walker != 0 && lanes_per_walker != 32)
+            return fail(EMP_E_INVALID, "the adjoint kernel runs 32 lanes per walker, not %d", lanes_per_walker);
+        if (tile_epochs != 0 && (tile_epochs < 32 || tile_epochs > 4096 || tile_epochs % 32))
+            return fail(EMP_E_INVALID, "adjoint tile %d: a multiple of 32 in [32, 4096]", tile_epochs);
+        h->grad_tile = tile_epochs;
+        return EMP_OK;
+    }
     if (precision != EMP_PREC_FP64 && precision != EMP_PREC_MIXED)
         return fail(EMP_E_INVALID, "precision %d unknown", precision);
     if (lanes_per_walker != 0 && lanes_index(lanes_per_walker) < 0)
@@ -1009,6 +1101,51 @@ int emp_logpost(emp_handle* h, const double* theta, int B, const int32_t* system
     int rc = gp_reserve(h, B);
     if (rc) return rc;
     return launch_eval(h, precision, a, (cudaStream_t)stream);
+}
+
+int emp_set_astrometry(emp_handle* h, const emp_am_desc* am) {
+    if (!h) return fail(EMP_E_INVALID, "handle is NULL");
+    if (!am) return fail(EMP_E_INVALID, "astrometry descriptor is NULL");
+    if (!h->md.am_on) return fail(EMP_E_INVALID, "the handle's model has no astrometry");
+    if (am->n_hipp < 1 || am->n_gost < 5)
+        return fail(EMP_E_INVALID, "astrometry needs Hipparcos abscissae and at least 5 Gaia epochs");
+    if (!am->catalogs || !am->inv_cov || !am->log_det_cov || !am->astro_gost || !am->hipp || !am->gost || !am->gsv)
+        return fail(EMP_E_INVALID, "an astrometry array is NULL");
+    const size_t nh = (size_t)am->n_hipp, ng = (size_t)am->n_gost;
+    const size_t counts[7] = {21, 75, 3, 10, 7 * nh, 4 * ng, 10 * ng};
+    const double* srcs[7] = {am->catalogs, am->inv_cov, am->log_det_cov, am->astro_gost, am->hipp, am->gost,
+                             am->gsv};
+    size_t total = 0, offs[7];
+    for (int k = 0; k < 7; ++k) {
+        offs[k] = total;
+        total += (8 * counts[k] + 255) & ~(size_t)255;
+        for (size_t i = 0; i < counts[k]; ++i)
+            if (!isfinite(srcs[k][i])) return fail(EMP_E_INVALID, "astrometry array %d holds a non-finite value", k);
+    }
+    if (h->am_buf) {
+        cudaFree(h->am_buf);
+        h->am_buf = nullptr;
+        h->am_set = false;
+    }
+    CUDA_TRY(cudaMalloc(&h->am_buf, total));
+    char* b = (char*)h->am_buf;
+    for (int k = 0; k < 7; ++k) CUDA_TRY(cudaMemcpy(b + offs[k], srcs[k], 8 * counts[k], cudaMemcpyHostToDevice));
+    AmDev d{};
+    d.n_hipp = am->n_hipp;
+    d.n_gost = am->n_gost;
+    d.catalogs = (const double*)(b + offs[0]);
+    d.inv_cov = (const double*)(b + offs[1]);
+    d.log_det_cov = (const double*)(b + offs[2]);
+    d.astro_gost = (const double*)(b + offs[3]);
+    d.hipp = (const double*)(b + offs[4]);
+    d.gost = (const double*)(b + offs[5]);
+    d.gsv = (const double*)(b + offs[6]);
+    d.common_t = am->common_t;
+    h->am = d;
+    h->am_set = true;
+    h->gc.reset();
+    h->gch.reset();
+    return EMP_OK;
 }
 
 int emp_model_eval(emp_handle* h, const double* theta, int B, double* model, double* err2,
@@ -1079,49 +1216,68 @@ int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, do
         return fail(EMP_E_INVALID, "a NULL argument");
     if (h->n_sys > 1) return fail(EMP_E_UNSUPPORTED, "the gradient takes a one-system handle");
     if (h->gp_M > 0) return fail(EMP_E_UNSUPPORTED, "gradient: GP likelihoods are not built");
+    if (h->md.am_on) return fail(EMP_E_UNSUPPORTED, "gradient: the astrometric likelihood is not built");
     const emp_model_desc& m = h->md;
-    for (int p = 0; p < m.n_planets; ++p)
-        if (m.kep_param[p] != 0 && m.kep_param[p] != 1)
-            return fail(EMP_E_UNSUPPORTED, "gradient: parameterisation %d (0 and 1 are built)", m.kep_param[p]);
     if (m.n_ins > kGradMaxIns)
         return fail(EMP_E_UNSUPPORTED, "gradient: %d instruments (at most %d)", m.n_ins, kGradMaxIns);
     if (h->q > 2) return fail(EMP_E_UNSUPPORTED, "gradient: MA order %d (at most 2)", h->q);
-    static const int kL[4] = {32, 64, 128, 256};
-    static bool attr[3][4] = {};
-    // prefer ~16-32 epochs per lane, then the largest shape that fits
-    int order[4] = {0, 1, 2, 3};
-    if (h->n >= 2048) { order[0] = 2; order[1] = 3; order[2] = 1; order[3] = 0; }
-    else if (h->n >= 512) { order[0] = 1; order[1] = 2; order[2] = 0; order[3] = 3; }
-    for (int oi = 0; oi < 4; ++oi) {
-        const int li = order[oi];
-        const int L = kL[li];
-        const int NT = L > 128 ? L : 128;
-        GSmem lay;
-        lay.build(h->q, L, NT / L, h->n, m.n_full, m.n_free, m.n_planets, m.n_ins, m.acc_order);
-        if (lay.total > 227 * 1024) continue;
-        GFn fn = get_kernel_grad(h->q, li);
-        if (!fn) return fail(EMP_E_UNSUPPORTED, "no gradient kernel for q=%d", h->q);
-        if (!attr[h->q][li]) {
-            CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          227 * 1024));
-            attr[h->q][li] = true;
+    constexpr int L = 32, NT = 128, G = NT / L;
+    const int n = h->n;
+    // the epoch tile: the caller's, else the series rounded up to 32 lanes,
+    // halved while the CTA would leave fewer than four CTAs per SM
+    int tile = h->grad_tile;
+    if (tile == 0) {
+        tile = std::min(1024, ((n + L - 1) / L) * L);
+        GSmem l2;
+        for (;;) {
+            l2.build(h->q, L, G, tile, m.n_full, m.n_free, m.n_planets, m.n_ins, m.acc_order);
+            if (l2.total * 4 <= 224 * 1024 || tile <= 256) break;
+            tile = std::max(256, tile / 2);
         }
-        GArgs a{};
-        a.md = h->md_dev;
-        a.d = h->dd;
-        a.nwalk = B;
-        a.theta = theta;
-        a.logl = logl;
-        a.logprior = logprior;
-        a.grad_logl = grad_logl;
-        a.grad_logprior = grad_logprior;
-        const int G = NT / L;
-        fn<<<(B + G - 1) / G, NT, lay.total, (cudaStream_t)stream>>>(a);
-        g_launches.fetch_add(1);
-        CUDA_TRY(cudaGetLastError());
-        return EMP_OK;
     }
-    return fail(EMP_E_SIZE, "gradient: %d epochs do not fit in shared memory", h->n);
+    GSmem lay;
+    lay.build(h->q, L, G, tile, m.n_full, m.n_free, m.n_planets, m.n_ins, m.acc_order);
+    if (lay.total > 227 * 1024)
+        return fail(EMP_E_SIZE, "gradient: tile of %d epochs needs %d B of shared memory", tile, lay.total);
+    const int ntiles = (n + tile - 1) / tile;
+    const int64_t stride = (int64_t)ntiles * tile;
+    float* resid = nullptr;
+    if (h->q > 0 && ntiles > 1) {
+        // residuals between the forward and backward passes: B rows of the
+        // tiled series, allocated on first need (outside any capture)
+        const size_t need = (size_t)B * (size_t)stride * sizeof(float);
+        if (need > h->grad_bytes) {
+            if (h->grad_buf) CUDA_TRY(cudaFree(h->grad_buf));
+            h->grad_buf = nullptr;
+            h->grad_bytes = 0;
+            CUDA_TRY(cudaMalloc(&h->grad_buf, need));
+            h->grad_bytes = need;
+        }
+        resid = static_cast<float*>(h->grad_buf);
+    }
+    GFn fn = get_kernel_grad(h->q, 0);
+    if (!fn) return fail(EMP_E_UNSUPPORTED, "no gradient kernel for q=%d", h->q);
+    static bool attr[3] = {};
+    if (!attr[h->q]) {
+        CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr[h->q] = true;
+    }
+    GArgs a{};
+    a.md = h->md_dev;
+    a.d = h->dd;
+    a.nwalk = B;
+    a.tile = tile;
+    a.theta = theta;
+    a.logl = logl;
+    a.logprior = logprior;
+    a.grad_logl = grad_logl;
+    a.grad_logprior = grad_logprior;
+    a.resid = resid;
+    a.resid_stride = stride;
+    fn<<<(B + G - 1) / G, NT, lay.total, (cudaStream_t)stream>>>(a);
+    g_launches.fetch_add(1);
+    CUDA_TRY(cudaGetLastError());
+    return EMP_OK;
 }
 
 int64_t emp_pt_work_bytes(int ntemps, int nwalkers, int ndim) {
@@ -1143,6 +1299,7 @@ int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream) {
     a.st_logl = st->logl;
     a.st_logprior = st->logprior;
     if ((rc = gp_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
+    if ((rc = am_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
     return launch_eval(h, st->precision, a, (cudaStream_t)stream);
 }
 
@@ -1151,6 +1308,7 @@ int emp_pt_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec
     int rc = check_state(h, st);
     if (rc) return rc;
     if ((rc = gp_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
+    if ((rc = am_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
     return enqueue_sweep(h, st, rec, (cudaStream_t)stream, nullptr);
 }
 
@@ -1218,6 +1376,9 @@ extern "C" int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st, const 
     local.work = ws;
     local.work_bytes = (int64_t)kStaticWorkBytes;
     if ((rc = check_state(h, &local))) return rc;
+    if (h->md.am_on && h->am_rows < walkers)
+        return fail(EMP_E_UNSUPPORTED, "a model with astrometry needs its row workspace (emp_pt_evaluate or "
+                    "emp_pt_sweep allocates it) before the allocation-free sweep");
     if (h->gp_M > 0 && h->gp_rows < walkers)
         return fail(EMP_E_UNSUPPORTED, "a GP model needs its row workspace (emp_pt_evaluate or emp_pt_sweep "
                     "allocates it) before the allocation-free sweep");
@@ -1358,6 +1519,7 @@ int emp_pt_run(emp_handle* h, const emp_pt_state* st, const emp_pt_record* rec, 
     if (nsweeps < 0) return fail(EMP_E_INVALID, "nsweeps=%d < 0", nsweeps);
     if (nsweeps == 0) return EMP_OK;
     if ((rc = gp_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
+    if ((rc = am_reserve(h, (int64_t)st->ntemps * st->nwalkers))) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (!use_graph) {
         for (int i = 0; i < nsweeps; ++i)
@@ -1385,6 +1547,7 @@ int emp_pt_run_host(emp_handle* h, const emp_pt_state* st, const emp_pt_record* 
     CUDA_TRY(cudaPointerGetAttributes(&pa, host_state));
     if (pa.type != cudaMemoryTypeHost) return fail(EMP_E_INVALID, "host state is not page-locked host memory");
     if ((rc = gp_reserve(h, (int64_t)tw))) return rc;
+    if ((rc = am_reserve(h, (int64_t)tw))) return rc;
     cudaStream_t s = (cudaStream_t)stream, ls;
     if ((rc = launch_stream(h, s, &ls))) return rc;
     if (!graph_matches(h->gch, st, rec, ls, host_state))

@@ -543,24 +543,72 @@ class PTSampler:
     def get_smd(self, discard=0, thin=1):
         return self._hist(self.smd_h, discard, thin).cpu().numpy()[:, :max(self.ntemps - 1, 0)]
 
+    def _kept(self, discard, thin):
+        n = self.iteration
+        discard, thin = int(discard), max(1, int(thin))
+        return n, discard, thin, (max(0, n - discard) + thin - 1) // thin
+
     def get_autocorr_time(self, discard=0, thin=1, c=5, tol=50, quiet=False):
         """Integrated autocorrelation time per temperature and parameter
-        (emcee's estimator: FFT autocorrelation, automated window c)."""
-        from .stats import integrated_time
-        ch = self.get_chain(discard=discard, thin=thin)
-        return np.array([integrated_time(ch[t], c=c, tol=tol, quiet=quiet) * thin
-                         for t in range(self.ntemps)])
+        (emcee's estimator: walker-averaged autocorrelation, automated window
+        c).  The autocorrelation is computed on the device from the recorded
+        chain (``emp_autocorr``, lags doubled until every window closes);
+        the windows on the host."""
+        from .stats import check_tau, tau_from_acf
+        rows, discard, thin, n = self._kept(discard, thin)
+        T, D = self.ntemps, self.ndim
+        if n == 0:
+            raise ValueError('no samples after discard')
+        maxlag = min(n, 256)
+        while True:
+            f = torch.empty(T, D, maxlag, dtype=torch.float64, device=self.device)
+            N.call('emp_autocorr', _ptr(self.chain), rows, T, self.nwalkers, D, discard, thin, maxlag,
+                   _ptr(f), self.stream.cuda_stream)
+            self.stream.synchronize()
+            fh = f.cpu().numpy()
+            res = [[tau_from_acf(fh[t, d], c) for d in range(D)] for t in range(T)]
+            if all(ok for r in res for _, ok in r) or maxlag >= n:
+                break
+            maxlag = min(n, 4 * maxlag)
+        tau = np.array([[v for v, _ in r] for r in res])
+        for t in range(T):
+            check_tau(tau[t], n, tol, quiet)
+        return tau * thin
+
+    def _ladder_sums(self, discard, stones=False):
+        from .stats import stepping_stone_plan
+        rows, discard, thin, n = self._kept(discard, 1)
+        T = self.ntemps
+        out_t = torch.zeros(T, 2, dtype=torch.float64, device=self.device)
+        src = step = out_s = None
+        ns = 0
+        if stones:
+            _, s_np, d_np = stepping_stone_plan(self.betas)
+            ns = len(s_np)
+            src = torch.as_tensor(s_np, dtype=torch.int32, device=self.device)
+            step = torch.as_tensor(d_np, dtype=torch.float64, device=self.device)
+            out_s = torch.zeros(max(ns, 1), 4, dtype=torch.float64, device=self.device)
+        N.call('emp_ladder_sums', _ptr(self.log_like_h), rows, T, self.nwalkers, discard, 1,
+               _ptr(src) if ns else None, _ptr(step) if ns else None, ns, _ptr(out_t),
+               _ptr(out_s) if ns else None, self.stream.cuda_stream)
+        self.stream.synchronize()
+        return out_t.cpu().numpy(), (out_s[:ns].cpu().numpy() if ns else np.zeros((0, 4)))
 
     def get_evidence_ti(self, discard=0, pchip=True):
-        """Thermodynamic integration of <log L>_beta over the ladder."""
-        from .stats import thermodynamic_integration
-        ll = self.get_log_like(discard=discard)
-        return thermodynamic_integration(self.betas, ll, pchip=pchip)
+        """Thermodynamic integration of <log L>_beta over the ladder; the
+        per-temperature means reduced on the device (``emp_ladder_sums``)."""
+        from .stats import ti_from_means
+        sums, _ = self._ladder_sums(discard)
+        with np.errstate(invalid='ignore', divide='ignore'):
+            mean = np.where(sums[:, 1] > 0, sums[:, 0] / np.maximum(sums[:, 1], 1), -np.inf)
+        return ti_from_means(self.betas, mean, pchip=pchip)
 
     def get_evidence_ss(self, discard=0):
-        """Stepping-stone log-evidence and its error (``stats.stepping_stone``)."""
-        from .stats import stepping_stone
-        return stepping_stone(self.betas, self.get_log_like(discard=discard))
+        """Stepping-stone log-evidence and its error (``stats.stepping_stone``),
+        from the stones' sums reduced on the device (``emp_ladder_sums``)."""
+        from .stats import ss_from_sums
+        sums, stones = self._ladder_sums(discard, stones=True)
+        return ss_from_sums(self.betas, sums, stones)
 
     def get_evidence_hybrid(self, discard=0):
         """reddemcee's 'hybrid' estimator (EMPEROR's default

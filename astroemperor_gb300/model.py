@@ -38,6 +38,12 @@ _DEFAULTS = {
     'dOffset': ('Offset', False), 'dJitter': ('Jitter', False),
     'dMACoefficient': ('MACoefficient', False), 'dMATimescale': ('MATimescale', False),
     'dAcceleration': ('Acceleration', False),
+    # astrometry (param_repo.py:349-445)
+    'dInclination': ('Inclination', False), 'dOmega': ('Omega', False),
+    'dOffset_ra': ('Offset RA', False), 'dOffset_de': ('Offset DE', False),
+    'dOffset_plx': ('Offset PLX', False), 'dOffset_pm_ra': ('Offset pm RA', False),
+    'dOffset_pm_de': ('Offset pm DE', False),
+    'dJitterH': ('Jitter Hipp', False), 'dJitterG': ('Jitter Gaia', False),
 }
 
 # Keplerian parameter lists per parameterisation (block_repo.py:23-31)
@@ -134,6 +140,39 @@ def KeplerianBlock(parameterisation: int, number: int) -> Parameter_Block:
             p.name += f' {number}'
     return Parameter_Block(ps, name_=f'KeplerianBlock {number}', type_='Keplerian',
                            class_='Model', parameterisation=parameterisation, number_=number)
+
+
+def AstrometryKeplerianBlock(number: int) -> Parameter_Block:
+    """block_repo.py:426-448: a parameterisation-0 Keplerian (P, K, phase,
+    e, w) with inclination and longitude of the node for the astrometric
+    orbit; its RV term is kep00's (akep00.model)."""
+    kb = KeplerianBlock(0, number)
+    extra = [Parameter(k) for k in ('dInclination', 'dOmega')]
+    if number:
+        for p in extra:
+            p.name += f' {number}'
+    kb.list_ = list(kb.list_) + extra
+    kb.name_ = f'AstrometryKeplerianBlock {number}'
+    kb.astrometry_bool = True
+    kb.refresh_block()
+    return kb
+
+
+def AstrometryOffsetBlock() -> Parameter_Block:
+    """block_repo.py:451-475: offsets (mas, mas/yr) of the barycentre from
+    the Gaia DR3 solution."""
+    ps = [Parameter(k) for k in ('dOffset_ra', 'dOffset_de', 'dOffset_plx', 'dOffset_pm_ra',
+                                 'dOffset_pm_de')]
+    return Parameter_Block(ps, name_='AstrometryOffsetBlock', type_='AstrometryOffset', class_='Data',
+                           number_=5)
+
+
+def AstrometryJitterBlock() -> Parameter_Block:
+    """block_repo.py:478-502: jitters of the Hipparcos abscissae and of the
+    Gaia catalogue fits."""
+    ps = [Parameter(k) for k in ('dJitterH', 'dJitterG')]
+    return Parameter_Block(ps, name_='AstrometryJitterBlock', type_='AstrometryJitter', class_='Data',
+                           number_=2)
 
 
 def OffsetBlock(nins: int) -> Parameter_Block:
@@ -274,6 +313,11 @@ class SmartSetter:
             lims = [[1.5, per], [1e-6, amp], self.angular, list(ecc_limits), self.angular]
             priors = [uni, uni, uni, 'Normal', uni]
             prargs = [None, None, None, list(ecc_prargs), None]
+            if getattr(b, 'astrometry_bool', False):
+                # inclination (isotropic) and node (block_repo.py:534-537)
+                lims += [[0, np.pi], list(self.angular)]
+                priors += ['Isotropic', uni]
+                prargs += [None, None]
         elif par == 1:
             lims = [[1.5, per], [1e-6, amp], self.angular, [-1, 1], [-1, 1]]
             priors, prargs = [uni] * 5, [None] * 5
@@ -364,6 +408,14 @@ class SmartSetter:
         lims = [[1e-5, 1.0] if p.gp_key == 'f' else [1e-5, 5.0] for p in b]
         return lims, ['Uniform' if p.fixed is None else 'Fixed' for p in b], [None] * len(lims)
 
+    def set_AstrometryOffset(self, b, **kw):
+        """block_repo.py:843-850."""
+        return [[-1e1, 1e1]] * 5, ['Uniform'] * 5, [None] * 5
+
+    def set_AstrometryJitter(self, b, **kw):
+        """block_repo.py:835-840 (Hipparcos, Gaia)."""
+        return [[0, 20], [0, 10]], ['Uniform', 'Uniform'], [None, None]
+
     def set_Acceleration(self, b, **kw):
         return [[-1, 1]] * b.number_, ['Uniform'] * b.number_, [None] * b.number_
 
@@ -385,12 +437,15 @@ def prior_struct(prior: str, limits, prargs) -> N.EmpPrior:
         return p
     if prior not in N.PRIOR_KIND:
         raise ValueError(f'prior {prior!r} is not on this path '
-                         '(Uniform, Normal, Jeffreys, Beta, Fixed)')
+                         '(Uniform, Normal, Jeffreys, Beta, Isotropic, Fixed)')
     low, high = float(limits[0]), float(limits[1])
     p.kind = N.PRIOR_KIND[prior]
     p.lo, p.hi = low, high
     if prior in ('Uniform', 'Jeffreys'):
         p.a0 = float(np.log(1 / (high - low)))
+    elif prior == 'Isotropic':
+        # log(sin(x) / 2) - logZ, logZ = log((cos lo - cos hi) / 2) (emp_model.py:96-99)
+        p.a0 = float(np.log(0.5 * (np.cos(low) - np.cos(high))))
     elif prior == 'Normal':
         mu, s = float(prargs[0]), float(prargs[1])
         a, b = (low - mu) / s, (high - mu) / s

@@ -1,4 +1,4 @@
-"""Post-run reductions the reference asks of its sampler (host, numpy).
+"""Post-run estimators the reference asks of its sampler.
 
 * ``integrated_time`` -- emcee's integrated autocorrelation time estimator
   (Sokal's automated windowing with constant ``c``), which EMPEROR reads
@@ -11,6 +11,13 @@
   ``sampler.get_evidence_ss`` when EMPEROR's ``evidence_method`` is 'ss'
   (``emp.py:1431-1441``).
 * ``model_stats`` -- chi2, AIC, BIC, HQIC, RMSE of a fit (``emp.py:1187-1210``).
+* ``hdi_of_samples`` / ``hdi_of_chain`` -- highest-density intervals of the
+  posterior summaries (``math_utils.py:72-105``).
+
+The sampler reduces its histories on the device (``emp_ladder_sums``,
+``emp_autocorr``); ``ti_from_means``, ``ss_from_sums`` and ``tau_from_acf``
+finish the estimators from those summaries, and the array forms above are
+the same estimators on host arrays.
 """
 from __future__ import annotations
 
@@ -41,8 +48,30 @@ def _auto_window(taus, c):
     return len(taus) - 1
 
 
+def tau_from_acf(f, c=5):
+    """(tau, window found) from a walker-averaged autocorrelation f [lags]:
+    taus = 2 cumsum(f) - 1, the window the first lag m with m >= c taus[m]
+    (Sokal's automated windowing).  ``found`` is False when no lag of f
+    satisfies it (then tau is taken at the last lag, as emcee does for the
+    full series)."""
+    taus = 2.0 * np.cumsum(f) - 1.0
+    m = np.arange(len(taus)) < c * taus
+    if np.any(~m):
+        return float(taus[int(np.argmin(m))]), True
+    return float(taus[-1]), False
+
+
+def check_tau(tau, n_t, tol=50, quiet=False):
+    if tol > 0 and np.any(tol * np.asarray(tau) > n_t):
+        msg = (f'the chain is shorter than {tol} times the integrated autocorrelation '
+               f'time; N/{tol} = {n_t / tol:.0f}, tau = {tau}')
+        if not quiet:
+            raise RuntimeError(msg)
+
+
 def integrated_time(x, c=5, tol=50, quiet=False):
-    """tau per parameter of a chain x [steps, walkers, ndim]."""
+    """tau per parameter of a chain x [steps, walkers, ndim] (host; the
+    sampler computes the autocorrelation on the device, emp_autocorr)."""
     x = np.asarray(x, dtype=np.float64)
     if x.ndim == 1:
         x = x[:, None, None]
@@ -55,13 +84,8 @@ def integrated_time(x, c=5, tol=50, quiet=False):
         for k in range(n_w):
             f += autocorr_1d(x[:, k, d])
         f /= n_w
-        taus = 2.0 * np.cumsum(f) - 1.0
-        tau[d] = taus[_auto_window(taus, c)]
-    if tol > 0 and np.any(tol * tau > n_t):
-        msg = (f'the chain is shorter than {tol} times the integrated autocorrelation '
-               f'time; N/{tol} = {n_t / tol:.0f}, tau = {tau}')
-        if not quiet:
-            raise RuntimeError(msg)
+        tau[d] = tau_from_acf(f, c)[0]
+    check_tau(tau, n_t, tol, quiet)
     return tau
 
 
@@ -76,6 +100,13 @@ def thermodynamic_integration(betas, log_like, pchip=True):
     betas = np.asarray(betas, dtype=np.float64)
     ll = np.asarray(log_like, dtype=np.float64).reshape(len(betas), -1)
     mean = np.array([np.mean(r[np.isfinite(r)]) if np.any(np.isfinite(r)) else -np.inf for r in ll])
+    return ti_from_means(betas, mean, pchip)
+
+
+def ti_from_means(betas, mean, pchip=True):
+    """``thermodynamic_integration`` from the per-temperature means."""
+    betas = np.asarray(betas, dtype=np.float64)
+    mean = np.asarray(mean, dtype=np.float64)
     order = np.argsort(betas)
     b, m = betas[order], mean[order]
     if b[0] > 0:
@@ -173,3 +204,39 @@ def model_stats(residuals, err2, ndim, like_max, flags=None, nins=1):
     out['BIC'] = np.log(n) * ndim - 2 * like_max
     out['HQIC'] = 2 * ndim * np.log(np.log(n)) - 2 * like_max
     return out
+
+
+def stepping_stone_plan(betas):
+    """The stones of ``stepping_stone``: (order of the ladder ascending in
+    beta, source temperature of each stone, its beta step)."""
+    betas = np.asarray(betas, dtype=np.float64)
+    order = np.argsort(betas)
+    b = betas[order]
+    src = np.array([order[k - 1] for k in range(1, len(b))], dtype=np.int32)
+    step = np.array([b[k] - b[k - 1] for k in range(1, len(b))], dtype=np.float64)
+    return order, src, step
+
+
+def ss_from_sums(betas, temp_sums, stone_sums):
+    """``stepping_stone`` from the device summaries: temp_sums [T][2] (sum,
+    count of finite log L per temperature) and stone_sums [K][4] (max of
+    d L, sum exp(d L - max), sum of its square, count) of the stones of
+    ``stepping_stone_plan``."""
+    betas = np.asarray(betas, dtype=np.float64)
+    order, src, step = stepping_stone_plan(betas)
+    b0 = betas[order[0]]
+    logz, var = 0.0, 0.0
+    if b0 > 0:
+        s, n = temp_sums[order[0]]
+        if n == 0:
+            return -np.inf, np.inf
+        logz += b0 * s / n
+    for m, s1, s2, n in stone_sums:
+        if n == 0:
+            return -np.inf, np.inf
+        mw = s1 / n
+        logz += m + np.log(mw)
+        if n > 1:
+            vw = (s2 - n * mw * mw) / (n - 1)
+            var += max(vw, 0.0) / (n * mw * mw)
+    return float(logz), float(np.sqrt(var))

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define EMP_ABI_VERSION 3
+#define EMP_ABI_VERSION 4
 
 #define EMP_MAX_PARAMS   160   /* full theta length incl. fixed parameters */
 #define EMP_MAX_PLANETS  16
@@ -70,6 +70,8 @@ extern "C" {
 #define EMP_PREC_FP64   0  /* plain FP64 everywhere */
 #define EMP_PREC_MIXED  1  /* FP32 Kepler solve + RV sum; float-float phase;
                               compensated FP32 per-lane sums, FP64 across lanes */
+/* emp_set_launch target of the adjoint kernel (emp_logpost_grad) */
+#define EMP_LAUNCH_GRAD 2
 
 /* prior kinds (support/priors/<Name>.prior) */
 #define EMP_PRIOR_UNIFORM   0
@@ -77,6 +79,7 @@ extern "C" {
 #define EMP_PRIOR_JEFFREYS  2
 #define EMP_PRIOR_BETA      3
 #define EMP_PRIOR_NONE      4
+#define EMP_PRIOR_ISOTROPIC 5   /* ln(sin(x)/2) - logZ, a0 = logZ (Isotropic.prior) */
 
 typedef struct emp_prior {
     int32_t kind;
@@ -84,7 +87,8 @@ typedef struct emp_prior {
     double lo, hi;        /* support, inclusive (the reference's `limits`) */
     double a0, a1, a2;    /* Uniform/Jeffreys: a0 = ln(1/(hi-lo))
                              Normal: a0 = mu, a1 = 1/s, a2 = ln(s sqrt(2 pi)) + logZ
-                             Beta:   a0 = a, a1 = b, a2 = ln B(a, b) */
+                             Beta:   a0 = a, a1 = b, a2 = ln B(a, b)
+                             Isotropic: a0 = ln((cos lo - cos hi) / 2) */
 } emp_prior;
 
 /*
@@ -148,7 +152,36 @@ typedef struct emp_model_desc {
     int32_t hill_mask;
     int32_t _pad3;
     double  hill_starmass;
+    /* joint RV + astrometry likelihood (support/likelihoods/a00.like): with
+       am_on the log-likelihood adds the astrometric term of the data given to
+       emp_set_astrometry; every Keplerian block then has seven slots (P, K,
+       phase, e, w, inclination, node: akep00.model with parameterisation 0) */
+    int32_t am_on;
+    int32_t am_offset_slot;       /* offsets RA, DE, PLX, pm RA, pm DE (mas, mas/yr) */
+    int32_t am_jitter_slot;       /* jitters of Hipparcos and Gaia */
+    int32_t _pad4;
 } emp_model_desc;
+
+/*
+ * Astrometric data of a joint fit (DataWrapper's AM mode,
+ * qol_utils.py:103-455; the generated script's AM prologue,
+ * emp_model.py:609-706), host FP64 arrays:
+ */
+typedef struct emp_am_desc {
+    int32_t n_hipp;               /* Hipparcos abscissae */
+    int32_t n_gost;               /* Gaia scan epochs (before the DR3 baseline) */
+    const double* catalogs;       /* [3][7] Hipparcos, DR2, DR3: ref epoch, ra, dec
+                                     (deg), parallax (mas), pmra, pmdec (mas/yr), rv */
+    const double* inv_cov;        /* [3][5][5] inverse catalogue covariances */
+    const double* log_det_cov;    /* [3] */
+    const double* astro_gost;     /* [2][5] DR2, DR3 solutions relative to DR3 */
+    const double* hipp;           /* [7][n_hipp]: BJD, EPOCH, PARF, CPSI, SPSI, RES, SRES */
+    const double* gost;           /* [4][n_gost]: BJD, CPSI, SPSI, PARF */
+    const double* gsv;            /* [2][5][n_gost]: DR2, DR3 solution vectors
+                                     (pseudo-inverse of the release's design
+                                     matrix) at its epochs, 0 at the others */
+    double common_t;              /* the RV time origin (BJD) */
+} emp_am_desc;
 
 /*
  * One or more RV systems, ragged.  System s owns epochs
@@ -210,14 +243,24 @@ int emp_logpost(emp_handle* h, const double* theta, int B,
    adjoint of support/likelihoods/00.like:3-5 through my_model,
    emp_model.py:706-781) for a batch of B walkers: logl/logprior [B] and
    grad_logl/grad_logprior [B][n_free] (device, FP64), with respect to the
-   free parameters.  FP32 forward and adjoint per epoch, float-float sums
-   finished in FP64.  Keplerian parameterisations 0 and 1, up to 4
-   instruments, MA order <= 2, whole series <= shared memory (~8000 epochs
-   with MA(1)); EMP_E_UNSUPPORTED / EMP_E_SIZE otherwise.  Walkers outside
-   the prior support get logl = -inf and a zero logl gradient. */
+   free parameters.  Planet constants in float-float from FP64, FP32
+   per-epoch forward and adjoint terms, float-float sums finished in FP64.
+   Every Keplerian parameterisation (kep00-kep07.model), sinusoid and
+   magnetic-cycle terms, acceleration, up to 4 instruments, MA order <= 2,
+   any number of epochs (streamed in tiles).  With MA and a series longer
+   than one tile the handle keeps a residual buffer of B * epochs floats,
+   allocated by the first call that needs more (make that call outside any
+   stream capture).  Walkers outside the prior support get logl = -inf and
+   a zero logl gradient.  GP models and batch handles: EMP_E_UNSUPPORTED. */
 int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl,
                      double* logprior, double* grad_logl, double* grad_logprior,
                      void* stream);
+
+/* Replaces: the astrometric data prologue of the generated script
+   (emp_model.py:609-706) for a handle whose model has am_on: copies the
+   arrays to the device.  Call once after emp_create, outside any stream
+   capture.  One-system handles only. */
+int emp_set_astrometry(emp_handle* h, const emp_am_desc* am);
 
 /* Replaces: my_model(theta) -> (model0, err20) (emp_model.py:706-781) for a
    batch of B walkers; model/err2 are device [B][n] in the dataset's input
@@ -335,11 +378,36 @@ int emp_pt_run_host(emp_handle* h, const emp_pt_state* st,
 int emp_pt_evaluate(emp_handle* h, const emp_pt_state* st, void* stream);
 
 /* Lanes per walker (4, 8, 16, 32) and epoch tile used by emp_logpost /
-   emp_pt_*; 0 = library default.  Set by the autotuner. */
+   emp_pt_*; 0 = library default.  Set by the autotuner.  With precision =
+   EMP_LAUNCH_GRAD: the adjoint kernel's epoch tile (lanes 0 or 32; tile 0
+   = chosen per call, else a multiple of 32 up to 4096). */
 int emp_set_launch(emp_handle* h, int precision, int lanes_per_walker,
                    int tile_epochs);
 int emp_get_launch(emp_handle* h, int precision, int* lanes_per_walker,
                    int* tile_epochs);
+
+/* Replaces: the per-temperature summaries behind reddemcee's
+   get_evidence_ti / get_evidence_ss (read by postprocess, emp.py:1431-1447)
+   from the log-likelihood history log_like [rows][ntemps][nwalkers] (device,
+   the rows discard, discard+thin, ...): out_temp [ntemps][2] = sum and count
+   of the finite values per temperature; for each of nstones stepping stones
+   (samples of temperature stone_src[k], step stone_d[k] in beta; device
+   arrays) out_stone [nstones][4] = max of d L, sum of exp(d L - max), sum
+   of its square, count.  FP64, compensated sums. */
+int emp_ladder_sums(const double* log_like, int rows, int ntemps, int nwalkers,
+                    int discard, int thin, const int* stone_src,
+                    const double* stone_d, int nstones, double* out_temp,
+                    double* out_stone, void* stream);
+
+/* Replaces: the autocorrelation function behind get_autocorr_time
+   (emp.py:1372-1385; emcee's estimator): for the chain [rows][ntemps]
+   [nwalkers][ndim] (device; rows discard, discard+thin, ...), f [ntemps]
+   [ndim][maxlag] = the walkers' mean of each series' autocorrelation at lags
+   0..maxlag-1 (mean removed, normalised by lag 0; a constant series counts
+   as 1).  The integrated time and its window follow on the host.  At most
+   51200 kept rows (EMP_E_SIZE). */
+int emp_autocorr(const double* chain, int rows, int ntemps, int nwalkers, int ndim,
+                 int discard, int thin, int maxlag, double* f, void* stream);
 
 /* Measured CUDA-core throughput (FMA chains) for the roofline:
    fp32/fp64 FLOP/s of this device.  Launches a short probe kernel. */

@@ -2,8 +2,9 @@
 INFRASTRUCTURE ONLY).
 
 A batched, differentiable restatement of the same generated functions as
-``oracle.rv`` (``support/models/kep00/kep01.model``, ``offset00.model``,
-``jitter00.model``, the MA recurrence of ``moav01.model``, ``acc.model``,
+``oracle.rv`` (``support/models/kep00-kep07.model``, ``sinusoid00.model``,
+``magneticcycle00.model``, ``offset00.model``, ``jitter00.model``, the MA
+recurrence of ``moav01.model``, ``acc.model``,
 ``support/likelihoods/00.like``) in FP64 torch, so that
 ``torch.autograd.grad`` gives the reference gradient the adjoint kernel is
 checked against.  The Kepler equation is solved without gradient and then
@@ -65,18 +66,55 @@ class TorchRV:
         return torch.stack(cols, dim=1)
 
     @staticmethod
+    def elements(par, v):
+        """(period, K, phase, tp or None, e, cos w, sin w) of one Keplerian
+        block [B, 5], differentiable: the prologues of kep00-kep07.model
+        (the angles of (S, C) and (As, Ac) through their cosines and sines
+        directly; a 2 pi shift of the phase leaves the model unchanged)."""
+        c = [v[:, i:i + 1] for i in range(5)]
+        per = torch.exp(c[0]) if par in (2, 6, 7) else c[0]
+        tp = None
+        if par in (0, 3, 6):
+            e, w = c[3], c[4]
+            cw, sw = torch.cos(w), torch.sin(w)
+        else:
+            S, C = c[3], c[4]
+            e = S * S + C * C
+            r = torch.sqrt(e)
+            small = e < (1e-5 if par in (2, 4) else 1e-6)
+            one = torch.ones_like(e)
+            cw = torch.where(small, one, C / torch.where(small, one, r))
+            sw = torch.where(small, torch.zeros_like(e), S / torch.where(small, one, r))
+        if par == 2:
+            As, Ac = c[1], c[2]
+            K = As * As + Ac * Ac
+            phase = torch.atan2(As, Ac)
+        else:
+            K = c[1]
+            phase = c[2]
+        if par in (3, 4):
+            tp, phase = c[2], None
+        return per, K, phase, tp, e, cw, sw
+
+    @staticmethod
     def kepler(M, e):
-        with torch.no_grad():
-            Mr = torch.remainder(M + np.pi, 2 * np.pi) - np.pi
-            E = Mr + 0.85 * e * torch.sign(torch.sin(Mr))
-            for _ in range(60):
-                f = E - e * torch.sin(E) - Mr
-                E = E - f / (1 - e * torch.cos(E))
-            E = E + (M - Mr)
-        # one Newton step with the graph: exact first derivatives at the root
+        # the iterations on detached values (no derivative through them, in
+        # reverse or forward mode), then one Newton step with the graph:
+        # exact first derivatives at the root
+        Md, ed = M.detach(), e.detach()
+        Mr = torch.remainder(Md + np.pi, 2 * np.pi) - np.pi
+        E = Mr + 0.85 * ed * torch.sign(torch.sin(Mr))
+        for _ in range(60):
+            f = E - ed * torch.sin(E) - Mr
+            E = E - f / (1 - ed * torch.cos(E))
+        E = E + (Md - Mr)
         return E - (E - e * torch.sin(E) - M) / (1 - e * torch.cos(E))
 
     def loglike(self, theta):
+        return torch.sum(self.terms(theta), dim=1) + self.const
+
+    def terms(self, theta):
+        """Per-epoch terms -(r_i^2 / err2_i + ln err2_i) / 2 [B, n]."""
         th = self.full(theta)
         B = th.shape[0]
         X = self.X[None, :]
@@ -86,25 +124,19 @@ class TorchRV:
         for b, sl in zip(self.blocks, self.slices):
             v = th[:, sl]
             if b['type'] == 'Keplerian':
-                par = b['parameterisation']
-                if par == 1:
-                    P, K, phase, S, C = [v[:, i:i + 1] for i in range(5)]
-                    e = S * S + C * C
-                    r = torch.sqrt(e)
-                    small = e < 1e-6
-                    cw = torch.where(small, torch.ones_like(e), C / torch.where(small, torch.ones_like(r), r))
-                    sw = torch.where(small, torch.zeros_like(e), S / torch.where(small, torch.ones_like(r), r))
-                elif par == 0:
-                    P, K, phase, e, w = [v[:, i:i + 1] for i in range(5)]
-                    cw, sw = torch.cos(w), torch.sin(w)
-                else:
-                    raise ValueError('gradient reference: parameterisations 0 and 1')
-                M = 2 * np.pi / P * X + phase
+                per, K, phase, tp, e, cw, sw = self.elements(b['parameterisation'], v)
+                M = 2 * np.pi / per * (X - tp) if tp is not None else 2 * np.pi / per * X + phase
                 E = self.kepler(M, e.expand_as(M))
                 cE, sE = torch.cos(E), torch.sin(E)
                 D = 1 - e * cE
                 q = torch.sqrt(1 - e * e)
                 model = model + K * (((cE - e) * cw - q * sE * sw) / D + e * cw)
+            elif b['type'] == 'Sinusoid':                     # sinusoid00.model
+                P, A, phase = [v[:, i:i + 1] for i in range(3)]
+                model = model + A * torch.cos(2 * np.pi / P * X + phase)
+            elif b['type'] == 'MagneticCycle':                # magneticcycle00.model
+                P, A1, A2, ph1, ph2 = [v[:, i:i + 1] for i in range(5)]
+                model = model + A1 * torch.cos(np.pi / P * X + ph1) + A2 * torch.cos(2 * np.pi / P * X + ph2)
             elif b['type'] == 'Acceleration':
                 x = X - X[:, :1]
                 pv = torch.zeros_like(model)
@@ -121,7 +153,7 @@ class TorchRV:
                     resid = self._moav(resid, v)
         if resid is None:
             resid = self.Y[None, :] - model
-        return -0.5 * torch.sum(resid ** 2 / err2 + torch.log(err2), dim=1) + self.const
+        return -0.5 * (resid ** 2 / err2 + torch.log(err2))
 
     def _moav(self, resid, v):
         q, is_global, seqs = self.ma
@@ -141,6 +173,22 @@ class TorchRV:
                 prev.append(x)
                 out[i] = x
         return torch.stack(out, dim=1)
+
+    def condition(self, theta, chunk=100):
+        """sum_i |d term_i / d theta_j| [B, ndim]: the size of the summands of
+        each gradient component (forward-mode derivatives of the per-epoch
+        terms); a component computed from rounded terms is only defined to
+        the terms' rounding times this."""
+        th = torch.as_tensor(theta, dtype=torch.float64, device=self.dev)
+        out = torch.zeros_like(th)
+        for b0 in range(0, th.shape[0], chunk):
+            x = th[b0:b0 + chunk]
+            for j in range(x.shape[1]):
+                t = torch.zeros_like(x)
+                t[:, j] = 1.0
+                _, d = torch.func.jvp(self.terms, (x,), (t,))
+                out[b0:b0 + chunk, j] = d.abs().sum(1)
+        return out.cpu().numpy()
 
     def grad(self, theta):
         th = torch.as_tensor(theta, dtype=torch.float64, device=self.dev).clone().requires_grad_(True)

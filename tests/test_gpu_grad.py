@@ -2,15 +2,18 @@
 autograd reference and central finite differences; the autograd wrapper;
 multistart MAP.
 
-Gradient error measure: per walker, the relative error of the gradient with
-respect to the prior-width-scaled parameters (theta_j - lo_j)/(hi_j - lo_j),
-e = ||(g - g_ref) w|| / ||g_ref w|| with w = hi - lo.  Asserted on the C4
-model at 1000 prior draws: median e <= 1e-6, 99th percentile and maximum
-<= 1e-5 (measured: 1.6e-7, 1.7e-6, 3.0e-6).  The forward pass is FP32:
-components whose per-epoch terms cancel strongly (period and phase, whose
-terms oscillate over hundreds of orbital cycles) inherit the ~1e-7
-precision of the FP32 mean anomaly amplified by the cancellation; their
-component-wise errors are printed.
+Gradient tolerance, component by component: |g_j - ref_j| <= 1e-5 |ref_j|
++ 1e-7 cond_j, where cond_j = sum_i |d term_i / d theta_j| is the size of the
+summands of component j (the per-epoch log-likelihood terms, from forward-mode
+derivatives of the FP64 reference).  The kernel's per-epoch terms are FP32,
+so a component is defined to about the FP32 rounding of its summands times
+their size: where the summands cancel (|ref_j| << cond_j, e.g. a period
+component whose terms oscillate over hundreds of orbits) that, not 1e-5
+|ref_j|, bounds it.  With an MA model the residual and adjoint recurrences
+run in FP32 and carry their rounding along runs where Phi exp(-dt/tau) is
+close to 1, so the cond term is 5e-6 there (measured up to 3.1e-6; 2.2e-7
+without MA).  The plain component-wise relative errors (median, 99th
+percentile, maximum) are printed.
 """
 import numpy as np
 import pytest
@@ -28,19 +31,33 @@ from tests.golden.cases import kat_case_models, model_51peg
 pytestmark = pytest.mark.gpu
 
 GRAD_RTOL = 1e-5
+COND_TOL = 5e-7
+COND_TOL_MA = 5e-6
+CASES = ['51peg_k0', '51peg_k1_p0', '51peg_k1_p1', '51peg_k1_p2', '51peg_k1_p3', '51peg_k1_p4',
+         '51peg_k1_p6', '51peg_k1_p7', '51peg_fixed_acc', '51peg_gma2', '51peg_k1_sin',
+         '51peg_k1_cycle_gma1', '51peg_k2_hill', '51peg_ma2_inst', 'c2_ma1', 'c2_ma1_quirk']
 
 
 def _rel_err(g, ref):
-    """component-wise, with a floor for components near zero (reported)"""
-    floor = 1e-3 * np.max(np.abs(ref), axis=1, keepdims=True)
-    return np.abs(g - ref) / np.maximum(np.abs(ref), floor)
+    """plain component-wise relative error (reported)"""
+    return np.abs(g - ref) / np.abs(ref)
 
 
-def _scaled_err(g, ref, model):
-    """norm-wise error of the width-scaled gradient (asserted)"""
-    lim = model.limits_free()
-    w = (lim[:, 1] - lim[:, 0])[None, :]
-    return np.linalg.norm((g - ref) * w, axis=1) / np.linalg.norm(ref * w, axis=1)
+def _ctol(model):
+    live_ma = any(b.type_ == 'MOAV' and (b.is_global or not model.moav_reference_quirk) for b in model.blocks)
+    return COND_TOL_MA if live_ma else COND_TOL
+
+
+def _check(name, g, ref, cond, rtol=GRAD_RTOL, ctol=COND_TOL):
+    """|g - ref| <= rtol |ref| + ctol cond, component by component."""
+    err = np.abs(g - ref)
+    bound = rtol * np.abs(ref) + ctol * cond
+    rel = _rel_err(g, ref)
+    print(f'{name}: component relative error median {np.median(rel):.2e} p99 {np.percentile(rel, 99):.2e} '
+          f'max {rel.max():.2e}; error/cond max {np.max(err / cond):.2e}; bound used max '
+          f'{np.max(err / bound):.3f}')
+    bad = np.argwhere(err > bound)
+    assert bad.size == 0, (name, bad[:5], err[tuple(bad[0])], bound[tuple(bad[0])])
 
 
 def _prior_draws(model, o, n, rng, shrink_ecc=0.7):
@@ -56,26 +73,44 @@ def _prior_draws(model, o, n, rng, shrink_ecc=0.7):
     return np.array(out)
 
 
-@pytest.mark.parametrize('name', ['51peg_k1_p1', '51peg_k1_p0', '51peg_fixed_acc', '51peg_gma2',
-                                  'c2_ma1', 'c2_ma1_quirk', '51peg_k0'])
+def _grad(ctx, th):
+    ll, lp, gl, gp = ctx.logpost_grad(torch.as_tensor(th, dtype=torch.float64, device='cuda:0'))
+    torch.cuda.synchronize()
+    return ll.cpu().numpy(), lp.cpu().numpy(), gl.cpu().numpy(), gp.cpu().numpy()
+
+
+@pytest.mark.parametrize('name', CASES)
 def test_gradient_matches_fp64_autograd(peg_arr, lib, cuda, name):
     m, d, _ = kat_case_models(peg_arr)[name]
     o = OracleRV(m.spec(), d.as_dict())
     th = _prior_draws(m, o, 16, np.random.default_rng(3))
     ctx = Context(m, 'cuda:0')
-    t = torch.as_tensor(th, dtype=torch.float64, device='cuda:0')
-    ll, lp, gl, gp = ctx.logpost_grad(t)
-    torch.cuda.synchronize()
-    ll, gl = ll.cpu().numpy(), gl.cpu().numpy()
+    ll, lp, gl, _ = _grad(ctx, th)
     want_ll = np.array([o.my_likelihood(x) for x in th])
     assert np.max(np.abs(ll - want_ll) / np.abs(want_ll)) <= 1e-6
-    ref_ll, ref_g = TorchRV(m.spec(), d.as_dict()).grad(th)
-    err = _rel_err(gl, ref_g)
-    serr = _scaled_err(gl, ref_g, m)
-    print(name, 'scaled norm error max', serr.max(), '| component error max', err.max(),
-          'median', np.median(err))
-    assert np.median(serr) <= 1e-6 and serr.max() <= 2e-5, (name, np.median(serr), serr.max())
-    np.testing.assert_allclose(lp.cpu().numpy(), [o.my_prior(x) for x in th], rtol=1e-13, atol=1e-13)
+    ref = TorchRV(m.spec(), d.as_dict(), device='cuda:0')
+    _, ref_g = ref.grad(th)
+    _check(name, gl, ref_g, ref.condition(th), ctol=_ctol(m))
+    np.testing.assert_allclose(lp, [o.my_prior(x) for x in th], rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize('name', ['51peg_k1_p1', '51peg_gma2', '51peg_ma2_inst', 'c2_ma1', '51peg_fixed_acc'])
+def test_gradient_over_several_tiles(peg_arr, lib, cuda, name):
+    """The series streamed in tiles of 64 epochs (the MA state and adjoints
+    carried across tiles, the residuals through the handle's buffer) gives
+    the one-tile gradient."""
+    m, d, _ = kat_case_models(peg_arr)[name]
+    o = OracleRV(m.spec(), d.as_dict())
+    th = _prior_draws(m, o, 12, np.random.default_rng(8))
+    ctx = Context(m, 'cuda:0')
+    ll1, _, g1, _ = _grad(ctx, th)
+    N.call('emp_set_launch', ctx.h, N.EMP_LAUNCH_GRAD, 32, 64)
+    ll2, _, g2, _ = _grad(ctx, th)
+    N.call('emp_set_launch', ctx.h, N.EMP_LAUNCH_GRAD, 0, 0)
+    np.testing.assert_allclose(ll2, ll1, rtol=1e-7)
+    ref = TorchRV(m.spec(), d.as_dict(), device='cuda:0')
+    _, ref_g = ref.grad(th)
+    _check(name + ' (64-epoch tiles)', g2, ref_g, ref.condition(th), ctol=_ctol(m))
 
 
 def test_prior_gradient(peg_arr, lib, cuda):
@@ -83,8 +118,7 @@ def test_prior_gradient(peg_arr, lib, cuda):
     o = OracleRV(m.spec(), d.as_dict())
     th = _prior_draws(m, o, 8, np.random.default_rng(4))
     ctx = Context(m, 'cuda:0')
-    _, _, _, gp = ctx.logpost_grad(torch.as_tensor(th, device='cuda:0'))
-    gp = gp.cpu().numpy()
+    _, _, _, gp = _grad(ctx, th)
     for b, x in enumerate(th):
         for j in range(len(x)):
             h = 1e-6 * max(1.0, abs(x[j]))
@@ -95,42 +129,72 @@ def test_prior_gradient(peg_arr, lib, cuda):
             assert gp[b, j] == pytest.approx(fd, abs=1e-6, rel=1e-6)
 
 
+def _richardson(f, x, j, width):
+    """d f / d x_j by Richardson-extrapolated central differences at
+    decreasing steps; the pair of estimates that agrees best (truncation
+    gone, rounding not yet dominant) gives the value and its spread."""
+    def D(h):
+        a, c = x.copy(), x.copy()
+        a[j] += h
+        c[j] -= h
+        return (f(a) - f(c)) / (2 * h)
+    R = [(4 * D(h / 2) - D(h)) / 3 for h in (10.0 ** -k * width for k in range(5, 10))]
+    k = int(np.argmin([abs(R[i] - R[i + 1]) for i in range(len(R) - 1)]))
+    return 0.5 * (R[k] + R[k + 1]), abs(R[k] - R[k + 1])
+
+
 def test_c4_gradient_at_1000_prior_draws(lib, cuda):
-    """5 Keplerians, 3 instruments with offset, jitter, MA(1) each, N=4096."""
+    """5 Keplerians, 3 instruments with offset, jitter, MA(1) each, N=4096
+    (the gradient workload): 1000 prior draws against the FP64 reference;
+    three draws against Richardson central differences of the oracle on
+    every component, periods included."""
     model, data, setup, truth = synth.build_model('c4', seed=11)
     o = OracleRV(model.spec(), data.as_dict())
     th = _prior_draws(model, o, 1000, np.random.default_rng(12), shrink_ecc=0.6)
     ctx = Context(model, 'cuda:0')
-    ll, lp, gl, gp = ctx.logpost_grad(torch.as_tensor(th, device='cuda:0'))
-    torch.cuda.synchronize()
+    ll, lp, g, gp = _grad(ctx, th)
     ref = TorchRV(model.spec(), data.as_dict(), device='cuda:0')
     ref_ll, ref_g = ref.grad(th)
-    rel_ll = np.abs(ll.cpu().numpy() - ref_ll) / np.abs(ref_ll)
+    rel_ll = np.abs(ll - ref_ll) / np.abs(ref_ll)
     assert rel_ll.max() <= 1e-6
-    err = _rel_err(gl.cpu().numpy(), ref_g)
-    serr = _scaled_err(gl.cpu().numpy(), ref_g, model)
-    print('C4 gradient: scaled norm error max', serr.max(), 'median', np.median(serr),
-          '| component error max', err.max(), 'median', np.median(err))
-    print('C4 gradient: 99th percentile', np.percentile(serr, 99))
-    assert np.median(serr) <= 1e-6
-    assert np.percentile(serr, 99) <= GRAD_RTOL
-    assert serr.max() <= GRAD_RTOL
-    # central finite differences (h = 1e-6 relative) on the FP64 oracle for a
-    # few draws; period components excluded (their second derivative makes
-    # the 1e-6 step's truncation error larger than the tolerance)
-    g = gl.cpu().numpy()
-    names = [p.name for p in model.free_parameters()]
+    _check('C4 (1000 prior draws)', g, ref_g, ref.condition(th, chunk=1000), ctol=_ctol(model))
+    rel = _rel_err(g, ref_g)
+    assert np.median(rel) <= 1e-6
+    lim = model.limits_free()
     for b in range(3):
         x = th[b]
         for j in range(len(x)):
-            if names[j].startswith('Period'):
-                continue
-            h = 1e-6 * max(1.0, abs(x[j]))
-            a, c = x.copy(), x.copy()
-            a[j] += h
-            c[j] -= h
-            fd = (o.my_likelihood(a) - o.my_likelihood(c)) / (2 * h)
-            assert abs(g[b, j] - fd) <= 1e-3 * max(abs(fd), 1e-2 * np.max(np.abs(g[b]))), (names[j], g[b, j], fd)
+            fd, spread = _richardson(o.my_likelihood, x, j, lim[j, 1] - lim[j, 0])
+            assert abs(g[b, j] - fd) <= 1e-5 * abs(fd) + spread + 1e-7 * np.max(np.abs(g[b])), (j, g[b, j], fd)
+
+
+def test_c5_shape_gradient(lib, cuda):
+    """7 Keplerians, 4 instruments with per-instrument MA(2), N = 16384:
+    the series spans 16 tiles, the residuals go through the handle's
+    buffer.  Three points (two near the generating values, one prior
+    draw); the FP64 reference's recurrence over 16384 epochs makes the
+    forward-mode condition too slow here, so the check is the width-scaled
+    norm-wise error (<= 1e-5) with the component-wise errors printed; the
+    component-wise bound is asserted on the C4 workload above."""
+    model, data, setup, truth = synth.build_model('c5', seed=5)
+    o = OracleRV(model.spec(), data.as_dict())
+    rng = np.random.default_rng(21)
+    lim = model.limits_free()
+    near = np.clip(truth + 1e-4 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(2, len(truth))),
+                   lim[:, 0], lim[:, 1])
+    th = np.concatenate([near, _prior_draws(model, o, 1, rng, shrink_ecc=0.6)])
+    ctx = Context(model, 'cuda:0')
+    ll, lp, g, _ = _grad(ctx, th)
+    want = np.array([o.my_likelihood(x) for x in th])
+    assert np.max(np.abs(ll - want) / np.abs(want)) <= 1e-6
+    ref = TorchRV(model.spec(), data.as_dict(), device='cuda:0')
+    _, ref_g = ref.grad(th)
+    w = (lim[:, 1] - lim[:, 0])[None, :]
+    scaled = np.linalg.norm((g - ref_g) * w, axis=1) / np.linalg.norm(ref_g * w, axis=1)
+    rel = _rel_err(g, ref_g)
+    print(f'C5 shape: width-scaled norm error max {scaled.max():.2e}; component relative error median '
+          f'{np.median(rel):.2e} p99 {np.percentile(rel, 99):.2e} max {rel.max():.2e}')
+    assert scaled.max() <= 1e-5
 
 
 def test_autograd_function(peg_arr, lib, cuda):
@@ -157,6 +221,6 @@ def test_multistart_map_finds_the_51peg_fit(peg_arr, lib, cuda):
     best = res['theta'][int(np.argmax(lp))].cpu().numpy()
     # the oracle's maximum posterior with the current Normal normaliser
     assert lp.max() == pytest.approx(o.my_likelihood(best) + o.my_prior(best), abs=1e-4)
-    # FP32-forward gradients stall L-BFGS within ~0.1 of the FP64 optimum
-    assert lp.max() >= -881.52 - 0.1
+    print('51 Peg multistart MAP: best log posterior', lp.max())
+    assert lp.max() >= -881.52 - 0.01
     assert best[0] == pytest.approx(4.2308, abs=5e-4)
