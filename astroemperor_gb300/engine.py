@@ -79,6 +79,28 @@ class Context:
         h = C.c_void_p()
         N.call('emp_create', C.byref(self.md), C.byref(ds), C.byref(h))
         self.h = h
+        if getattr(model, 'am_data', None) is not None and self.md.am_on:
+            self._set_astrometry(model.am_data)
+
+    def _set_astrometry(self, am):
+        """Upload the astrometric data of a joint fit (emp_set_astrometry)."""
+        f64 = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+        ng = am.n_gost
+        gsv = np.zeros((2, 5, ng))
+        for c, cat in enumerate(('GDR2', 'GDR3')):
+            gsv[c][:, am.masks[cat]] = am.gsv[cat]
+        arrs = {
+            'catalogs': f64(am.catalogs), 'inv_cov': f64(am.inv_cov), 'log_det_cov': f64(am.log_det_cov),
+            'astro_gost': f64(am.astro_gost),
+            'hipp': f64(np.stack([am.hipp[k] for k in ('BJD', 'EPOCH', 'PARF', 'CPSI', 'SPSI', 'RES', 'SRES')])),
+            'gost': f64(np.stack([am.gost[k] for k in ('BJD', 'CPSI', 'SPSI', 'parf')])),
+            'gsv': f64(gsv)}
+        d = N.EmpAmDesc()
+        d.n_hipp, d.n_gost = am.n_hipp, ng
+        for k, v in arrs.items():
+            setattr(d, k, v.ctypes.data)
+        d.common_t = float(am.common_t)
+        N.call('emp_set_astrometry', self.h, C.byref(d))
 
     def close(self):
         if getattr(self, 'h', None):

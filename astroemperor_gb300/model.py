@@ -466,12 +466,15 @@ class ReddModel:
     """
 
     HOT_TYPES = ('Keplerian', 'Acceleration', 'Offset', 'Jitter', 'MOAV', 'Sinusoid', 'MagneticCycle',
-                 'Celerite2')
+                 'Celerite2', 'AstrometryOffset', 'AstrometryJitter')
 
-    def __init__(self, blocks, data, moav_reference_quirk=False):
+    def __init__(self, blocks, data, moav_reference_quirk=False, am_data=None):
         self.blocks = list(blocks)
         self.data = data
         self.moav_reference_quirk = bool(moav_reference_quirk)
+        # astrometric data (astrometry.AMData) of a joint fit, with the
+        # AstrometryOffset / AstrometryJitter blocks
+        self.am_data = am_data
         self.refresh__()
 
     def __iter__(self):
@@ -504,6 +507,18 @@ class ReddModel:
         if gp and any(b.type_ == 'MOAV' and (b.is_global or not self.moav_reference_quirk)
                       for b in self.blocks):
             raise ValueError('a GP likelihood and a live MOAV block cannot be combined on this path')
+        am = [b for b in self.blocks if b.type_ in ('AstrometryOffset', 'AstrometryJitter')]
+        if am:
+            types = sorted(b.type_ for b in am)
+            if types != ['AstrometryJitter', 'AstrometryOffset']:
+                raise ValueError('astrometry needs one AstrometryOffset and one AstrometryJitter block')
+            if self.am_data is None:
+                raise ValueError('astrometry blocks without astrometric data (am_data)')
+            if gp:
+                raise ValueError('a GP likelihood and astrometry cannot be combined on this path')
+            for b in self.blocks:
+                if b.type_ == 'Keplerian' and not getattr(b, 'astrometry_bool', False):
+                    raise ValueError('with astrometry every Keplerian is an AstrometryKeplerianBlock')
         # the MOAV residual is taken after every mean-model block
         seen_moav = False
         for b in self.blocks:
@@ -522,6 +537,8 @@ class ReddModel:
             if b.type_ == 'Keplerian':
                 d['parameterisation'] = b.parameterisation
                 d['additional'] = [p.as_spec() for p in b.additional_parameters]
+                if getattr(b, 'astrometry_bool', False):
+                    d['astrometry'] = True
             if b.type_ == 'MOAV':
                 d['order'] = b.moav
                 d['global'] = b.is_global
@@ -575,6 +592,7 @@ class ReddModel:
         md.n_free = self.ndim__
         md.n_ins = self.nins__
         md.offset_slot = md.jitter_slot = md.ma_slot = md.acc_slot = -1
+        md.am_offset_slot = md.am_jitter_slot = -1
         planet = 0
         free_i = 0
         for b in self.blocks:
@@ -630,6 +648,11 @@ class ReddModel:
             elif b.type_ == 'Acceleration':
                 md.acc_slot = s0
                 md.acc_order = len(b)
+            elif b.type_ == 'AstrometryOffset':
+                md.am_on = 1
+                md.am_offset_slot = s0
+            elif b.type_ == 'AstrometryJitter':
+                md.am_jitter_slot = s0
             for i, p in enumerate(b):
                 slot = s0 + i
                 if p.fixed is None:

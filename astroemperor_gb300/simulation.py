@@ -25,8 +25,9 @@ import time
 import numpy as np
 
 from .data import RVData, load_target, preprocess_instruments
-from .model import (AccelerationBlock, CeleriteBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock,
-                    MOAVBlock, OffsetBlock, ReddModel, SinusoidBlock, SmartSetter, full_theta)
+from .model import (AccelerationBlock, AstrometryJitterBlock, AstrometryKeplerianBlock, AstrometryOffsetBlock,
+                    CeleriteBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock, MOAVBlock, OffsetBlock,
+                    ReddModel, SinusoidBlock, SmartSetter, full_theta)
 from .stats import model_stats
 
 
@@ -60,6 +61,14 @@ class Simulation:
         self.jitter_limits = [0, 1]
         self.jitter_prargs = [5, 5]
         self.instrument_names_RV = None
+        # joint astrometry (emp.py:2279-2281): switched on by an AM folder
+        # next to the RV one; Gaia's astrometric-gap tables (DR2, EDR3) as
+        # (start, end) arrays or file paths, which the reference ships in its
+        # support/deadtime folder
+        self.switch_AM = False
+        self.switch_inclination = False
+        self.gaia_deadtime = None
+        self.am_data = None
         self.starmass = 1.
         self.switch_dynamics = False
         self.dynamics_already_included = False
@@ -86,10 +95,22 @@ class Simulation:
 
     # ------------------------------------------------------------------ data
     def load_data(self, folder_name):
-        """emp.py:2263-2312 (RV mode)."""
+        """emp.py:2263-2312: the RV folder, and an AM folder when present
+        (qol_utils.py:103-455, astrometry.load_am)."""
+        import os
         self.starname = folder_name
         self.my_data = load_target(folder_name, read_loc=self.read_loc)
         self._after_data()
+        am_dir = f'{self.read_loc}datafiles/{folder_name}/AM/'
+        if os.path.isdir(am_dir):
+            from .astrometry import load_am, read_deadtime
+            if self.gaia_deadtime is None:
+                raise ValueError('astrometry needs the Gaia DR2 and EDR3 astrometric-gap tables: set '
+                                 'gaia_deadtime = (dr2, edr3) as (start, end) arrays or file paths')
+            dead = [read_deadtime(x) if isinstance(x, str) else x for x in self.gaia_deadtime]
+            self.am_data = load_am(am_dir, dead[0], dead[1], self.my_data.common_t)
+            self.switch_AM = True
+            self.switch_inclination = True
 
     def load_arrays(self, instruments, labels=None, name='custom'):
         """Same as load_data for in-memory per-instrument (BJD, RV, eRV) arrays."""
@@ -126,9 +147,16 @@ class Simulation:
 
     # ---------------------------------------------------------------- blocks
     def add_keplerian(self):
-        """emp.py:1212-1236; Keplerian blocks go in front of the data blocks."""
+        """emp.py:1212-1236; Keplerian blocks go in front of the data blocks
+        (astrometric Keplerians with inclination and node when astrometry is
+        on, parameterisation 0)."""
         self.kplanets__ += 1
-        kb = KeplerianBlock(self.keplerian_parameterisation, self.kplanets__)
+        if self.switch_inclination:
+            if self.keplerian_parameterisation != 0:
+                raise ValueError('astrometric Keplerians use parameterisation 0')
+            kb = AstrometryKeplerianBlock(self.kplanets__)
+        else:
+            kb = KeplerianBlock(self.keplerian_parameterisation, self.kplanets__)
         self.SmartSetter(kb, ecc_limits=self.eccentricity_limits, ecc_prargs=self.eccentricity_prargs,
                          starmass=self.starmass, dynamics=self.switch_dynamics, kplan=self.kplanets__,
                          dynamics_already_included=self.dynamics_already_included)
@@ -146,6 +174,18 @@ class Simulation:
 
     def add_moav(self):
         b = MOAVBlock(self.nins__, self.moav)
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def add_offset_am(self):
+        """emp.py:1307-1310."""
+        b = AstrometryOffsetBlock()
+        self.SmartSetter(b)
+        self.blocks__.append(b)
+
+    def add_jitter_am(self):
+        """emp.py:1300-1304."""
+        b = AstrometryJitterBlock()
         self.SmartSetter(b)
         self.blocks__.append(b)
 
@@ -213,7 +253,8 @@ class Simulation:
         return bool(self.moav_reference_quirk)
 
     def update_model(self):
-        self.model = ReddModel(self.blocks__, self.my_data, moav_reference_quirk=self.moav_quirk())
+        self.model = ReddModel(self.blocks__, self.my_data, moav_reference_quirk=self.moav_quirk(),
+                               am_data=self.am_data if self.switch_AM else None)
 
     # ------------------------------------------------------------ init walkers
     def set_init(self, rng=np.random):
@@ -452,9 +493,13 @@ class Simulation:
         self.k_start, self.k_end = k_start, k_end
         while self.k_start <= self.k_end:
             if self.switch_first_run:
+                # emp.py:2614-2625
                 self._autorun_add_RV_ins()
                 for _ in range(self.k_start):
                     self.add_keplerian()
+                if self.switch_AM:
+                    self.add_offset_am()
+                    self.add_jitter_am()
                 self.switch_first_run = False
             old = getattr(self, self._crit_current)
             self.run()

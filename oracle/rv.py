@@ -13,8 +13,9 @@ Every function below restates one piece of the reference and cites it
 * moving average ............. ``support/models/moav00.model`` (per instrument),
                                ``support/models/moav01.model`` (global)
 * acceleration ............... ``support/models/acc.model:2``
-* Gaussian likelihood ........ ``support/likelihoods/00.like:1-5``
-* priors ..................... ``support/priors/{Uniform,Normal,Jeffreys,Beta,Fixed}.prior``
+* Gaussian likelihood ........ ``support/likelihoods/00.like:1-5``; with
+                               astrometry ``a00.like`` (``oracle/am.py``)
+* priors ..................... ``support/priors/{Uniform,Normal,Jeffreys,Beta,Fixed,Isotropic}.prior``
                                with normalisers from ``emp_model.py:82-120``
 * prior writer (my_prior) .... ``src/astroemperor/emp.py:182-254``
 
@@ -142,6 +143,9 @@ def check_prargs(prior, limits, prargs):
         a, b = (low - mu) / s, (high - mu) / s
         logZ = np.log(_norm.cdf(b) - _norm.cdf(a))
         return [mu, s, logZ]
+    if prior == 'Isotropic':                                   # emp_model.py:96-99
+        low, high = limits
+        return np.log(0.5 * (np.cos(low) - np.cos(high)))
     return prargs
 
 
@@ -178,8 +182,16 @@ def prior_Fixed(x, limits, args):            # support/priors/Fixed.prior:1-2
     return 0.
 
 
+def prior_Isotropic(x, limits, args):        # support/priors/Isotropic.prior:1-5
+    logZ = args
+    if limits[0] <= x <= limits[1]:
+        return np.log(0.5 * np.sin(x)) - logZ
+    return -np.inf
+
+
 PRIORS = {'Uniform': prior_Uniform, 'Normal': prior_Normal,
-          'Jeffreys': prior_Jeffreys, 'Beta': prior_Beta, 'Fixed': prior_Fixed}
+          'Jeffreys': prior_Jeffreys, 'Beta': prior_Beta, 'Fixed': prior_Fixed,
+          'Isotropic': prior_Isotropic}
 
 
 def cps(pers, amps, eccs, starmass):
@@ -313,6 +325,7 @@ class OracleRV:
         self.quirk = bool(spec.get('moav_reference_quirk', False))
         # run the reference's no-op per-instrument MA loop literally (timing)
         self.faithful_quirk_loop = bool(spec.get('faithful_quirk_loop', False))
+        self.am = data.get('am') if any(b['type'] == 'AstrometryOffset' for b in self.blocks) else None
         self.X_ = np.asarray(data['X'], dtype=np.float64)
         self.Y_ = np.asarray(data['Y'], dtype=np.float64)
         self.YERR_ = np.asarray(data['YERR'], dtype=np.float64)
@@ -377,7 +390,8 @@ class OracleRV:
         for b, sl in zip(self.blocks, self.slices):
             t = b['type']
             if t == 'Keplerian':
-                per, A, phase, tp, ecc, w = kepler_elements(b['parameterisation'], theta[sl])
+                # an astrometric Keplerian's RV term is kep00's (akep00.model)
+                per, A, phase, tp, ecc, w = kepler_elements(b['parameterisation'], theta[sl][:5])
                 if tp is not None:                            # kep03/kep04: M = freq*(X_-tp)
                     freq = 2. * np.pi / per
                     M = freq * (X_ - tp)
@@ -398,7 +412,7 @@ class OracleRV:
                 M1 = freq1 * X_ + phase1
                 M2 = freq2 * X_ + phase2
                 model0 += A1 * np.cos(M1) + A2 * np.cos(M2)
-            elif t == 'Celerite2':                             # hyperparameters only
+            elif t in ('Celerite2', 'AstrometryOffset', 'AstrometryJitter'):   # no RV model
                 pass
             elif t == 'Acceleration':                          # acc.model:2
                 model0 += np.polyval(np.concatenate([theta[sl], [0]]), (X_ - X_[0]))
@@ -490,8 +504,15 @@ class OracleRV:
             co = gp.coefficients([(k, [th[i] for i in sl]) for k, sl in gp_terms[0]])
             return gp.semisep_loglike(self.X_, self.Y_ - model, err2, co)
         model, err2 = self.my_model(theta)
-        return -0.5 * (np.sum((self.Y_ - model) ** 2 / err2 + np.log(err2))) \
-            + self.likelihood_constant
+        ll = -0.5 * (np.sum((self.Y_ - model) ** 2 / err2 + np.log(err2))) + self.likelihood_constant
+        if self.am is not None:                          # support/likelihoods/a00.like
+            from . import am as _am
+            th = self.full_theta(theta)
+            planets = [th[sl] for b, sl in zip(self.blocks, self.slices) if b['type'] == 'Keplerian']
+            off = [th[sl] for b, sl in zip(self.blocks, self.slices) if b['type'] == 'AstrometryOffset'][0]
+            jit = [th[sl] for b, sl in zip(self.blocks, self.slices) if b['type'] == 'AstrometryJitter'][0]
+            ll += _am.loglike_am(self.am, planets, off, jit)
+        return ll
 
     def my_prior(self, theta):
         """Restates the generated ``my_prior`` (emp.py:182-254)."""

@@ -199,3 +199,66 @@ def kat_case_models(arr):
     m, d, setup, truth = synth.build_model('c5', seed=5)
     add('c5_ma2', m, d, center=truth, spread=1e-4)
     return cases
+
+
+# ---------------------------------------------------------------------------
+# joint RV + astrometry: HIP 21850 (the reference's tests/03_hip21850_test.ipynb)
+# ---------------------------------------------------------------------------
+# the maximum-posterior fit that notebook recorded (P, K, phase, e, w, I,
+# Omega; acceleration; 4 offsets; 4 jitters; 5 astrometric offsets; jitters
+# of Hipparcos and Gaia)
+HIP_MAP = [2567.37, 120.188, 5.553, 0.201, 0.659, 1.084, 4.289, 0.006,
+           -24.341, -4.909, -105.186, -97.556, 29.644, 0.825, 8.933, 1.743,
+           -0.437, -0.257, 0.003, -0.183, 0.154, 0.257, 1.086]
+
+
+def hip21850_data(fix):
+    """(RVData, AMData) from the HIP 21850 fixture (tests/golden/hip21850.npz)."""
+    from astroemperor_gb300.astrometry import build_am
+    names = [str(n) for n in fix['rv_names']]
+    inst = [fix[f'rv_{k}'] for k in range(len(names))]
+    data = preprocess_instruments(inst, names)
+    hg = {k[3:]: fix[k] for k in fix.files if k.startswith('hg_')}
+    hipp = {k[5:]: fix[k] for k in fix.files if k.startswith('hipp_')}
+    gost = {'ObservationTimeAtBarycentre[BarycentricJulianDateInTCB]': fix['gost_bjd'],
+            'scanAngle[rad]': fix['gost_psi'], 'parallaxFactorAlongScan': fix['gost_parf']}
+    am = build_am(hg, hipp, gost, fix['dead_dr2'], fix['dead_dr3'], data.common_t)
+    return data, am
+
+
+def model_hip21850(fix):
+    """The notebook's model: one astrometric Keplerian, acceleration, offsets
+    and jitters of four instruments, astrometric offsets and jitters, with
+    its conditions and prior arguments."""
+    from astroemperor_gb300.model import (AstrometryJitterBlock, AstrometryKeplerianBlock,
+                                          AstrometryOffsetBlock)
+    data, am = hip21850_data(fix)
+    ss = SmartSetter(data)
+    kb = AstrometryKeplerianBlock(1)
+    ss(kb, ecc_prargs=(0, 0.3))
+    for j, lim in enumerate(([2000, 3000], [50, 150], [np.pi, 2 * np.pi], [0, 0.5], [0, np.pi])):
+        kb[j].limits = list(lim)
+    ab = AccelerationBlock(1)
+    ss(ab)
+    ob = OffsetBlock(4)
+    ss(ob)
+    jb = JitterBlock(4)
+    ss(jb, jit_prargs=(0, 10))
+    for k in range(4):
+        ob[k].limits = [-150, 150]
+        jb[k].limits = [1e-4, 30]
+    aob = AstrometryOffsetBlock()
+    ss(aob)
+    for p in aob:
+        p.limits = [-1, 1]
+    ajb = AstrometryJitterBlock()
+    ss(ajb)
+    ajb[0].limits, ajb[0].prior, ajb[0].prargs = [0, 10], 'Normal', [0, 5]
+    ajb[1].limits, ajb[1].prior, ajb[1].prargs = [0, 10], 'Normal', [1, 0.1]
+    model = ReddModel([kb, ab, ob, jb, aob, ajb], data, am_data=am)
+    return model, data, am
+
+
+def am_case_thetas(model, n_in=24, n_near=8):
+    rng = np.random.default_rng(20251204)
+    return draw_thetas(model, rng, n_in=n_in, center=np.array(HIP_MAP), n_near=n_near, spread=0.01)

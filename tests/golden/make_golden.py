@@ -30,6 +30,12 @@ Writes
                        own per-instrument template does not compute) is pinned
                        to its live global template moav01.model run on each
                        instrument's time-ordered subsequence
+  hip21850.npz      -- the reference's HIP 21850 RV and astrometric data and the
+                       Gaia dead-time tables of its support folder, as arrays
+  am_kat.npz        -- loglike_AM of the HIP 21850 model at seeded theta by the
+                       reference's own generated astrometry functions
+                       (ReddModel._write_model_AM text with constants.scr), and
+                       the oracle's (logL, logprior) of the a00.like model
   smartsetter_kat.json -- default limits / priors / prargs of every block type
                        as the reference's SmartSetter methods (block_repo.py,
                        run from its source on a small column shim) set them
@@ -71,6 +77,8 @@ def main(ref_root):
     gp_fixture(arr)
     template_fixture(ref_root, arr)
     smartsetter_fixture(ref_root, arr)
+    hip21850_fixture(ref_root)
+    am_fixture(ref_root)
 
 
 class _Col:
@@ -389,6 +397,105 @@ def hill_fixture(ref_root):
     np.savez_compressed(os.path.join(HERE, 'hill_kat.npz'), x=np.array(X), args=np.array(A),
                         value=np.array(out))
     print('hill_kat:', int(np.sum(np.isfinite(out))), 'stable of', len(out))
+
+
+def hip21850_fixture(ref_root):
+    """The reference's HIP 21850 data (tests/datafiles/HIP21850: four RV files,
+    the Hipparcos/Gaia catalogue rows, the Hipparcos abscissae and the Gaia
+    scan epochs) and its Gaia dead-time tables (support/deadtime), as
+    arrays: tests/golden/hip21850.npz."""
+    from astroemperor_gb300.astrometry import _read_csv, _read_whitespace_table, read_deadtime
+    base = os.path.join(ref_root, 'tests', 'datafiles', 'HIP21850')
+    out = {}
+    names = sorted(fn for fn in os.listdir(os.path.join(base, 'RV')) if fn != '.DS_Store')
+    out['rv_names'] = np.array(names)
+    for k, fn in enumerate(names):
+        out[f'rv_{k}'] = np.loadtxt(os.path.join(base, 'RV', fn), ndmin=2)[:, :3]
+    am = os.path.join(base, 'AM')
+    hg = _read_whitespace_table(os.path.join(am, 'HIP21850_hipgaia.hg123'))
+    for k, v in hg.items():
+        if v.dtype.kind == 'f':
+            out[f'hg_{k}'] = v
+    hipp = _read_whitespace_table(os.path.join(am, 'HIP21850_hip2.abs'))
+    for k in ('BJD', 'EPOCH', 'PARF', 'CPSI', 'SPSI', 'RES', 'SRES'):
+        out[f'hipp_{k}'] = hipp[k]
+    g = _read_csv(os.path.join(am, 'HIP21850_gost.csv'))
+    out['gost_bjd'] = g['ObservationTimeAtBarycentre[BarycentricJulianDateInTCB]']
+    out['gost_psi'] = g['scanAngle[rad]']
+    out['gost_parf'] = g['parallaxFactorAlongScan']
+    dead = os.path.join(ref_root, 'src', 'astroemperor', 'support', 'deadtime')
+    out['dead_dr2'] = read_deadtime(os.path.join(dead, 'astrometric_gaps_gaiadr2_08252020.csv'))
+    out['dead_dr3'] = read_deadtime(os.path.join(dead, 'astrometric_gaps_gaiaedr3_12232020.csv'))
+    np.savez_compressed(os.path.join(HERE, 'hip21850.npz'), **out)
+    print('hip21850:', {k: np.shape(v) for k, v in out.items() if not k.startswith('hg_')})
+
+
+def _reference_am_text(src_dir, model):
+    """The text ReddModel._write_model_AM (emp_model.py:1232-1675) writes for
+    this model's blocks, produced by the reference's own method."""
+    import ast
+    import io
+    import textwrap
+    import types
+    text = open(os.path.join(src_dir, 'emp_model.py')).read()
+    tree = ast.parse(text)
+    fn = next(n for n in ast.walk(tree) if isinstance(n, ast.FunctionDef) and n.name == '_write_model_AM')
+    ns = {'np': np}
+    exec(textwrap.dedent(ast.get_source_segment(text, fn)), ns)
+
+    class Fake:
+        data_AM = {'AM_cata': True}
+
+        def __iter__(self):
+            return iter(types.SimpleNamespace(type_=b.type_, slice=b.slice) for b in model.blocks)
+    buf = io.StringIO()
+    ns['_write_model_AM'](Fake(), buf)
+    return buf.getvalue()
+
+
+def am_fixture(ref_root):
+    """loglike_AM of the HIP 21850 model at seeded theta, evaluated by the
+    reference's own generated functions (the text of _write_model_AM with
+    support/astrometry/constants.scr) on the data arrays of this package's
+    loader; kepler.solve (absent) is the oracle's solver.  Written with the
+    oracle's (logL, logprior) of the whole a00.like model:
+    tests/golden/am_kat.npz."""
+    import types
+    from oracle.rv import kepler_solve
+    from tests.golden.cases import am_case_thetas, model_hip21850
+    fix = np.load(os.path.join(HERE, 'hip21850.npz'))
+    model, data, am = model_hip21850(fix)
+    src_dir = os.path.join(ref_root, 'src', 'astroemperor')
+    g = {'np': np, 'kepler': types.SimpleNamespace(solve=kepler_solve)}
+    exec(open(os.path.join(src_dir, 'support', 'astrometry', 'constants.scr')).read(), g)
+    cat = am.catalogs
+    nh, ng = am.n_hipp, am.n_gost
+    g.update({
+        'AM_catalogs_': cat, 'AM_iref_': -1, 'AM_ref_epoch_': cat[-1, 0],
+        'AM_catalogs_times_refed': cat[:, 0] - cat[-1, 0], 'AM_catalogs_obs_ref': cat[-1, 1:],
+        'AM_PLX_ref': cat[-1, 3],
+        'time_iad_all': np.concatenate([am.hipp['BJD'], am.gost['BJD']]),
+        'time_iad_gost_refed': am.gost['BJD'] - cat[-1, 0], 'common_t': am.common_t,
+        'N_HIPP': nh, 'N_GOST': ng, 'N_IAD': nh + ng,
+        'CPSI_HIPP_': am.hipp['CPSI'], 'SPSI_HIPP_': am.hipp['SPSI'], 'EPOCH_HIPP_': am.hipp['EPOCH'],
+        'PARF_HIPP_': am.hipp['PARF'], 'RES_HIPP_': am.hipp['RES'], 'SRES_HIPP_': am.hipp['SRES'],
+        'CPSI_GOST_': am.gost['CPSI'], 'SPSI_GOST_': am.gost['SPSI'], 'PARF_GOST_': am.gost['parf'],
+        'GAIA_CATS': dict(GDR2=dict(mask=am.masks['GDR2'], row=0, cov_idx=1),
+                          GDR3=dict(mask=am.masks['GDR3'], row=1, cov_idx=2)),
+        'AM_GSV': am.gsv, 'AM_astro_gost': types.SimpleNamespace(values=am.astro_gost),
+        'AM_inv_COV': am.inv_cov, 'AM_log_det_COV': am.log_det_cov,
+    })
+    exec(_reference_am_text(src_dir, model), g)
+    th = am_case_thetas(model)
+    from oracle.rv import OracleRV
+    o = OracleRV(model.spec(), dict(data.as_dict(), am=am.as_dict()))
+    full = [o.full_theta(t) for t in th]
+    ref_am = np.array([float(g['loglike_AM'](f)) for f in full])
+    lp = np.array([o.my_prior(t) for t in th])
+    ll = np.array([o.my_likelihood(t) if np.isfinite(p) else -np.inf for t, p in zip(th, lp)])
+    np.savez_compressed(os.path.join(HERE, 'am_kat.npz'), theta=th, loglike_am_ref=ref_am, logl=ll,
+                        logprior=lp)
+    print('am_kat:', len(th), 'points;', int(np.isfinite(lp).sum()), 'inside the prior')
 
 
 if __name__ == '__main__':

@@ -1,0 +1,61 @@
+"""The astrometric oracle against the reference's own code: loglike_AM of the
+HIP 21850 model (tests/golden/am_kat.npz, written by tests/golden/make_golden.py
+by executing the text ReddModel._write_model_AM writes, with
+support/astrometry/constants.scr, on the data arrays of this package's
+loader).  The reference converts mas to degrees in long double; the oracle
+stays in FP64 (relative 1e-11).  And the notebook's recorded fit decomposes
+as the notebook printed it."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import am as oam
+from oracle.rv import OracleRV
+from tests.golden.cases import HIP_MAP, model_hip21850
+
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+@pytest.fixture(scope='module')
+def hip():
+    fix = np.load(os.path.join(GOLDEN, 'hip21850.npz'))
+    model, data, am = model_hip21850(fix)
+    return model, data, am, OracleRV(model.spec(), dict(data.as_dict(), am=am.as_dict()))
+
+
+def test_loglike_am_equals_the_reference_functions(hip):
+    model, data, am, o = hip
+    k = np.load(os.path.join(GOLDEN, 'am_kat.npz'))
+    got = []
+    for t in k['theta']:
+        f = o.full_theta(t)
+        planets = [f[b.slice] for b in model.blocks if b.type_ == 'Keplerian']
+        off = [f[b.slice] for b in model.blocks if b.type_ == 'AstrometryOffset'][0]
+        jit = [f[b.slice] for b in model.blocks if b.type_ == 'AstrometryJitter'][0]
+        got.append(oam.loglike_am(am.as_dict(), planets, off, jit))
+    ref = k['loglike_am_ref']
+    fin = np.isfinite(ref)
+    assert fin.sum() >= 30
+    np.testing.assert_allclose(np.array(got)[fin], ref[fin], rtol=1e-11)
+
+
+def test_recorded_fit_decomposes_as_recorded(hip):
+    """tests/03_hip21850_test.ipynb: maximum posterior -700.428, likelihood
+    at it -642.157, so the prior there is -58.271; at the printed (rounded)
+    fit the oracle's prior agrees to the rounding and the likelihood lies
+    within the rounding of the maximum."""
+    model, data, am, o = hip
+    x = np.array(HIP_MAP)
+    assert o.my_prior(x) == pytest.approx(-58.271, abs=0.02)
+    assert o.my_likelihood(x) == pytest.approx(-642.157, abs=0.5)
+    assert data.ndata == 97 and model.ndim__ == 23
+    assert data.common_t == pytest.approx(2451118.09737, abs=1e-5)
+
+
+def test_astrometry_data_shapes(hip):
+    model, data, am, o = hip
+    assert am.n_hipp == 108 and am.n_gost == 40
+    assert int(am.masks['GDR2'].sum()) == 17 and int(am.masks['GDR3'].sum()) == 32
+    assert am.gsv['GDR2'].shape == (5, 17) and am.gsv['GDR3'].shape == (5, 32)
+    np.testing.assert_allclose(am.astro_gost[1, :2], 0.0)

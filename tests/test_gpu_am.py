@@ -1,0 +1,98 @@
+"""Joint RV + astrometry likelihood (support/likelihoods/a00.like) on the
+GPU against the oracle, which tests/test_am_oracle.py pins to the
+reference's own generated astrometry functions: the HIP 21850 model of the
+reference's tests/03_hip21850_test.ipynb.
+
+Tolerances: FP64 logL relative 1e-11 (the astrometric term is FP64 in both
+precisions; the RV term as in test_gpu_logpost), mixed 1e-6, logprior 1e-13
+(the Isotropic inclination prior included); the PT sampler with the
+astrometric term walks the oracle sampler's chain (same Philox stream).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from astroemperor_gb300 import _native as N
+from astroemperor_gb300.engine import Context, PTSampler
+from oracle.pt import OraclePT
+from oracle.rv import OracleRV
+from tests.golden.cases import HIP_MAP, model_hip21850
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+@pytest.fixture(scope='module')
+def hip(lib, cuda):
+    fix = np.load(os.path.join(GOLDEN, 'hip21850.npz'))
+    model, data, am = model_hip21850(fix)
+    return model, data, am, Context(model, 'cuda:0')
+
+
+@pytest.mark.parametrize('prec,tol', [(N.EMP_PREC_FP64, 1e-11), (N.EMP_PREC_MIXED, 1e-6)])
+def test_logpost_matches_the_oracle(hip, prec, tol):
+    model, data, am, ctx = hip
+    k = np.load(os.path.join(GOLDEN, 'am_kat.npz'))
+    th = k['theta']
+    ll, lp = ctx.logpost(torch.as_tensor(th, device='cuda:0'), precision=prec)
+    torch.cuda.synchronize()
+    ll, lp = ll.cpu().numpy(), lp.cpu().numpy()
+    np.testing.assert_allclose(lp, k['logprior'], rtol=1e-13, atol=1e-13)
+    fin = np.isfinite(k['logprior'])
+    assert np.all(ll[~fin] == -np.inf)
+    rel = np.abs(ll[fin] - k['logl'][fin]) / np.abs(k['logl'][fin])
+    print('astrometry + RV logL: max relative error', rel.max())
+    assert rel.max() <= tol
+
+
+def test_pt_replay_matches_the_oracle_sampler(hip):
+    model, data, am, ctx = hip
+    T, W, S = 3, 16, 8
+    betas = [1.0, 0.3, 0.05]
+    rng = np.random.default_rng(7)
+    lim = model.limits_free()
+    p0 = np.clip(np.array(HIP_MAP) + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, len(HIP_MAP))),
+                 lim[:, 0], lim[:, 1])
+    s = PTSampler(W, model.ndim__, model, ntemps=T, betas=betas, precision='fp64', seed=2024,
+                  adapt_tau=20, use_graph=False, context=ctx, autotune=False)
+    s.run_mcmc(p0, nsweeps=S)
+    o = OracleRV(model.spec(), dict(data.as_dict(), am=am.as_dict()))
+
+    def f(th):
+        th = np.atleast_2d(th)
+        lp = np.array([o.my_prior(t) for t in th])
+        ll = np.array([o.my_likelihood(t) if np.isfinite(x) else -np.inf for t, x in zip(th, lp)])
+        return ll, lp
+    ora = OraclePT(f, T, W, model.ndim__, betas, adapt=True, adapt_tau=20, rng='philox', seed=2024)
+    ora.set_positions(p0)
+    ora.run(S)
+    np.testing.assert_allclose(s.get_chain(), np.moveaxis(np.array(ora.chain), 1, 0), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(s.get_log_like(), np.moveaxis(np.array(ora.log_like), 1, 0), rtol=1e-11)
+    assert ora.accepted.sum() > 0
+
+
+def test_graph_equals_eager(hip):
+    model, data, am, ctx = hip
+    T, W = 2, 16
+    rng = np.random.default_rng(9)
+    lim = model.limits_free()
+    p0 = np.clip(np.array(HIP_MAP) + 1e-3 * (lim[:, 1] - lim[:, 0]) * rng.normal(size=(T, W, len(HIP_MAP))),
+                 lim[:, 0], lim[:, 1])
+    out = []
+    for ug in (False, True):
+        s = PTSampler(W, model.ndim__, model, ntemps=T, betas=[1.0, 0.2], precision='mixed', seed=5,
+                      use_graph=ug, context=ctx, autotune=False)
+        s.run_mcmc(p0, nsweeps=20)
+        out.append((s.get_chain(), s.get_log_like()))
+    for a, b in zip(out[0], out[1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_gradient_refuses_astrometry(hip):
+    model, data, am, ctx = hip
+    th = torch.as_tensor(np.array([HIP_MAP]), device='cuda:0')
+    with pytest.raises(N.EmpError) as e:
+        ctx.logpost_grad(th)
+    assert e.value.code == N.EMP_E_UNSUPPORTED

@@ -79,3 +79,97 @@ def test_autorun_51peg_reproduces_the_reference_notebook(peg_arr, lib, cuda, tmp
     assert abs(lam - lam_ref) <= 0.05, lam
     # the sampler's cold chain is the posterior the reference reported
     assert np.isfinite(sim.evidence[0])
+
+
+def _write_hip21850(root, fix):
+    """The reference's HIP 21850 data files, written back from the fixture."""
+    rv = root / 'datafiles' / 'HIP21850' / 'RV'
+    am = root / 'datafiles' / 'HIP21850' / 'AM'
+    rv.mkdir(parents=True)
+    am.mkdir(parents=True)
+    for k, name in enumerate(fix['rv_names']):
+        np.savetxt(rv / str(name), fix[f'rv_{k}'])
+    hg = [k for k in fix.files if k.startswith('hg_')]
+    with open(am / 'HIP21850_hipgaia.hg123', 'w') as f:
+        f.write(' '.join(k[3:] for k in hg) + '\n')
+        for r in range(len(fix[hg[0]])):
+            f.write(' '.join(repr(float(fix[k][r])) for k in hg) + '\n')
+    cols = ('BJD', 'EPOCH', 'PARF', 'CPSI', 'SPSI', 'RES', 'SRES')
+    with open(am / 'HIP21850_hip2.abs', 'w') as f:
+        f.write(' '.join(cols) + '\n')
+        for r in range(len(fix['hipp_BJD'])):
+            f.write(' '.join(repr(float(fix[f'hipp_{c}'][r])) for c in cols) + '\n')
+    with open(am / 'HIP21850_gost.csv', 'w') as f:
+        f.write('ObservationTimeAtBarycentre[BarycentricJulianDateInTCB],scanAngle[rad],parallaxFactorAlongScan\n')
+        for r in range(len(fix['gost_bjd'])):
+            f.write(','.join(repr(float(fix[k][r])) for k in ('gost_bjd', 'gost_psi', 'gost_parf')) + '\n')
+
+
+def test_autorun_hip21850_reproduces_the_reference_notebook(lib, cuda, tmp_path):
+    """tests/03_hip21850_test.ipynb through Simulation: RV of four
+    instruments with acceleration plus Hipparcos and Gaia astrometry
+    (support/likelihoods/a00.like), autorun(1, 1) with the notebook's setup
+    and conditions (its 'Jitter Hipparcos' is 'Jitter Hipp' in the
+    reference's current parameter names).  Recorded: BIC 1389.532, maximum
+    posterior -700.428, the fit of HIP_MAP; BIC held to +-2 (the likelihood
+    at the maximum-posterior sample to +-1: the Gaia jitter's Normal(1, 0.1)
+    prior moves that sample), the well-constrained fit parameters to three
+    times the notebook's printed ranges."""
+    import os
+    from tests.golden.cases import HIP_MAP
+    fix = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'hip21850.npz'))
+    _write_hip21850(tmp_path, fix)
+    np.random.seed(1234)
+    sim = Simulation()
+    sim.read_loc = str(tmp_path) + '/'
+    sim.gaia_deadtime = (fix['dead_dr2'], fix['dead_dr3'])
+    ntemps = 11
+    sim.set_engine('reddemcee')
+    sim.engine_config['setup'] = [ntemps, 256, 3000, 1]
+    sim.engine_config['adapt_tau'] = 100
+    sim.engine_config['adapt_nu'] = 1.5
+    sim.engine_config['adapt_mode'] = 0
+    sim.engine_config['betas'] = list(np.geomspace(1, 0.001, ntemps))
+    sim.engine_config['seed'] = 1234
+    sim.run_config['burnin'] = 0.5
+    sim.starmass = 0.98
+    sim.instrument_names_RV = ['AAT', 'HAR1', 'HAR2', 'HAR3']
+    sim.jitter_prargs = [0, 10]
+    sim.eccentricity_prargs = [0, 0.3]
+    sim.acceleration = 1
+    for i in range(1, 5):
+        sim.add_condition([f'Offset {i}', 'limits', [-150, 150]])
+        sim.add_condition([f'Jitter {i}', 'limits', [1e-4, 30]])
+    sim.add_condition(['Period 1', 'limits', [2000, 3000]])
+    sim.add_condition(['Amplitude 1', 'limits', [50, 150]])
+    sim.add_condition(['Eccentricity 1', 'limits', [0, 0.5]])
+    sim.add_condition(['Phase 1', 'limits', [np.pi, 2 * np.pi]])
+    sim.add_condition(['Longitude 1', 'limits', [0, np.pi]])
+    for off in ['RA', 'DE', 'PLX', 'pm RA', 'pm DE']:
+        sim.add_condition([f'Offset {off}', 'limits', [-1, 1]])
+    sim.add_condition(['Jitter Gaia', 'limits', [0, 10]])
+    sim.add_condition(['Jitter Gaia', 'prior', 'Normal'])
+    sim.add_condition(['Jitter Gaia', 'prargs', [1, 0.1]])
+    sim.add_condition(['Jitter Hipp', 'limits', [0, 10]])
+    sim.add_condition(['Jitter Hipp', 'prior', 'Normal'])
+    sim.add_condition(['Jitter Hipp', 'prargs', [0, 5]])
+    sim.load_data('HIP21850')
+    assert sim.switch_AM
+    sim.autorun(1, 1)
+
+    h = sim.history
+    assert len(h) == 1 and h[0]['k'] == 1
+    print('HIP 21850: BIC %.3f like_max %.3f post_max %.3f' % (h[0]['BIC'], h[0]['like_max'], h[0]['post_max']))
+    names = [p.name for p in sim.model.free_parameters()]
+    assert len(names) == 23
+    fit = dict(zip(names, sim.fit_max))
+    print('fit:', {k: round(float(v), 4) for k, v in fit.items()})
+    assert h[0]['BIC'] == pytest.approx(1389.532, abs=2.0)
+    assert h[0]['post_max'] == pytest.approx(-700.428, abs=1.5)
+    # (recorded value, printed -, + range)
+    recorded = {'Period 1': (2567.37, 4.407, 4.794), 'Amplitude 1': (120.188, 0.835, 0.318),
+                'Eccentricity 1': (0.201, 0.008, 0.009), 'Longitude 1': (0.659, 0.021, 0.015),
+                'Inclination 1': (1.084, 0.035, 0.032), 'Offset 2': (-4.909, 1.93, 2.672)}
+    for name, (v, lo, hi) in recorded.items():
+        assert abs(fit[name] - v) <= 3 * max(lo, hi), (name, fit[name], v)
+    assert np.isfinite(sim.evidence[0])
