@@ -4,9 +4,11 @@
 // log-likelihood; its functions are written by ReddModel._write_model_AM
 // (emp_model.py:1232-1675) with the helpers of support/astrometry/
 // constants.scr.  Per walker row:
-//   * the barycentre at each catalogue epoch (model_barycenter /
+//   * the barycentre at the Hipparcos epoch (model_barycenter /
 //     obs_lin_prop_PA): the DR3 solution minus the five offsets, propagated
-//     linearly in Cartesian coordinates; one lane per catalogue;
+//     linearly in Cartesian coordinates; at the DR3 epoch the propagation
+//     time is zero and the barycentre is that solution itself, used as
+//     offsets from the DR3 position;
 //   * every Keplerian's sky-plane offsets at every Hipparcos and Gaia scan
 //     epoch (calc_astro_new: Kepler solve, Thiele-Innes constants), lanes
 //     over epochs;
@@ -17,11 +19,11 @@
 //     matrix), compared with the catalogue solution under its covariance
 //     scaled by the jitter squared (compute_abs_signal_gost,
 //     gaussian_loglike_mvn).
-// Everything is FP64 in both precisions.  The reference converts mas to
-// degrees in long double; here the declination of a scan is formed as the
-// difference from the catalogue declination first, which keeps FP64 exact to
-// ~1e-16 deg where the reference's FP64 degrees would lose digits to the
-// ~60-degree magnitude.  k_logpost has written the RV part (logL of the row,
+// Everything is FP64 in both precisions.  The reference handles absolute
+// positions in degrees (one FP64 ulp of 60 degrees is 2.5e-8 mas, and the
+// Gaia term is sensitive at that level); here the scan positions are formed
+// as offsets from the DR3 position, which keeps them to ~1e-16 of the
+// offsets themselves.  k_logpost has written the RV part (logL of the row,
 // or for a stretch half-step the proposal, its prior and RV logL); this
 // kernel adds the astrometric term and finishes the mode (gp_finish).
 #pragma once
@@ -39,7 +41,7 @@ constexpr int kAmPC = 12;                      // doubles per planet
 struct AmSmem {                                // per warp
     double full[EMP_MAX_PARAMS];
     double pc[EMP_MAX_PLANETS][kAmPC];
-    double bary[3][6];
+    double bary[1][6];                         // the Hipparcos epoch
 };
 
 // one catalogue epoch of the barycentre: ra, dec (deg), parallax, pmra,
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(kAmThreads) k_am(KArgs A) {
     __syncwarp();
     const double* off = S.full + md->am_offset_slot;
     const double plx0 = d.catalogs[2 * 7 + 3] - off[2];
-    if (lane < 3) am_barycentre(d, off, lane, S.bary[lane]);
+    if (lane == 0) am_barycentre(d, off, 0, S.bary[0]);
     if (lane >= 8 && lane - 8 < md->n_planets) am_planet(S.full + md->kep_slot[lane - 8], plx0, S.pc[lane - 8]);
     __syncwarp();
     // Hipparcos: the barycentre at the Hipparcos epoch against its solution
@@ -135,8 +137,17 @@ __global__ void __launch_bounds__(kAmThreads) k_am(KArgs A) {
     const double dra_h = (b0[0] - hc[0]) * cos(mean_dec * (kPi / 180.0)) * kMasPerDeg;
     const double dde_h = (b0[1] - hc[1]) * kMasPerDeg;
     const double dplx_h = b0[2] - hc[2], dpmra_h = b0[3] - hc[3], dpmde_h = b0[4] - hc[4];
-    const double* b3 = S.bary[2];
-    const double ref_ra3 = d.catalogs[2 * 7 + 1], ref_dec3 = d.catalogs[2 * 7 + 2], t3 = d.catalogs[2 * 7];
+    // the barycentre at the DR3 epoch: model_barycenter propagates the DR3
+    // solution minus the offsets over zero time, which returns it unchanged
+    // (position, parallax, proper motion); taken as offsets from the DR3
+    // position in degrees, without the round trip through Cartesian
+    // coordinates that rounds ~60-degree angles
+    const double* r3 = d.catalogs + 2 * 7;                // epoch, ra, dec, plx, pmra, pmdec
+    const double ref_dec3 = r3[2], t3 = r3[0];
+    const double dde3 = -off[1] / kMasPerDeg;
+    const double dra3 = -off[0] / kMasPerDeg / cos(ref_dec3 * (kPi / 180.0));
+    const double plx3 = r3[3] - off[2], pmra3 = r3[4] - off[3], pmde3 = r3[5] - off[4];
+    const double dec3r = (ref_dec3 + dde3) * (kPi / 180.0);
     const double jh = S.full[md->am_jitter_slot], jg = S.full[md->am_jitter_slot + 1];
     const int nh = d.n_hipp, ng = d.n_gost;
     double sh = 0.0, pr[2][5];
@@ -172,13 +183,13 @@ __global__ void __launch_bounds__(kAmThreads) k_am(KArgs A) {
             } else {
                 const int j = i - nh;
                 const double tg = (t - t3) / kDayPerYear / 206265e3;
-                const double decs = b3[1] * (kPi / 180.0) + b3[4] * tg;
-                const double dras = b3[3] * tg / cos(decs);                 // ras - ra(b3), rad
-                const double ddeg = (b3[1] - ref_dec3) + b3[4] * tg * (180.0 / kPi) + c1 / kMasPerDeg;
+                const double decs = dec3r + pmde3 * tg;
+                const double dras = pmra3 * tg / cos(decs);                 // ras - RA3, rad
+                const double ddeg = dde3 + pmde3 * tg * (180.0 / kPi) + c1 / kMasPerDeg;
                 const double dec = ref_dec3 + ddeg;
-                const double dra = ((b3[0] - ref_ra3) + dras * (180.0 / kPi)) * cos(dec * (kPi / 180.0)) * kMasPerDeg + c0;
+                const double dra = (dra3 + dras * (180.0 / kPi)) * cos(dec * (kPi / 180.0)) * kMasPerDeg + c0;
                 const double ddec = ddeg * kMasPerDeg;
-                const double dplx = b3[2] + c2;
+                const double dplx = plx3 + c2;
                 const double ab = d.gost[ng + j] * ddec + d.gost[2 * ng + j] * dra + d.gost[3 * ng + j] * dplx;
 #pragma unroll
                 for (int c = 0; c < 2; ++c)

@@ -277,7 +277,7 @@ int validate_model(const emp_model_desc* m) {
         if (v < 0 || v >= m->n_free + 2 * m->n_planets)
             return fail(EMP_E_INVALID, "prior_var[%d]=%d out of range", i, v);
         const emp_prior& p = v < m->n_free ? m->prior[v] : m->derived[(v - m->n_free) >> 1][(v - m->n_free) & 1];
-        if (p.kind != EMP_PRIOR_NORMAL && p.kind != EMP_PRIOR_BETA)
+        if (p.kind != EMP_PRIOR_NORMAL && p.kind != EMP_PRIOR_BETA && p.kind != EMP_PRIOR_ISOTROPIC)
             return fail(EMP_E_INVALID, "prior_var[%d] names a constant prior", i);
     }
     for (int i = 0; i < m->n_free; ++i) {

@@ -21,11 +21,18 @@ of ``support/astrometry/constants.scr``) and of ``support/likelihoods/a00.like``
   covariance scaled by the jitter squared.
 
 The reference converts mas to degrees in ``np.longdouble`` (``mas2deg``:
-80-bit on x86); here every step is FP64, and the declination differences
-that the reference forms from degrees are formed as differences first
-(the same value, without cancelling two ~60-degree numbers).  The fixture
-``tests/golden/am_kat.npz`` holds the reference's own functions executed on
-the same data; the restatement agrees to the level the test states.
+80-bit on x86) and does everything else in FP64; ``dtype=np.float64`` (the
+default) follows it, and the fixture ``tests/golden/am_kat.npz`` holds the
+reference's own functions executed on the same data, which the restatement
+equals to ~1e-12.  The formulas handle absolute positions in degrees (~60
+degrees for HIP 21850), so their FP64 rounding is 7e-15 degrees = 2.5e-8
+mas per ulp, and one ulp of the Gaia DR3-epoch position moves the Gaia term
+of HIP 21850 by up to 2.8e-9 of the total log-likelihood.
+``dtype=np.longdouble`` evaluates the barycentre and the Gaia scan-epoch
+propagation (the parts that handle absolute positions) in extended
+precision: the value of the reference's formulas without that rounding
+noise, against which both FP64 evaluations (the reference's and the
+device's) are measured.
 """
 from __future__ import annotations
 
@@ -82,14 +89,14 @@ def _xyz2bl(x, y, z):
     return b, l
 
 
-def barycenter(am, off5):
+def barycenter(am, off5, dtype=np.float64):
     """[3 catalogues, 6]: ra, dec (deg), parallax, pmra, pmdec (mas, mas/yr),
     rv of the barycentre at each catalogue epoch (model_barycenter)."""
-    cat = am['catalogs']
+    cat = np.asarray(am['catalogs'], dtype=dtype)
     ref = cat[-1, 1:]                                    # DR3 solution (AM_iref_ = -1)
     t_refed = cat[:, 0] - cat[-1, 0]
-    th = np.array(off5, dtype=np.float64)
-    th0 = np.empty(6)
+    th = np.array(off5, dtype=dtype)
+    th0 = np.empty(6, dtype=dtype)
     th0[0] = th[0] / MAS_PER_DEG / np.cos(np.deg2rad(ref[1]))
     th0[1] = th[1] / MAS_PER_DEG
     th0[2:5] = th[2:5]
@@ -121,18 +128,20 @@ def barycenter(am, off5):
     return np.column_stack([np.rad2deg(ra1), np.rad2deg(de1), 1 / d1, v1 / d1, v2 / d1, v0 * AUYR2KMS])
 
 
-def loglike_am(am, theta_planets, off5, jit2):
+def loglike_am(am, theta_planets, off5, jit2, dtype=np.float64):
     """loglike_AM(theta): planets [(P, K, phase, e, w, I, Omega)], the five
-    offsets (RA, DE, PLX, pm RA, pm DE) and the jitters (Hipparcos, Gaia)."""
+    offsets (RA, DE, PLX, pm RA, pm DE) and the jitters (Hipparcos, Gaia).
+    ``dtype`` is the type of the barycentre and scan-epoch propagation (the
+    planets' offsets, in mas, are FP64 either way)."""
     hp, gs = am['hipp'], am['gost']
-    cat = am['catalogs']
+    cat = np.asarray(am['catalogs'], dtype=dtype)
     nh, ng = len(hp['BJD']), len(gs['BJD'])
     t_iad = np.concatenate([hp['BJD'], gs['BJD']])
     plx0 = cat[-1, 3] - off5[2]
     coor = np.zeros((3, nh + ng))
     for th in theta_planets:
         coor += calc_astro(th, plx0, t_iad, am['common_t'])
-    bary = barycenter(am, off5)
+    bary = barycenter(am, off5, dtype)
     J_H, J_G = jit2
     # Hipparcos: bary at the Hipparcos epoch against the Hipparcos solution
     ref_ra, ref_dec, ref_plx, ref_pmra, ref_pmde = cat[0, 1:6]
@@ -149,7 +158,7 @@ def loglike_am(am, theta_planets, off5, jit2):
     ll = -0.5 * (np.sum(res ** 2 / var + np.log(var)) + nh * LOG_2PI)
     # GOST: the DR3 barycentre propagated to each scan epoch
     b3 = bary[-1]
-    t_g = gs['BJD'] - cat[-1, 0]
+    t_g = np.asarray(gs['BJD'], dtype=dtype) - cat[-1, 0]
     decs = np.deg2rad(b3[1]) + b3[4] * t_g / DAY_PER_YEAR / 206265e3
     ras = np.deg2rad(b3[0]) + b3[3] * t_g / DAY_PER_YEAR / np.cos(decs) / 206265e3
     ref_ra3, ref_dec3 = cat[-1, 1], cat[-1, 2]
@@ -161,8 +170,8 @@ def loglike_am(am, theta_planets, off5, jit2):
     dplx_g = b3[2] + coor[2, nh:]
     abs_g = gs['SPSI'] * dra_g + gs['CPSI'] * ddec_g + gs['parf'] * dplx_g
     for row, (catn, ci) in enumerate((('GDR2', 1), ('GDR3', 2))):
-        p = am['gsv'][catn] @ abs_g[am['masks'][catn]]
-        r = am['astro_gost'][row] - p
-        quad = r @ am['inv_cov'][ci] @ r / J_G ** 2
+        p = np.asarray(am['gsv'][catn], dtype=dtype) @ abs_g[am['masks'][catn]]
+        r = np.asarray(am['astro_gost'][row], dtype=dtype) - p
+        quad = r @ np.asarray(am['inv_cov'][ci], dtype=dtype) @ r / J_G ** 2
         ll += -0.5 * (quad + 5 * np.log(J_G ** 2) + am['log_det_cov'][ci] + 5 * LOG_2PI)
-    return float(ll)
+    return ll if dtype is not np.float64 else float(ll)

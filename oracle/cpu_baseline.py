@@ -50,8 +50,9 @@ def faithful_spec(spec):
 def time_pool(spec, data, thetas, ncores=None, min_seconds=10.0, max_seconds=30.0):
     """evals/s of the reference-faithful path over a Pool of ncores processes.
 
-    Maps ``thetas`` repeatedly (chunks of one walker per task, as Pool.map
-    over walkers does) until at least ``min_seconds`` have passed.
+    Maps ``thetas`` repeatedly with Pool.map's default chunking (as emcee's
+    ``pool.map`` over the walkers does) until at least ``min_seconds`` have
+    passed.
     Returns (evals_per_second, n_evals, seconds, ncores).
     """
     ncores = int(ncores or os.cpu_count() or 1)
@@ -62,7 +63,7 @@ def time_pool(spec, data, thetas, ncores=None, min_seconds=10.0, max_seconds=30.
         n = 0
         t0 = time.perf_counter()
         while True:
-            pool.map(_eval, list(thetas), chunksize=1)
+            pool.map(_eval, list(thetas))
             n += len(thetas)
             el = time.perf_counter() - t0
             if el >= min_seconds or el >= max_seconds:
@@ -82,9 +83,9 @@ class PoolTimer:
         self.pool.map(_eval, list(thetas[:self.ncores]), chunksize=1)
 
     def step(self, thetas):
-        """Seconds to evaluate ``thetas`` one walker per task."""
+        """Seconds to evaluate ``thetas`` (Pool.map's default chunking)."""
         t0 = time.perf_counter()
-        self.pool.map(_eval, list(thetas), chunksize=1)
+        self.pool.map(_eval, list(thetas))
         return time.perf_counter() - t0
 
     def close(self):
@@ -138,7 +139,7 @@ def time_pool_many(specs, datas, tasks, n_epochs, ncores=None, min_seconds=10.0,
         n, units = 0, 0
         t0 = time.perf_counter()
         while True:
-            pool.map(_eval_many, tasks, chunksize=1)
+            pool.map(_eval_many, tasks)
             n += len(tasks)
             units += work
             el = time.perf_counter() - t0
@@ -156,9 +157,9 @@ class PoolTimerMany:
         self.pool = ctx.Pool(self.ncores, initializer=_init_many, initargs=(specs, datas))
 
     def step(self, tasks):
-        """Seconds to evaluate (system, theta) tasks, one walker per task."""
+        """Seconds to evaluate (system, theta) tasks (default chunking)."""
         t0 = time.perf_counter()
-        self.pool.map(_eval_many, list(tasks), chunksize=1)
+        self.pool.map(_eval_many, list(tasks))
         return time.perf_counter() - t0
 
     def close(self):

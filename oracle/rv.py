@@ -326,6 +326,9 @@ class OracleRV:
         # run the reference's no-op per-instrument MA loop literally (timing)
         self.faithful_quirk_loop = bool(spec.get('faithful_quirk_loop', False))
         self.am = data.get('am') if any(b['type'] == 'AstrometryOffset' for b in self.blocks) else None
+        # np.longdouble: the astrometric barycentre and scan-epoch propagation
+        # in extended precision (oracle/am.py)
+        self.am_dtype = np.float64
         self.X_ = np.asarray(data['X'], dtype=np.float64)
         self.Y_ = np.asarray(data['Y'], dtype=np.float64)
         self.YERR_ = np.asarray(data['YERR'], dtype=np.float64)
@@ -511,7 +514,7 @@ class OracleRV:
             planets = [th[sl] for b, sl in zip(self.blocks, self.slices) if b['type'] == 'Keplerian']
             off = [th[sl] for b, sl in zip(self.blocks, self.slices) if b['type'] == 'AstrometryOffset'][0]
             jit = [th[sl] for b, sl in zip(self.blocks, self.slices) if b['type'] == 'AstrometryJitter'][0]
-            ll += _am.loglike_am(self.am, planets, off, jit)
+            ll = float(ll + _am.loglike_am(self.am, planets, off, jit, dtype=self.am_dtype))
         return ll
 
     def my_prior(self, theta):

@@ -35,7 +35,8 @@ Writes
   am_kat.npz        -- loglike_AM of the HIP 21850 model at seeded theta by the
                        reference's own generated astrometry functions
                        (ReddModel._write_model_AM text with constants.scr), and
-                       the oracle's (logL, logprior) of the a00.like model
+                       the oracle's (logL, logprior) of the a00.like model, with
+                       logL also with the astrometric propagation in long double
   smartsetter_kat.json -- default limits / priors / prargs of every block type
                        as the reference's SmartSetter methods (block_repo.py,
                        run from its source on a small column shim) set them
@@ -493,8 +494,10 @@ def am_fixture(ref_root):
     ref_am = np.array([float(g['loglike_AM'](f)) for f in full])
     lp = np.array([o.my_prior(t) for t in th])
     ll = np.array([o.my_likelihood(t) if np.isfinite(p) else -np.inf for t, p in zip(th, lp)])
+    o.am_dtype = np.longdouble
+    ll_ld = np.array([o.my_likelihood(t) if np.isfinite(p) else -np.inf for t, p in zip(th, lp)])
     np.savez_compressed(os.path.join(HERE, 'am_kat.npz'), theta=th, loglike_am_ref=ref_am, logl=ll,
-                        logprior=lp)
+                        logl_ld=ll_ld, logprior=lp)
     print('am_kat:', len(th), 'points;', int(np.isfinite(lp).sum()), 'inside the prior')
 
 

@@ -59,3 +59,25 @@ def test_astrometry_data_shapes(hip):
     assert int(am.masks['GDR2'].sum()) == 17 and int(am.masks['GDR3'].sum()) == 32
     assert am.gsv['GDR2'].shape == (5, 17) and am.gsv['GDR3'].shape == (5, 32)
     np.testing.assert_allclose(am.astro_gost[1, :2], 0.0)
+
+
+def test_fp64_rounding_of_the_reference_formulas(hip):
+    """The reference's formulas in FP64 against the same formulas with the
+    barycentre and scan-epoch propagation in long double (the fixture's
+    logl_ld, recomputed here): they differ by the FP64 rounding of ~60-degree
+    positions, at most a few 1e-9 of the log-likelihood on these points
+    (measured 4.2e-9), which is the scale the device's astrometric term is
+    measured against."""
+    model, data, am, o = hip
+    k = np.load(os.path.join(GOLDEN, 'am_kat.npz'))
+    fin = np.isfinite(k['logprior'])
+    o.am_dtype = np.longdouble
+    try:
+        ld = np.array([o.my_likelihood(t) for t in k['theta'][fin]])
+    finally:
+        o.am_dtype = np.float64
+    if np.finfo(np.longdouble).eps < 1e-18:
+        np.testing.assert_allclose(ld, k['logl_ld'][fin], rtol=1e-14)
+    rel = np.abs(k['logl'][fin] - k['logl_ld'][fin]) / np.abs(k['logl_ld'][fin])
+    print(f'FP64 reference formulas against long double: median {np.median(rel):.2e} max {rel.max():.2e}')
+    assert rel.max() <= 1e-8

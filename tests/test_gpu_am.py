@@ -3,10 +3,19 @@ GPU against the oracle, which tests/test_am_oracle.py pins to the
 reference's own generated astrometry functions: the HIP 21850 model of the
 reference's tests/03_hip21850_test.ipynb.
 
-Tolerances: FP64 logL relative 1e-11 (the astrometric term is FP64 in both
-precisions; the RV term as in test_gpu_logpost), mixed 1e-6, logprior 1e-13
-(the Isotropic inclination prior included); the PT sampler with the
-astrometric term walks the oracle sampler's chain (same Philox stream).
+The reference's formulas handle absolute positions in degrees, whose FP64
+rounding (2.5e-8 mas per ulp of 60 degrees) moves the Gaia term by up to
+~4e-9 of the total log-likelihood (measured: the FP64 oracle, which equals
+the reference's own functions to 1e-12, against the same formulas with the
+propagation in long double).  The device forms the scan positions as offsets
+from the DR3 position and is compared with the long-double value:
+FP64 logL relative 5e-10 (the astrometric term is FP64 in both precisions;
+what remains is the Hipparcos-epoch barycentre, propagated through absolute
+angles as the reference does, where one ulp moves the Hipparcos term by up
+to 5.4e-11 of the total; measured 1.1e-10), mixed 1e-6, logprior 1e-13 (the
+Isotropic inclination prior included).  The PT sampler with the astrometric
+term walks the oracle sampler's chain (same Philox stream; the oracle's
+astrometric term in long double).
 """
 import os
 
@@ -31,7 +40,7 @@ def hip(lib, cuda):
     return model, data, am, Context(model, 'cuda:0')
 
 
-@pytest.mark.parametrize('prec,tol', [(N.EMP_PREC_FP64, 1e-11), (N.EMP_PREC_MIXED, 1e-6)])
+@pytest.mark.parametrize('prec,tol', [(N.EMP_PREC_FP64, 5e-10), (N.EMP_PREC_MIXED, 1e-6)])
 def test_logpost_matches_the_oracle(hip, prec, tol):
     model, data, am, ctx = hip
     k = np.load(os.path.join(GOLDEN, 'am_kat.npz'))
@@ -42,8 +51,11 @@ def test_logpost_matches_the_oracle(hip, prec, tol):
     np.testing.assert_allclose(lp, k['logprior'], rtol=1e-13, atol=1e-13)
     fin = np.isfinite(k['logprior'])
     assert np.all(ll[~fin] == -np.inf)
-    rel = np.abs(ll[fin] - k['logl'][fin]) / np.abs(k['logl'][fin])
-    print('astrometry + RV logL: max relative error', rel.max())
+    ld = k['logl_ld'][fin]
+    rel = np.abs(ll[fin] - ld) / np.abs(ld)
+    ref_noise = np.abs(k['logl'][fin] - ld) / np.abs(ld)
+    print(f'astrometry + RV logL against the long-double value: max relative error {rel.max():.2e} '
+          f'(the FP64 reference formulas: {ref_noise.max():.2e})')
     assert rel.max() <= tol
 
 
@@ -59,6 +71,7 @@ def test_pt_replay_matches_the_oracle_sampler(hip):
                   adapt_tau=20, use_graph=False, context=ctx, autotune=False)
     s.run_mcmc(p0, nsweeps=S)
     o = OracleRV(model.spec(), dict(data.as_dict(), am=am.as_dict()))
+    o.am_dtype = np.longdouble
 
     def f(th):
         th = np.atleast_2d(th)
@@ -69,7 +82,7 @@ def test_pt_replay_matches_the_oracle_sampler(hip):
     ora.set_positions(p0)
     ora.run(S)
     np.testing.assert_allclose(s.get_chain(), np.moveaxis(np.array(ora.chain), 1, 0), rtol=1e-12, atol=1e-12)
-    np.testing.assert_allclose(s.get_log_like(), np.moveaxis(np.array(ora.log_like), 1, 0), rtol=1e-11)
+    np.testing.assert_allclose(s.get_log_like(), np.moveaxis(np.array(ora.log_like), 1, 0), rtol=5e-10)
     assert ora.accepted.sum() > 0
 
 
