@@ -1388,10 +1388,6 @@ extern "C" int emp_pt_sweep_static(emp_handle* h, const emp_pt_state* st, const 
     return enqueue_sweep(h, &local, rec, s, nullptr);
 }
 
-extern "C" {
-
-}  // extern "C"
-
 namespace {
 
 // Capture one sweep into gc (replacing what it held): with `host` non-null
