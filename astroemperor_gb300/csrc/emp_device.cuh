@@ -191,13 +191,17 @@ struct Smem {
     int tile_bytes;        // staged epochs
     int group_bytes;       // per walker group
     int off_full, off_thp, off_pc, off_ins, off_acc, off_red, off_scan, off_pterm, off_misc;
+    int off_gma;               // GP with a live MA: per epoch of the tile x and g[q] (0 bytes otherwise)
     int off_fullf, n_fullf;    // float-float copy of the full vector (mixed): hi [n], lo [n]
     int total;
 
     __host__ __device__ static int align16(int x) { return (x + 15) & ~15; }
 
+    // gp_ma: a GP likelihood on the residuals of a live MA recurrence (the
+    // lane-chunk pass keeps each epoch's zero-state residual and its
+    // sensitivity to the incoming state until the scan gives that state)
     __host__ __device__ void build(int prec, int q, int L, int G, int tile, int n_full,
-                                   int n_free, int n_planets, int n_ins, int acc_order) {
+                                   int n_free, int n_planets, int n_ins, int acc_order, int gp_ma = 0) {
         int rs = prec == EMP_PREC_FP64 ? 8 : 4;          // real size
         int per_epoch = (prec == EMP_PREC_FP64) ? (8 * 3 + 4 + 8 * q)
                                                 : (4 * 5 + 4 + 4 * q);
@@ -215,6 +219,7 @@ struct Smem {
         off_scan = o; o += align16((L > 32 && q > 0) ? rs * (L / 32) * (q + q * q) : 0);
         off_pterm = o; o += align16(8 * (n_free + 2 * n_planets + 1));
         off_misc = o; o += 64;
+        off_gma = o;  o += align16((gp_ma && q > 0) ? rs * tile * (1 + q) : 0);
         group_bytes = align16(o);
         total = tile_bytes + G * group_bytes;
     }

@@ -791,7 +791,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
 
     Smem lay;
-    lay.build(PREC, Q, L, G, A.tile, A.lay_full, A.lay_free, A.lay_planets, A.lay_ins, A.lay_acc);
+    lay.build(PREC, Q, L, G, A.tile, A.lay_full, A.lay_free, A.lay_planets, A.lay_ins, A.lay_acc,
+              (A.gp_r != nullptr && Q > 0) ? 1 : 0);
 
     const int tid = threadIdx.x;
     const int g = tid / L;
@@ -809,6 +810,8 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
     R* scan = reinterpret_cast<R*>(gs + lay.off_scan);
     double* pterm = reinterpret_cast<double*>(gs + lay.off_pterm);
     double* misc = reinterpret_cast<double*>(gs + lay.off_misc);
+    R* gmx = reinterpret_cast<R*>(gs + lay.off_gma);     // [tile]: zero-state residual (GP with MA)
+    R* gmg = gmx + A.tile;                               // [q][tile]: its sensitivity
     int* flag = reinterpret_cast<int*>(misc + 4);
     constexpr int INSW = kInsW;
 
@@ -1169,17 +1172,18 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                     }
                     if (gp_on) {
                         // GP likelihood: hand the residual and err2 to k_gp
+                        // (with MA the residual follows the recurrence, below)
                         const size_t gi = (size_t)(base + r * C + k0 + e) * A.nwalk + wk;
                         if constexpr (PREC == EMP_PREC_FP64) {
-                            A.gp_r[gi] = (double)b;
+                            if (Q == 0) A.gp_r[gi] = (double)b;
                             A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
                         } else {
                             // float-float pairs for k_gp_ff
-                            reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)b, 0.f);
+                            if (Q == 0) reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)b, 0.f);
                             reinterpret_cast<float2*>(A.gp_e)[gi] =
                                 make_float2((float)(s_s2[ps] + insc[s_in[ps] * INSW + 1]), 0.f);
                         }
-                        continue;
+                        if (Q == 0) continue;
                     }
                     if (Q == 0) {
                         ks.add(b * b * w + lt);
@@ -1208,6 +1212,14 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                         xh[0] = x;
 #pragma unroll
                         for (int q2 = 0; q2 < NQ; ++q2) gh[0][q2] = gn[q2];
+                        if (gp_on) {
+                            // the residual is x + g . u once the scan gives
+                            // this lane's incoming state u
+                            gmx[ps] = x;
+#pragma unroll
+                            for (int q2 = 0; q2 < NQ; ++q2) gmg[q2 * tile + ps] = gn[q2];
+                            continue;
+                        }
                         const R wx = w * x;
                         ks.add(wx * x + lt);
 #pragma unroll
@@ -1282,6 +1294,19 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
                 for (int q3 = 0; q3 < NQ; ++q3) extra += u[q2] * u[q3] * S2[q2][q3];
             }
             if (valid) acc.add(extra);
+            if (gp_on && valid) {
+                // GP with MA: this lane's residuals after the recurrence
+                const int nr = max(0, min(C, nt - r * C));
+                for (int k = 0; k < nr; ++k) {
+                    const int ps = k * L + ((r + k) & (L - 1));
+                    R rr = gmx[ps];
+#pragma unroll
+                    for (int q2 = 0; q2 < NQ; ++q2) rr += gmg[q2 * tile + ps] * u[q2];
+                    const size_t gi = (size_t)(base + r * C + k) * A.nwalk + wk;
+                    if constexpr (PREC == EMP_PREC_FP64) A.gp_r[gi] = (double)rr;
+                    else reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)rr, 0.f);
+                }
+            }
             R nc[NQ];
             map_apply<R, NQ>(all, carry, nc);
 #pragma unroll

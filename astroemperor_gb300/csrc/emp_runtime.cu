@@ -241,9 +241,6 @@ int validate_model(const emp_model_desc* m) {
     if (m->gp_nterms < 0 || m->gp_nterms > EMP_MAX_GP_TERMS)
         return fail(EMP_E_SIZE, "gp_nterms=%d outside [0, %d]", m->gp_nterms, EMP_MAX_GP_TERMS);
     if (m->gp_nterms > 0) {
-        // a per-instrument MA under the reference quirk is a no-op (no MA on the device)
-        if (m->ma_order > 0 && (m->ma_global || !m->ma_quirk))
-            return fail(EMP_E_UNSUPPORTED, "a GP likelihood with an MA model");
         int dims = 0;
         for (int j = 0; j < m->gp_nterms; ++j) {
             const int kind = m->gp_kind[j];
@@ -312,7 +309,8 @@ int pick_tile(const emp_handle* h, int prec, int L, int G, Smem& lay) {
     int t = round_L(std::min(want, h->n));
     t = std::max(t, L);
     for (;;) {
-        lay.build(prec, h->q, L, G, t, h->lay[0], h->lay[1], h->lay[2], h->lay[3], h->lay[4]);
+        lay.build(prec, h->q, L, G, t, h->lay[0], h->lay[1], h->lay[2], h->lay[3], h->lay[4],
+                  (h->gp_M > 0 && h->q > 0) ? 1 : 0);
         if (lay.total <= 200 * 1024 || t <= L) break;
         t = std::max(L, round_L(t / 2));
     }

@@ -501,12 +501,10 @@ class ReddModel:
         gp = [b for b in self.blocks if b.type_ == 'Celerite2']
         if len(gp) > 1:
             raise ValueError('one Celerite2 block per model')
-        # the reference's per-instrument MOAV is a no-op (moav00.model:18-19), so
-        # with the quirk it leaves the GP's residuals alone; a live MA is not
-        # combined with the GP on this path
-        if gp and any(b.type_ == 'MOAV' and (b.is_global or not self.moav_reference_quirk)
-                      for b in self.blocks):
-            raise ValueError('a GP likelihood and a live MOAV block cannot be combined on this path')
+        # with a live MOAV block the GP models the residuals after the MA
+        # recurrence (02.like: gp_.mean = my_model's model, which the MA terms
+        # are part of); the reference's per-instrument MOAV is a no-op
+        # (moav00.model:18-19), so with the quirk the GP sees the plain residuals
         am = [b for b in self.blocks if b.type_ in ('AstrometryOffset', 'AstrometryJitter')]
         if am:
             types = sorted(b.type_ for b in am)

@@ -130,6 +130,18 @@ def gp_case_models(arr, n_in=12, n_near=8):
             c[j] = 0.5 * (lim[j, 0] + lim[j, 1])
         th = draw_thetas(m, rng, n_in=n_in, center=c, n_near=n_near)
         out[name] = (m, d, th)
+    # a GP on the residuals of a live MA recurrence: global MA(1), and the
+    # documented per-instrument MA(2) (the reference's quirk off)
+    for name, ker, moav in (('grot_gma1', GP_KERNELS['grot'], {'order': 1, 'global': True}),
+                            ('sho_ma2_inst', GP_KERNELS['sho_rho_tau_sigma'], {'order': 2, 'global': False})):
+        m, d = model_51peg(arr, k=1, par=1, gp=ker, moav=moav, quirk=False)
+        free = m.free_parameters()
+        lim = m.limits_free()
+        c = np.array(PEG_MAP_P1 + [0.0] * (len(free) - len(PEG_MAP_P1)))
+        for j in range(len(PEG_MAP_P1), len(free)):
+            c[j] = 0.5 * (lim[j, 0] + lim[j, 1])
+        th = draw_thetas(m, rng, n_in=n_in, center=c, n_near=n_near)
+        out[name] = (m, d, th)
     return out
 
 

@@ -239,9 +239,6 @@ def test_create_rejects_bad_gp_and_hill_fields(lib, peg_arr):
             md.gp_slot[j][i] = md.gp_slot[0][i]
     rc, msg = _create(lib, md, ds)
     assert rc == N.EMP_E_UNSUPPORTED and 'dimensions' in msg
-    md = m.descriptor(); md.ma_order = 1; md.ma_slot = 0; md.ma_global = 1
-    rc, msg = _create(lib, md, ds)
-    assert rc == N.EMP_E_UNSUPPORTED and 'MA' in msg
     # Hill priors
     m2, d2 = model_51peg(peg_arr, k=2, par=1, hill=1.1)
     ds2, keep2 = _dataset(d2.BJD, d2.RV, d2.eRV, d2.Flag)

@@ -120,12 +120,27 @@ def test_oracle_gp_likelihood_equals_dense(peg_arr):
         assert n_fin >= 3, name
 
 
-def test_gp_with_moav_rejected(peg_arr):
-    data = peg_data(peg_arr)
-    with pytest.raises(ValueError, match='MOAV'):
-        ReddModel([MOAVBlock(1, {'order': 1, 'global': True}), CeleriteBlock(GP_KERNELS['grot'])], data)
-    with pytest.raises(ValueError, match='MOAV'):
-        ReddModel([MOAVBlock(1, {'order': 1, 'global': False}), CeleriteBlock(GP_KERNELS['grot'])], data)
+def test_gp_with_live_moav_models_the_ma_residuals(peg_arr):
+    # 02.like: gp_.mean = my_model's model, which holds the MA terms of a live
+    # MOAV block (moav01.model), so the GP sees the residuals after the MA
+    from oracle import gp
+    for moav in ({'order': 1, 'global': True}, {'order': 2, 'global': False}):
+        m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'], moav=moav, quirk=False)
+        o = OracleRV(m.spec(), d.as_dict())
+        (terms,) = [b['gp_terms'] for b in o.blocks if b['type'] == 'Celerite2']
+        nma = 2 * moav['order']
+        x = np.concatenate([[4.231, 55.957, 1.769, 0.087, 0.061, 3.642, 2.961],
+                            [0.4, 5.0] * moav['order'], [2.5, 2.5, 2.5, 2.5]])
+        assert len(x) == m.ndim__
+        model, err2 = o.my_model(x)
+        x0 = x.copy()
+        x0[7:7 + nma:2] = 0.0                                   # MA coefficients off
+        model0, _ = o.my_model(x0)
+        assert np.max(np.abs(model - model0)) > 0.1
+        full = o.full_theta(x)
+        co = gp.coefficients([(k, [full[i] for i in sl]) for k, sl in terms])
+        dense = gp.dense_loglike(o.X_, o.Y_ - model, err2, co)
+        assert abs(o.my_likelihood(x) - dense) <= RTOL * abs(dense)
 
 
 def test_gp_with_quirk_moav_is_the_gp_alone(peg_arr):

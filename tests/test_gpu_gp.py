@@ -8,6 +8,9 @@ Tolerances
   mixed : |dlogL| / |logL| <= 1e-6 (residuals from the mixed-precision
           Keplerian pipeline, recursion in FP64)
   PT replay (FP64, same Philox stream): chains within 1e-13, logL 1e-9
+The cases include a GP on the residuals of a live MA recurrence (global
+MA(1); the documented per-instrument MA(2)), which the kernel forms after the
+lane-chunk scan has given each lane its incoming MA state.
 """
 import numpy as np
 import pytest
@@ -98,10 +101,12 @@ def _p0_near(m, T, W, seed):
     return np.clip(p, lo + 1e-9, hi - 1e-9)
 
 
-def test_gp_pt_replay_matches_oracle(peg_arr, lib, cuda):
+@pytest.mark.parametrize('moav', [None, {'order': 1, 'global': True}])
+def test_gp_pt_replay_matches_oracle(peg_arr, lib, cuda, moav):
     """Same Philox stream: the FP64 device sampler (stretch proposals through
-    k_logpost, likelihood and Metropolis test in k_gp) walks the oracle's chain."""
-    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['sho_rho_tau_sigma'])
+    k_logpost, likelihood and Metropolis test in k_gp) walks the oracle's chain;
+    with a global MA(1) the GP models the residuals after the recurrence."""
+    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['sho_rho_tau_sigma'], moav=moav, quirk=False)
     T, W, S = 2, 8, 5
     betas = np.array([1.0, 0.2])
     p0 = _p0_near(m, T, W, 3)
