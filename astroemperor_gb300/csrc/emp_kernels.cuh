@@ -535,7 +535,13 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 // a - b with one rounding (the product b * -1 is exact)
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.f), a); }
-__device__ __forceinline__ float2 rint2(float2 a) { return make_float2(rintf(a.x), rintf(a.y)); }
+// nearest integer by adding and subtracting 1.5 * 2^23, two packed FP32 adds instead of two
+// round-to-integer instructions (equal to rintf for |a| < 2^22; beyond, an integer within 1 of
+// a, which keeps a - rint2_add(a) exact and the phase reduction correct)
+__device__ __forceinline__ float2 rint2_add(float2 a) {
+    const float2 m = make_float2(12582912.f, 12582912.f);
+    return __fadd2_rn(__fadd2_rn(a, m), make_float2(-12582912.f, -12582912.f));
+}
 __device__ __forceinline__ float2 rcp_approx2(float2 a) { return make_float2(rcp_fast(a.x), rcp_fast(a.y)); }
 // 1/a to about 1 ulp per element
 __device__ __forceinline__ float2 rcp_nr2(float2 a) {
@@ -551,12 +557,12 @@ __device__ __forceinline__ float2 mean_anomaly_pair(const float* pc, float2 th, 
     const float2 x = add2(p, ph);
     const float2 bv = sub2(x, p);
     const float2 xe = add2(sub2(p, sub2(x, bv)), sub2(ph, bv));
-    const float2 fr = sub2(x, rint2(x));
+    const float2 fr = sub2(x, rint2_add(x));
     const float2 lo = add2(add2(add2(pe, xe), bc2(pc[3])), fma2(th, bc2(pc[1]), mul2(tl, fh)));
     const float2 cyc0 = add2(fr, lo);
     const float2 cb = sub2(cyc0, fr);
     const float2 ce = add2(sub2(fr, sub2(cyc0, cb)), sub2(lo, cb));
-    const float2 cyc = sub2(cyc0, rint2(cyc0));
+    const float2 cyc = sub2(cyc0, rint2_add(cyc0));
     const float2 tp = bc2(6.28318530717958647692f);
     const float2 M = mul2(cyc, tp);
     mlo = add2(fma2(cyc, tp, make_float2(-M.x, -M.y)), fma2(cyc, bc2(-1.7484555e-07f), mul2(ce, tp)));
@@ -565,7 +571,9 @@ __device__ __forceinline__ float2 mean_anomaly_pair(const float* pc, float2 th, 
 
 // sincos_acc on a pair
 __device__ __forceinline__ void sincos_acc_pair(float2 x, float2& s, float2& c) {
-    const float2 q = rint2(mul2(x, bc2(0.636619772367581343f)));
+    // q = rint(x 2/pi) (|x| is a few radians), and its integer from the bits of x 2/pi + 1.5 * 2^23
+    const float2 qm = add2(mul2(x, bc2(0.636619772367581343f)), bc2(12582912.f));
+    const float2 q = add2(qm, bc2(-12582912.f));
     float2 r = fma2(q, bc2(-1.5703125f), x);
     r = fma2(q, bc2(-4.83826794896619231e-04f), r);
     r = fma2(q, bc2(-2.56328273e-12f), r);
@@ -579,7 +587,7 @@ __device__ __forceinline__ void sincos_acc_pair(float2 x, float2& s, float2& c) 
     pc = fma2(r2, pc, bc2(4.16666667e-02f));
     pc = fma2(r2, pc, bc2(-0.5f));
     const float2 cr = fma2(r2, pc, bc2(1.f));
-    const int qx = (int)q.x, qy = (int)q.y;
+    const int qx = __float_as_int(qm.x) - 0x4B400000, qy = __float_as_int(qm.y) - 0x4B400000;
     float ssx = (qx & 1) ? cr.x : sr.x, ccx = (qx & 1) ? sr.x : cr.x;
     float ssy = (qy & 1) ? cr.y : sr.y, ccy = (qy & 1) ? sr.y : cr.y;
     s = make_float2((qx & 2) ? -ssx : ssx, (qy & 2) ? -ssy : ssy);
