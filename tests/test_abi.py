@@ -41,9 +41,12 @@ LAYOUT_C = r'''
 #include "emp_gpu.h"
 #define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
 int main(void) {
-  printf("emp_prior %zu\nemp_model_desc %zu\nemp_dataset_desc %zu\nemp_pt_state %zu\nemp_pt_record %zu\n",
+  printf("emp_prior %zu\nemp_model_desc %zu\nemp_dataset_desc %zu\nemp_pt_state %zu\nemp_pt_record %zu\n"
+         "emp_am_desc %zu\n",
          sizeof(emp_prior), sizeof(emp_model_desc), sizeof(emp_dataset_desc),
-         sizeof(emp_pt_state), sizeof(emp_pt_record));
+         sizeof(emp_pt_state), sizeof(emp_pt_record), sizeof(emp_am_desc));
+  P(emp_model_desc, am_on) P(emp_model_desc, am_jitter_slot)
+  P(emp_am_desc, catalogs) P(emp_am_desc, gsv) P(emp_am_desc, common_t)
   P(emp_model_desc, kep_param) P(emp_model_desc, full_fixed) P(emp_model_desc, prior)
   P(emp_model_desc, prior_slot) P(emp_model_desc, derived) P(emp_model_desc, loglike_const)
   P(emp_pt_state, theta) P(emp_pt_state, n_perm_units) P(emp_pt_state, seed)
@@ -65,7 +68,7 @@ def test_struct_layout_matches_c(tmp_path):
                                                          check=True).stdout.strip().splitlines())
     types = {'emp_prior': N.EmpPrior, 'emp_model_desc': N.EmpModelDesc,
              'emp_dataset_desc': N.EmpDatasetDesc, 'emp_pt_state': N.EmpPtState,
-             'emp_pt_record': N.EmpPtRecord}
+             'emp_pt_record': N.EmpPtRecord, 'emp_am_desc': N.EmpAmDesc}
     for k, v in out.items():
         if '.' in k:
             t, f = k.split('.')
@@ -162,6 +165,21 @@ def test_null_handles_are_errors_not_crashes(lib):
     assert lib.emp_set_launch(None, 0, 32, 0) == N.EMP_E_INVALID
     assert lib.emp_destroy(None) == N.EMP_OK
     assert b'NULL' in lib.emp_last_error_string()
+    am = N.EmpAmDesc()
+    assert lib.emp_set_astrometry(None, C.byref(am)) == N.EMP_E_INVALID
+    assert lib.emp_logpost_grad(None, None, 1, None, None, None, None, None) == N.EMP_E_INVALID
+
+
+def test_history_reductions_reject_bad_arguments(lib):
+    # emp_ladder_sums / emp_autocorr check their arguments before any launch
+    buf = C.c_void_p(16)            # never dereferenced: the checks fail first
+    assert lib.emp_ladder_sums(None, 10, 2, 4, 0, 1, None, None, 0, buf, None, None) == N.EMP_E_INVALID
+    assert lib.emp_ladder_sums(buf, 10, 0, 4, 0, 1, None, None, 0, buf, None, None) == N.EMP_E_INVALID
+    assert lib.emp_ladder_sums(buf, 10, 2, 4, 0, 0, None, None, 0, buf, None, None) == N.EMP_E_INVALID
+    assert lib.emp_ladder_sums(buf, 10, 2, 4, 0, 1, None, None, 3, buf, None, None) == N.EMP_E_INVALID
+    assert lib.emp_autocorr(None, 10, 2, 4, 3, 0, 1, 8, buf, None) == N.EMP_E_INVALID
+    assert lib.emp_autocorr(buf, 10, 2, 4, 3, 0, 1, 0, buf, None) == N.EMP_E_INVALID
+    assert lib.emp_autocorr(buf, 60000, 1, 2, 1, 0, 1, 8, buf, None) == N.EMP_E_SIZE
 
 
 def _batch(lib, models, parts):
