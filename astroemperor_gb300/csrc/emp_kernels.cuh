@@ -21,6 +21,7 @@
 // exp of log-periods, the varying prior terms and the final sums.  Bounds
 // of priors are compared exactly on the integer pipe.
 #pragma once
+#include <type_traits>
 #include "emp_device.cuh"
 
 namespace emp {
@@ -789,8 +790,11 @@ template <> struct LaneAcc<EMP_PREC_MIXED> {
     }
 };
 
+// Mixed kernels of 128 threads are held to 5 resident CTAs per SM (at most
+// 102 registers): a half-step of 10 x 256 walkers at 64 lanes is 640 CTAs,
+// which then run in one wave on 152 SMs instead of 608 + 32.
 template <int PREC, int Q, int L, int NT>
-__global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
+__global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 : 1) k_logpost(KArgs A) {
     using R = typename P<PREC>::R;
     constexpr int G = NT / L;
     constexpr int PC = P<PREC>::kPC;
@@ -1059,188 +1063,195 @@ __global__ void __launch_bounds__(NT) k_logpost(KArgs A) {
 #pragma unroll
             for (int q2 = 0; q2 < NQ; ++q2) { gh[m][q2] = (m == q2) ? R(1) : R(0); S2[m][q2] = R(0); }
         }
-        if (valid) {
-            const int nr = max(0, min(C, nt - r * C));
-#pragma unroll 1
-            for (int k0 = 0; k0 < nr; k0 += NE) {
-                int pos[NE];
-                bool ok[NE];
-                R model[NE];
-#pragma unroll
-                for (int e = 0; e < NE; ++e) {
-                    const int kk = k0 + e < nr ? k0 + e : nr - 1;
-                    ok[e] = k0 + e < nr;
-                    pos[e] = kk * L + ((r + kk) & (L - 1));
-                    model[e] = R(0);
-                }
-                if constexpr (PREC == EMP_PREC_FP64) {
-#pragma unroll
+        // the pass over the lane's epochs, compiled once with the GP residual
+        // writes and once without, so that the Gaussian path carries none of them
+        auto epoch_pass = [&](auto gpw) {
+            constexpr bool GPW = decltype(gpw)::value;
+            if (valid) {
+                const int nr = max(0, min(C, nt - r * C));
+    #pragma unroll 1
+                for (int k0 = 0; k0 < nr; k0 += NE) {
+                    int pos[NE];
+                    bool ok[NE];
+                    R model[NE];
+    #pragma unroll
                     for (int e = 0; e < NE; ++e) {
-                        const double t = (double)s_t0[pos[e]];
-                        double m = 0.0;
-                        for (int p = 0; p < n_planets; ++p)
-                            m += rv_term_f64((const double*)(pcs + p * PC), t);
-                        if (acc_order > 0) {
-                            // np.polyval(concat(theta_acc, [0]), X_ - X_[0])
-                            double x = t - t0, pv = 0.0;
-                            for (int j = 0; j < acc_order; ++j) pv = pv * x + accc[j];
-                            m += pv * x;
-                        }
-                        model[e] = (R)m;
+                        const int kk = k0 + e < nr ? k0 + e : nr - 1;
+                        ok[e] = k0 + e < nr;
+                        pos[e] = kk * L + ((r + kk) & (L - 1));
+                        model[e] = R(0);
                     }
-                } else {
-                    constexpr int NP = NE / 2;
-                    float th[NE], tl[NE];
-#pragma unroll
-                    for (int e = 0; e < NE; ++e) { th[e] = (float)s_t0[pos[e]]; tl[e] = (float)s_t1[pos[e]]; }
-                    float2 th2[NP], tl2[NP], mod2[NP];
-#pragma unroll
-                    for (int j = 0; j < NP; ++j) {
-                        th2[j] = make_float2(th[2 * j], th[2 * j + 1]);
-                        tl2[j] = make_float2(tl[2 * j], tl[2 * j + 1]);
-                        mod2[j] = bc2(0.f);
-                    }
-                    for (int p = 0; p < n_planets; ++p) {
-                        const float* pc = (const float*)(pcs + p * PC);
-                        float2 M[NP], ml[NP], sn[NP], cs[NP];
-#pragma unroll
-                        for (int j = 0; j < NP; ++j) M[j] = mean_anomaly_pair(pc, th2[j], tl2[j], ml[j]);
-                        const float ec = pc[4], el = pc[8];
-                        kepler_pairs<NP>(M, ml, ec, el, pc + 12, sn, cs);
-#pragma unroll
-                        for (int j = 0; j < NP; ++j) {
-                            // (A (cos E - e) - B sin E) / (1 - e cos E) + C with
-                            // float-float A, B, C, e
-                            const float2 cme = sub2(sub2(cs[j], bc2(ec)), bc2(el));
-                            const float2 inv = rcp_nr2(fma2(bc2(-el), cs[j], fma2(bc2(-ec), cs[j], bc2(1.f))));
-                            const float2 hi = fma2(fma2(bc2(pc[5]), cme, mul2(bc2(-pc[6]), sn[j])), inv, bc2(pc[7]));
-                            const float2 lo = fma2(fma2(bc2(pc[9]), cme, mul2(bc2(-pc[10]), sn[j])), inv, bc2(pc[11]));
-                            mod2[j] = add2(mod2[j], add2(hi, lo));
-                        }
-                    }
-#pragma unroll
-                    for (int j = 0; j < NP; ++j) {
-                        model[2 * j] = (R)mod2[j].x;
-                        model[2 * j + 1] = (R)mod2[j].y;
-                    }
-                    if (acc_order > 0) {
-#pragma unroll
-                        for (int e = 0; e < NE; ++e) {
-                            const float x = (th[e] - (float)t0) + tl[e];
-                            float pv = 0.f;
-                            for (int j = 0; j < acc_order; ++j) pv = pv * x + (float)accc[j];
-                            model[e] += (R)(pv * x);
-                        }
-                    }
-                }
-                // mixed: the per-epoch quantities that do not depend on the MA
-                // state (residual, 1/err2, log err2, MA coefficients) two epochs
-                // per instruction; the recurrence below stays sequential
-                R bb[NE], ww[NE], lw[NE], aa[NE][NQ];
-                if constexpr (PREC == EMP_PREC_MIXED) {
-#pragma unroll
-                    for (int j = 0; j < NE / 2; ++j) {
-                        const int p0 = pos[2 * j], p1 = pos[2 * j + 1];
-                        const float* i0 = (const float*)(insc + s_in[p0] * INSW);
-                        const float* i1 = (const float*)(insc + s_in[p1] * INSW);
-                        const float2 m2 = make_float2((float)model[2 * j], (float)model[2 * j + 1]);
-                        const float2 b2 = add2(sub2(sub2(make_float2(s_y[p0], s_y[p1]), make_float2(i0[0], i1[0])), m2),
-                                               sub2(make_float2(s_ylo[p0], s_ylo[p1]), make_float2(i0[2], i1[2])));
-                        const float2 e2 = add2(make_float2(s_s2[p0], s_s2[p1]), make_float2(i0[1], i1[1]));
-                        const float2 w2 = rcp_nr2(e2);
-                        const float2 l2 = mul2(make_float2(lg2_fast(e2.x), lg2_fast(e2.y)),
-                                               bc2(0.69314718055994531f));
-                        bb[2 * j] = b2.x; bb[2 * j + 1] = b2.y;
-                        ww[2 * j] = w2.x; ww[2 * j + 1] = w2.y;
-                        lw[2 * j] = l2.x; lw[2 * j + 1] = l2.y;
-#pragma unroll
-                        for (int c = 0; c < Q; ++c) {
-                            const float2 x2 = mul2(make_float2(s_dt[c * tile + p0], s_dt[c * tile + p1]),
-                                                   make_float2(i0[4 + 2 * c], i1[4 + 2 * c]));
-                            const float2 a2 = mul2(make_float2(i0[3 + 2 * c], i1[3 + 2 * c]),
-                                                   make_float2(ex2_fast(x2.x), ex2_fast(x2.y)));
-                            aa[2 * j][c] = a2.x; aa[2 * j + 1][c] = a2.y;
-                        }
-                    }
-                }
-#pragma unroll
-                for (int e = 0; e < NE; ++e) {
-                    if (!ok[e]) continue;
-                    const int ps = pos[e];
-                    R b, w, lt;
-                    const R* ic = insc;
                     if constexpr (PREC == EMP_PREC_FP64) {
-                        ic = insc + s_in[ps] * INSW;
-                        const R err2 = s_s2[ps] + ic[1];
-                        b = s_y[ps] - (model[e] + ic[0]);
-                        w = R(1) / err2;
-                        lt = (R)log((double)err2);
+    #pragma unroll
+                        for (int e = 0; e < NE; ++e) {
+                            const double t = (double)s_t0[pos[e]];
+                            double m = 0.0;
+                            for (int p = 0; p < n_planets; ++p)
+                                m += rv_term_f64((const double*)(pcs + p * PC), t);
+                            if (acc_order > 0) {
+                                // np.polyval(concat(theta_acc, [0]), X_ - X_[0])
+                                double x = t - t0, pv = 0.0;
+                                for (int j = 0; j < acc_order; ++j) pv = pv * x + accc[j];
+                                m += pv * x;
+                            }
+                            model[e] = (R)m;
+                        }
                     } else {
-                        b = bb[e]; w = ww[e]; lt = lw[e];
+                        constexpr int NP = NE / 2;
+                        float th[NE], tl[NE];
+    #pragma unroll
+                        for (int e = 0; e < NE; ++e) { th[e] = (float)s_t0[pos[e]]; tl[e] = (float)s_t1[pos[e]]; }
+                        float2 th2[NP], tl2[NP], mod2[NP];
+    #pragma unroll
+                        for (int j = 0; j < NP; ++j) {
+                            th2[j] = make_float2(th[2 * j], th[2 * j + 1]);
+                            tl2[j] = make_float2(tl[2 * j], tl[2 * j + 1]);
+                            mod2[j] = bc2(0.f);
+                        }
+                        for (int p = 0; p < n_planets; ++p) {
+                            const float* pc = (const float*)(pcs + p * PC);
+                            float2 M[NP], ml[NP], sn[NP], cs[NP];
+    #pragma unroll
+                            for (int j = 0; j < NP; ++j) M[j] = mean_anomaly_pair(pc, th2[j], tl2[j], ml[j]);
+                            const float ec = pc[4], el = pc[8];
+                            kepler_pairs<NP>(M, ml, ec, el, pc + 12, sn, cs);
+    #pragma unroll
+                            for (int j = 0; j < NP; ++j) {
+                                // (A (cos E - e) - B sin E) / (1 - e cos E) + C with
+                                // float-float A, B, C, e
+                                const float2 cme = sub2(sub2(cs[j], bc2(ec)), bc2(el));
+                                const float2 inv = rcp_nr2(fma2(bc2(-el), cs[j], fma2(bc2(-ec), cs[j], bc2(1.f))));
+                                const float2 hi = fma2(fma2(bc2(pc[5]), cme, mul2(bc2(-pc[6]), sn[j])), inv, bc2(pc[7]));
+                                const float2 lo = fma2(fma2(bc2(pc[9]), cme, mul2(bc2(-pc[10]), sn[j])), inv, bc2(pc[11]));
+                                mod2[j] = add2(mod2[j], add2(hi, lo));
+                            }
+                        }
+    #pragma unroll
+                        for (int j = 0; j < NP; ++j) {
+                            model[2 * j] = (R)mod2[j].x;
+                            model[2 * j + 1] = (R)mod2[j].y;
+                        }
+                        if (acc_order > 0) {
+    #pragma unroll
+                            for (int e = 0; e < NE; ++e) {
+                                const float x = (th[e] - (float)t0) + tl[e];
+                                float pv = 0.f;
+                                for (int j = 0; j < acc_order; ++j) pv = pv * x + (float)accc[j];
+                                model[e] += (R)(pv * x);
+                            }
+                        }
                     }
-                    if (gp_on) {
-                        // GP likelihood: hand the residual and err2 to k_gp
-                        // (with MA the residual follows the recurrence, below)
-                        const size_t gi = (size_t)(base + r * C + k0 + e) * A.nwalk + wk;
+                    // mixed: the per-epoch quantities that do not depend on the MA
+                    // state (residual, 1/err2, log err2, MA coefficients) two epochs
+                    // per instruction; the recurrence below stays sequential
+                    R bb[NE], ww[NE], lw[NE], aa[NE][NQ];
+                    if constexpr (PREC == EMP_PREC_MIXED) {
+    #pragma unroll
+                        for (int j = 0; j < NE / 2; ++j) {
+                            const int p0 = pos[2 * j], p1 = pos[2 * j + 1];
+                            const float* i0 = (const float*)(insc + s_in[p0] * INSW);
+                            const float* i1 = (const float*)(insc + s_in[p1] * INSW);
+                            const float2 m2 = make_float2((float)model[2 * j], (float)model[2 * j + 1]);
+                            const float2 b2 = add2(sub2(sub2(make_float2(s_y[p0], s_y[p1]), make_float2(i0[0], i1[0])), m2),
+                                                   sub2(make_float2(s_ylo[p0], s_ylo[p1]), make_float2(i0[2], i1[2])));
+                            const float2 e2 = add2(make_float2(s_s2[p0], s_s2[p1]), make_float2(i0[1], i1[1]));
+                            const float2 w2 = rcp_nr2(e2);
+                            const float2 l2 = mul2(make_float2(lg2_fast(e2.x), lg2_fast(e2.y)),
+                                                   bc2(0.69314718055994531f));
+                            bb[2 * j] = b2.x; bb[2 * j + 1] = b2.y;
+                            ww[2 * j] = w2.x; ww[2 * j + 1] = w2.y;
+                            lw[2 * j] = l2.x; lw[2 * j + 1] = l2.y;
+    #pragma unroll
+                            for (int c = 0; c < Q; ++c) {
+                                const float2 x2 = mul2(make_float2(s_dt[c * tile + p0], s_dt[c * tile + p1]),
+                                                       make_float2(i0[4 + 2 * c], i1[4 + 2 * c]));
+                                const float2 a2 = mul2(make_float2(i0[3 + 2 * c], i1[3 + 2 * c]),
+                                                       make_float2(ex2_fast(x2.x), ex2_fast(x2.y)));
+                                aa[2 * j][c] = a2.x; aa[2 * j + 1][c] = a2.y;
+                            }
+                        }
+                    }
+    #pragma unroll
+                    for (int e = 0; e < NE; ++e) {
+                        if (!ok[e]) continue;
+                        const int ps = pos[e];
+                        R b, w, lt;
+                        const R* ic = insc;
                         if constexpr (PREC == EMP_PREC_FP64) {
-                            if (Q == 0) A.gp_r[gi] = (double)b;
-                            A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
+                            ic = insc + s_in[ps] * INSW;
+                            const R err2 = s_s2[ps] + ic[1];
+                            b = s_y[ps] - (model[e] + ic[0]);
+                            w = R(1) / err2;
+                            lt = (R)log((double)err2);
                         } else {
-                            // float-float pairs for k_gp_ff
-                            if (Q == 0) reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)b, 0.f);
-                            reinterpret_cast<float2*>(A.gp_e)[gi] =
-                                make_float2((float)(s_s2[ps] + insc[s_in[ps] * INSW + 1]), 0.f);
+                            b = bb[e]; w = ww[e]; lt = lw[e];
                         }
-                        if (Q == 0) continue;
-                    }
-                    if (Q == 0) {
-                        ks.add(b * b * w + lt);
-                    } else {
-                        R x = b;
-                        R gn[NQ];
-#pragma unroll
-                        for (int q2 = 0; q2 < NQ; ++q2) gn[q2] = R(0);
-#pragma unroll
-                        for (int c = 0; c < Q; ++c) {
-                            R a;
-                            if constexpr (PREC == EMP_PREC_FP64)
-                                a = ic[3 + 2 * c] * (R)exp((double)(s_dt[c * tile + ps] * ic[4 + 2 * c]));
-                            else
-                                a = aa[e][c];
-                            x -= a * xh[c];
-#pragma unroll
-                            for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
+                        if constexpr (GPW) {
+                            // GP likelihood: hand the residual and err2 to k_gp
+                            // (with MA the residual follows the recurrence, below)
+                            const size_t gi = (size_t)(base + r * C + k0 + e) * A.nwalk + wk;
+                            if constexpr (PREC == EMP_PREC_FP64) {
+                                if (Q == 0) A.gp_r[gi] = (double)b;
+                                A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
+                            } else {
+                                // float-float pairs for k_gp_ff
+                                if (Q == 0) reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)b, 0.f);
+                                reinterpret_cast<float2*>(A.gp_e)[gi] =
+                                    make_float2((float)(s_s2[ps] + insc[s_in[ps] * INSW + 1]), 0.f);
+                            }
+                            if (Q == 0) continue;
                         }
-#pragma unroll
-                        for (int m = NQ - 1; m > 0; --m) {
-                            xh[m] = xh[m - 1];
-#pragma unroll
-                            for (int q2 = 0; q2 < NQ; ++q2) gh[m][q2] = gh[m - 1][q2];
-                        }
-                        xh[0] = x;
-#pragma unroll
-                        for (int q2 = 0; q2 < NQ; ++q2) gh[0][q2] = gn[q2];
-                        if (gp_on) {
-                            // the residual is x + g . u once the scan gives
-                            // this lane's incoming state u
-                            gmx[ps] = x;
-#pragma unroll
-                            for (int q2 = 0; q2 < NQ; ++q2) gmg[q2 * tile + ps] = gn[q2];
-                            continue;
-                        }
-                        const R wx = w * x;
-                        ks.add(wx * x + lt);
-#pragma unroll
-                        for (int q2 = 0; q2 < NQ; ++q2) {
-                            S1[q2] += wx * gn[q2];
-                            const R wg = w * gn[q2];
-#pragma unroll
-                            for (int q3 = 0; q3 < NQ; ++q3) S2[q2][q3] += wg * gn[q3];
+                        if (Q == 0) {
+                            ks.add(b * b * w + lt);
+                        } else {
+                            R x = b;
+                            R gn[NQ];
+    #pragma unroll
+                            for (int q2 = 0; q2 < NQ; ++q2) gn[q2] = R(0);
+    #pragma unroll
+                            for (int c = 0; c < Q; ++c) {
+                                R a;
+                                if constexpr (PREC == EMP_PREC_FP64)
+                                    a = ic[3 + 2 * c] * (R)exp((double)(s_dt[c * tile + ps] * ic[4 + 2 * c]));
+                                else
+                                    a = aa[e][c];
+                                x -= a * xh[c];
+    #pragma unroll
+                                for (int q2 = 0; q2 < NQ; ++q2) gn[q2] -= a * gh[c][q2];
+                            }
+    #pragma unroll
+                            for (int m = NQ - 1; m > 0; --m) {
+                                xh[m] = xh[m - 1];
+    #pragma unroll
+                                for (int q2 = 0; q2 < NQ; ++q2) gh[m][q2] = gh[m - 1][q2];
+                            }
+                            xh[0] = x;
+    #pragma unroll
+                            for (int q2 = 0; q2 < NQ; ++q2) gh[0][q2] = gn[q2];
+                            if constexpr (GPW) {
+                                // the residual is x + g . u once the scan gives
+                                // this lane's incoming state u
+                                gmx[ps] = x;
+    #pragma unroll
+                                for (int q2 = 0; q2 < NQ; ++q2) gmg[q2 * tile + ps] = gn[q2];
+                                continue;
+                            }
+                            const R wx = w * x;
+                            ks.add(wx * x + lt);
+    #pragma unroll
+                            for (int q2 = 0; q2 < NQ; ++q2) {
+                                S1[q2] += wx * gn[q2];
+                                const R wg = w * gn[q2];
+    #pragma unroll
+                                for (int q3 = 0; q3 < NQ; ++q3) S2[q2][q3] += wg * gn[q3];
+                            }
                         }
                     }
                 }
             }
-        }
+        };
+        if (gp_on) epoch_pass(std::true_type{});
+        else epoch_pass(std::false_type{});
         if (valid) {
             acc.add((R)ks.s);
             acc.add((R)(-ks.c));

@@ -51,7 +51,10 @@ SEED = 1234
 # captures summarised in profiles/ (k_logpost_mixed_c2_halfstep.md,
 # k_logpost_mixed_c3_ragged_stretch.md; for gp the k_gp_prep + k_gp_ff pair of
 # k_gp_celerite_gp_sweep.md); None where no capture was taken
-NCU_TRAFFIC = {'c2': 614912, 'c3': 581037824, 'gp': 247542784}
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of each workload's dominant
+# kernel, from the ncu captures summarised under profiles/ (k_logpost_mixed_c2_halfstep.md,
+# k_logpost_mixed_c3_ragged_stretch.md, k_gp_celerite_gp_sweep.md, k_grad_c4_gradient_batch.md)
+NCU_TRAFFIC = {'c2': 614912, 'c3': 581037824, 'gp': 247542784, 'c4grad': 1083646568}
 
 
 def parse():
@@ -518,7 +521,10 @@ def main_grad(args):
     achieved = Fg * units / (k_ms * 1e-3) / 1e12
     peak32 = f32.value / 1e12
     roof = {'bound': 'fp32', 'achieved': achieved, 'peak': peak32, 'unit': 'TFLOP/s', 'frac': achieved / peak32,
-            'traffic': None, 'algorithmic_bytes': n * 25 + B * (8 * D * 3 + 16),
+            'traffic': NCU_TRAFFIC.get('c4grad'),
+            'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (the MA '
+                              'residual buffer written back from L2)',
+            'algorithmic_bytes': n * 25 + B * (8 * D * 3 + 16),
             'kernel': 'k_grad<Q=1> (log-posterior and its adjoint gradient)', 'kernel_ms': k_ms,
             'flop_per_eval_epoch': Fg,
             'peak_source': 'measured on this GPU by the library FMA probe (MEASURED_PEAKS.json has no '
