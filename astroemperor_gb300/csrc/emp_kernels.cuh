@@ -44,15 +44,20 @@ __device__ __forceinline__ bool in_support(double x, double lo, double hi) {
     return k >= dkey(lo) && k <= dkey(hi);
 }
 
+// the prior terms with FP64 transcendentals, out of line (rare; keeps the
+// kernels' code small)
+static __device__ __noinline__ double prior_var_term_rare(const emp_prior& p, double x) {
+    if (p.kind == EMP_PRIOR_BETA) return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
+    if (p.kind == EMP_PRIOR_ISOTROPIC) return log(0.5 * sin(x)) - p.a0;
+    return 0.0;
+}
 // value of a prior term that varies with x (Normal, Beta); x in support
 __device__ __forceinline__ double prior_var_term(const emp_prior& p, double x) {
     if (p.kind == EMP_PRIOR_NORMAL) {
         const double z = (x - p.a0) * p.a1;                // a1 = 1/s
         return -0.5 * z * z - p.a2;
     }
-    if (p.kind == EMP_PRIOR_BETA) return (p.a0 - 1.0) * log(x) + (p.a1 - 1.0) * log1p(-x) - p.a2;
-    if (p.kind == EMP_PRIOR_ISOTROPIC) return log(0.5 * sin(x)) - p.a0;
-    return 0.0;
+    return prior_var_term_rare(p, x);
 }
 
 // priors whose value varies with the parameter (the others are constants
@@ -303,7 +308,7 @@ __device__ __forceinline__ void split_ff(double x, float& hi, float& lo) {
 //        the low parts of e, A, B, C: the constants are formed in FP64 and
 //        kept as float-float pairs, so their rounding adds no systematic
 //        error to the model (a rounded constant shifts every epoch alike)
-__device__ __forceinline__ void planet_consts_mixed(int par, const double* v, float* pc) {
+static __device__ __noinline__ void planet_consts_mixed(int par, const double* v, float* pc) {
     double per, K, e = 0.0, cw = 1.0, sw = 0.0;
     bool use_tp = false;
     double phase = 0.0, tp = 0.0;
@@ -645,6 +650,10 @@ __device__ __forceinline__ void kepler_pairs(const float2 (&M)[NP], const float2
     }
 }
 
+// reference arithmetic: ((ndim-1) ln z + nlp) - cur > ln u (out of line: rare)
+static __device__ __noinline__ bool metropolis_fp64(double nlp, double cur, double z, int dm1, double u) {
+    return __dsub_rn(__dadd_rn(__dmul_rn((double)dm1, log(z)), nlp), cur) > log(u);
+}
 // log u < x with FP32 logarithms; inside a guard band the FP64 values decide
 __device__ __forceinline__ bool metropolis(double nlp, double cur, double z, int dm1, uint32_t uword) {
     const double u = u32u(uword);
@@ -655,8 +664,7 @@ __device__ __forceinline__ bool metropolis(double nlp, double cur, double z, int
     const float guard = 1e-4f * (1.f + fabsf(a) + fabsf(lu) + (float)dm1 * fabsf(lz));
     if (m > guard) return true;
     if (m < -guard) return false;
-    // reference arithmetic: ((ndim-1) ln z + nlp) - cur > ln u
-    return __dsub_rn(__dadd_rn(__dmul_rn((double)dm1, log(z)), nlp), cur) > log(u);
+    return metropolis_fp64(nlp, cur, z, dm1, u);
 }
 
 // ----------------------------------------------------------------------------
@@ -1176,7 +1184,7 @@ __global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 
                         if (!ok[e]) continue;
                         const int ps = pos[e];
                         R b, w, lt;
-                        const R* ic = insc;
+                        [[maybe_unused]] const R* ic = insc;
                         if constexpr (PREC == EMP_PREC_FP64) {
                             ic = insc + s_in[ps] * INSW;
                             const R err2 = s_s2[ps] + ic[1];
