@@ -84,6 +84,14 @@ struct SwapArgs {
     int64_t cap;
     int thin;
     int record_chain;
+    // the history rows, written by the swap CTA itself (REC) when they are
+    // small, instead of by k_record
+    const double* theta;
+    const double* logprior;
+    double* chain;
+    double* log_like;
+    double* log_prob;
+    double* smd_hist;
 };
 
 // uniform of a 32-bit word in FP32 (within 1e-7 of u32u; used only where a
@@ -113,7 +121,10 @@ __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
 // kernel) and the sweep counters advance here; for a batch (BATCH), system
 // s = blockIdx.x works on its own [T][W] block of every array with key
 // seed + s * 0x9E3779B97F4A7C15, and k_advance moves the shared counters.
-template <bool SMEM, bool BATCH>
+// REC (one system, staged): the CTA also writes the sweep's history rows
+// (chain, logL, tempered log-posterior, mean swap distances) as k_record
+// would, which saves a launch when they are small.
+template <bool SMEM, bool BATCH, bool REC = false>
 __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     // programmatic dependent launch (no-ops without the launch attribute):
     // the next kernel may launch now; this one waits for the stretch moves
@@ -233,6 +244,60 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     }
     if (SMEM)
         for (int k = tid; k < TW; k += nth) members[k] = s_mem[k];
+    if constexpr (REC && SMEM && !BATCH) {
+        // the rows k_record writes, from the staged positions; every thread
+        // reads the row counters before warp 0 advances them below
+        const bool rec_s = (S.thin <= 1) || ((int64_t)sweep % S.thin == (S.thin - 1));
+        const int64_t crow = S.n_rec[0], srow = S.n_rec[1];
+        if (S.record_chain && rec_s && crow < S.cap) {
+            if (S.chain) {
+                const int64_t tot = (int64_t)TW * S.D;
+                double* dst = S.chain + crow * tot;
+                for (int64_t idx = tid; idx < tot; idx += nth) {
+                    const int64_t tj = idx / S.D;
+                    const int d = (int)(idx - tj * S.D);
+                    dst[idx] = S.theta[(int64_t)s_mem[tj] * S.D + d];
+                }
+            }
+            for (int k = tid; k < TW; k += nth) {
+                const int slot = s_mem[k];
+                const double ll = S.logl[slot], lp = S.logprior[slot];
+                if (S.log_like) S.log_like[crow * TW + k] = ll;
+                if (S.log_prob)
+                    S.log_prob[crow * TW + k] =
+                        lp > -INFINITY ? __dadd_rn(__dmul_rn(s_bused[k / W], ll), lp) : -INFINITY;
+            }
+        }
+        if (S.have_smd && S.smd_hist && rec_s && srow < S.cap && T >= 2) {
+            // mean Euclidean distance of each pair's accepted swaps: one warp per swap
+            float* s_smd = reinterpret_cast<float*>(s_ratio);     // reused: [T] floats
+            for (int i = tid; i < T; i += nth) s_smd[i] = 0.f;
+            __syncthreads();
+            const int lane = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+            for (int i = 1; i < T; ++i) {
+                const int c = s_cnt[i];
+                for (int k = warp; k < c; k += nwarp) {
+                    const int2 pr = wk.pairs[i * W + k];
+                    const double* xa = S.theta + (size_t)pr.x * S.D;
+                    const double* xb = S.theta + (size_t)pr.y * S.D;
+                    float ss = 0.f;
+                    for (int d = lane; d < S.D; d += 32) {
+                        const float v = (float)(xa[d] - xb[d]);
+                        ss = fmaf(v, v, ss);
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                    if (lane == 0) atomicAdd(&s_smd[i], sqrtf(ss));
+                }
+            }
+            __syncthreads();
+            for (int i = 1 + tid; i < T; i += nth) {
+                const int c = s_cnt[i];
+                S.smd_hist[srow * (T - 1) + i - 1] = c > 0 ? (double)s_smd[i] / (double)c : 0.0;
+            }
+        }
+        __syncthreads();
+    }
     if (tid >= 32) return;
     // one warp: acceptance ratios, ladder adaptation (exponentials and
     // reciprocals across lanes, the cumulative sum as a warp scan) and the

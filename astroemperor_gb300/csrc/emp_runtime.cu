@@ -140,6 +140,10 @@ struct emp_handle {
 
 // dynamic shared memory of the staged swap kernel (static arrays use ~12 KB)
 static const size_t kSwapSmemMax = 200 * 1024;
+// history rows of one sweep up to this size are written by the swap CTA (one
+// SM writes ~20 GB/s: measured 39.6 -> 35.5 us per sweep for 2 x 100 walkers
+// (14 KB of rows), but 82 -> 107 us for 10 x 256 (512 KB))
+static const size_t kRecInSwapMax = 64 * 1024;
 // threads per CTA of the GP recursion (M lanes per walker row): one warp,
 // so that the recursion's warps spread over the SMs (measured 5 % faster
 // than four warps per CTA for 1280 rows; FP64 issue is per SM sub-partition)
@@ -361,6 +365,8 @@ int prepare_sweep(emp_handle* h, int prec) {
     if (rc) return rc;
     if (!h->swap_attr) {
         CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+        CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false, true>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
         h->swap_attr = true;
     }
@@ -678,6 +684,12 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
     S.cap = have_rec ? rec->capacity : 0;
     S.thin = have_rec ? std::max(1, rec->thin) : 1;
     S.record_chain = have_rec && (rec->chain || rec->log_like || rec->log_prob);
+    S.theta = st->theta;
+    S.logprior = st->logprior;
+    S.chain = have_rec ? rec->chain : nullptr;
+    S.log_like = have_rec ? rec->log_like : nullptr;
+    S.log_prob = have_rec ? rec->log_prob : nullptr;
+    S.smd_hist = have_rec ? rec->smd_history : nullptr;
     const size_t swap_smem = (size_t)st->ntemps * st->nwalkers * 24;
     if (batch) {
         // one CTA per system; threads cover a temperature's walkers
@@ -720,20 +732,26 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
         return EMP_OK;
     }
     const int nth = 1024;
+    // small history rows are written by the swap CTA itself (one launch less)
+    const size_t rec_bytes = (size_t)st->ntemps * st->nwalkers * (size_t)(st->ndim + 2) * 8;
+    const bool rec_in_swap = swap_smem <= kSwapSmemMax && rec_bytes <= kRecInSwapMax;
     if (swap_smem <= kSwapSmemMax) {
         if (!h->swap_attr) {
             CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
+            CUDA_TRY(cudaFuncSetAttribute((const void*)k_swap<true, false, true>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSwapSmemMax));
             h->swap_attr = true;
         }
-        CUDA_TRY(launch_pdl(k_swap<true, false>, dim3(1), dim3(nth), swap_smem, s, S));
+        if (rec_in_swap) CUDA_TRY(launch_pdl(k_swap<true, false, true>, dim3(1), dim3(nth), swap_smem, s, S));
+        else CUDA_TRY(launch_pdl(k_swap<true, false>, dim3(1), dim3(nth), swap_smem, s, S));
     } else {
         CUDA_TRY(launch_pdl(k_swap<false, false>, dim3(1), dim3(nth), (size_t)0, s, S));
     }
     g_launches.fetch_add(1);
     ++kcount;
     CUDA_TRY(cudaGetLastError());
-    if (S.record_chain || S.have_smd) {
+    if ((S.record_chain || S.have_smd) && !rec_in_swap) {
         RecArgs R{};
         R.T = st->ntemps; R.W = st->nwalkers; R.D = st->ndim;
         R.theta = st->theta; R.logl = st->logl; R.logprior = st->logprior;
