@@ -732,7 +732,11 @@ def main():
                 'kernel': 'k_gp_prep<4> + k_gp_ff<4> (celerite recursion, float-float, half-step rows)',
                 'kernel_ms': g_ms,
                 'flop_per_row_epoch': Fg,
-                'peak_source': 'FP64 peak measured on this GPU by the library FMA probe',
+                'peak_source': 'FP64 peak measured on this GPU by the library FMA probe (the '
+                               "algorithm's arithmetic is FP64-equivalent)",
+                # the float-float recursion issues FP32 instructions (about 10 per
+                # FP64-equivalent operation): the same work against the FP32 pipe
+                'fp32_pipe': {'peak': peak32, 'frac': ach / peak32},
                 'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp_ff)',
                               'kernel_ms_with_gp_kernels': k_ms, 'launch': roof['launch']}}
 
