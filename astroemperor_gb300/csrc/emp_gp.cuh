@@ -17,13 +17,14 @@
 //   logL = -0.5 sum(z_n^2 / D_n + log D_n) - 0.5 N log(2 pi).
 //
 // k_logpost writes each valid row's residuals and err2 (epoch-major) and the
-// prior; k_gp_prep evaluates, for every (row, epoch) in parallel, the parts of
-// the recursion that do not depend on its state (the sincos and exp); the
-// recursion runs with one lane per state dimension -- k_gp in FP64, k_gp_ff in
-// float-float for the mixed precision -- and finishes the mode: log-posterior
-// rows, state slots, or the stretch move's Metropolis test.  FP64 on this GPU
+// prior.  The parts of the recursion that do not depend on its state (the
+// sincos and exp) are evaluated for every (row, epoch) in parallel -- by
+// k_gp_prep for the FP64 recursion k_gp, by the producer warps of k_gp_fused
+// beside its float-float recursion for the mixed precision -- and the
+// recursion runs with one lane per state dimension and finishes the mode:
+// log-posterior rows, state slots, or the stretch move's Metropolis test.  FP64 on this GPU
 // issues one warp instruction per ~64 cycles per SM sub-partition, so the
-// transcendentals leave the sequential chain for the parallel kernel (and, in
+// transcendentals leave the sequential chain for parallel threads (and, in
 // the mixed precision, run in float-float on the FP32 pipes), the lanes share
 // a row's S, and log det needs no log per epoch.
 #pragma once
@@ -245,11 +246,11 @@ __device__ __forceinline__ FF ff_exp_neg(double y) {
     return FF{q.hi * sc, q.lo * sc};
 }
 
-// Everything of the recursion that does not depend on its state, for every
-// (row, epoch) in parallel: U_n, V_n and phi_n (one sincos and one exp per
-// component).  Thread (row, g): rows across the warp's lanes (coalesced
+// Everything of the FP64 recursion that does not depend on its state, for
+// every (row, epoch) in parallel: U_n, V_n and phi_n (one sincos and one exp
+// per component).  Thread (row, g): rows across the warp's lanes (coalesced
 // [n][rows][M] writes), epochs g, g + E, ... with E = 8 * gridDim.y.
-template <int M, bool FFO>
+template <int M>
 __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
     const int row = blockIdx.x * 32 + (threadIdx.x & 31);
     const int E = gridDim.y * 8;
@@ -281,34 +282,6 @@ __global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
     if (!finite) return;
     const double* t = A.d.t;
     const int n = A.d.n;
-    if constexpr (FFO) {
-        // float-float transcendentals and products (mixed precision)
-        FF fa[M], fb[M];
-#pragma unroll
-        for (int k = 0; k < M; ++k) { fa[k] = ff_of(ff_split_bits(pa[k])); fb[k] = ff_of(ff_split_bits(pb[k])); }
-        for (int i = g; i < n; i += E) {
-            const double ti = t[i];
-            const double dt = i > 0 ? ti - t[i - 1] : 0.0;
-            FF sn[M], cs[M], ph[M];
-            const size_t o = ((size_t)i * A.nwalk + row) * M;
-#pragma unroll
-            for (int k = 0; k < M; ++k) {
-                if (k > 0 && ps[k]) { sn[k] = sn[k - 1]; cs[k] = cs[k - 1]; ph[k] = ph[k - 1]; }
-                else {
-                    if (pd[k] != 0.0) ff_sincos(pd[k] * ti, sn[k], cs[k]);
-                    else { sn[k] = FF{0.f, 0.f}; cs[k] = FF{1.f, 0.f}; }
-                    ph[k] = pc[k] != 0.0 ? ff_exp_neg(pc[k] * dt) : FF{1.f, 0.f};
-                }
-                const FF u = ps[k] ? ff_add(ff_mul(fa[k], sn[k]), ff_neg(ff_mul(fb[k], cs[k])))
-                                   : ff_add(ff_mul(fa[k], cs[k]), ff_mul(fb[k], sn[k]));
-                const FF v = pv[k] != 0.0 ? (ps[k] ? sn[k] : cs[k]) : FF{0.f, 0.f};
-                reinterpret_cast<float2*>(A.gp_u)[o + k] = make_float2(u.hi, u.lo);
-                reinterpret_cast<float2*>(A.gp_v)[o + k] = make_float2(v.hi, v.lo);
-                reinterpret_cast<float2*>(A.gp_ph)[o + k] = make_float2(ph[k].hi, ph[k].lo);
-            }
-        }
-        return;
-    }
     for (int i = g; i < n; i += E) {
         const double ti = t[i];
         const double dt = i > 0 ? ti - t[i - 1] : 0.0;
@@ -483,7 +456,7 @@ __global__ void __launch_bounds__(128) k_gp(KArgs A) {
     gp_finish<M>(A, row, k, live, valid, lp, th, ll);
 }
 
-// FP64 residual rows of a caller to the float-float pairs of k_gp_ff
+// FP64 residual rows of a caller to the float-float pairs of k_gp_fused
 static __global__ void __launch_bounds__(256) k_gp_cvt(const double* r, const double* e, float2* ro, float2* eo,
                                                  size_t count) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
@@ -494,40 +467,146 @@ static __global__ void __launch_bounds__(256) k_gp_cvt(const double* r, const do
 }
 
 
-// The same recursion in float-float arithmetic (~2^-46 relative per
-// operation) for the mixed precision: FP32 instructions issue ~60 times as
-// fast as FP64 ones on this GPU.  Inputs are the float-float pairs of
-// k_gp_prep<M, true> and k_logpost's FP32 residuals; the sums across a row's
-// lanes are broadcast from lane 0 so that every lane holds the same D and z.
+// The mixed precision's preparation and recursion in one CTA: warps 1..3
+// compute U, V and phi (sincos and exp in float-float after an FP64 argument
+// reduction) and stage the residuals of the next chunk of kGPChunk epochs in
+// shared memory while warp 0 runs the recursion in float-float arithmetic
+// (~2^-46 relative per operation; FP32 instructions issue ~60 times as fast
+// as FP64 ones on this GPU) on the current chunk, so the U, V, phi rows never
+// go through device memory and the transcendentals stay off the recursion's
+// dependent chain.
+constexpr int kGPChunk = 16;
+constexpr int kGPProducers = 3;                   // producer warps per CTA
+
 template <int M>
-__global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
-    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int rowr = gtid / M;
-    const int k = gtid & (M - 1);
+__global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
+    constexpr int R = 32 / M;                     // rows per CTA (one warp of the recursion)
+    constexpr int E = kGPChunk;
+    __shared__ float2 sU[2][E][32], sV[2][E][32], sP[2][E][32];
+    __shared__ float2 sr[2][E][R], se[2][E][R];
+    __shared__ double s_c[R][M], s_d[R][M], s_asum[R];
+    __shared__ float2 s_a[R][M], s_b[R][M];
+    __shared__ int s_fl[R];                       // bit k: sine part, bit 8+k: live dim, bit 30: compute
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ptid = threadIdx.x - 32;            // producer thread index (warps 1..)
+    const int row0 = blockIdx.x * R;
+    const int n = A.d.n;
+    const size_t ld = (size_t)A.nwalk;
+    const int nch = (n + E - 1) / E;
+
+    // ---- producer: row constants, then the chunks ahead of the recursion
+    auto fill = [&](int c, int b) {
+        for (int task = ptid; task < E * R; task += 32 * kGPProducers) {
+            const int e = task / R, rr = task - e * R;
+            const int i = c * E + e;
+            const int row = min(row0 + rr, A.nwalk - 1);
+            const int fl = s_fl[rr];
+            const bool on = i < n && (fl >> 30 & 1);
+            if (on) {
+                const double ti = A.d.t[i];
+                const double dt = i > 0 ? ti - A.d.t[i - 1] : 0.0;
+                FF sn[M], cs[M], ph[M];
+#pragma unroll
+                for (int k = 0; k < M; ++k) {
+                    const bool ps = fl >> k & 1, pv = fl >> (8 + k) & 1;
+                    const double pc = s_c[rr][k], pd = s_d[rr][k];
+                    if (k > 0 && ps) { sn[k] = sn[k - 1]; cs[k] = cs[k - 1]; ph[k] = ph[k - 1]; }
+                    else {
+                        if (pd != 0.0) ff_sincos(pd * ti, sn[k], cs[k]);
+                        else { sn[k] = FF{0.f, 0.f}; cs[k] = FF{1.f, 0.f}; }
+                        ph[k] = pc != 0.0 ? ff_exp_neg(pc * dt) : FF{1.f, 0.f};
+                    }
+                    const FF fa = ff_of(s_a[rr][k]), fb = ff_of(s_b[rr][k]);
+                    const FF u = ps ? ff_add(ff_mul(fa, sn[k]), ff_neg(ff_mul(fb, cs[k])))
+                                    : ff_add(ff_mul(fa, cs[k]), ff_mul(fb, sn[k]));
+                    const FF v = pv ? (ps ? sn[k] : cs[k]) : FF{0.f, 0.f};
+                    sU[b][e][rr * M + k] = make_float2(u.hi, u.lo);
+                    sV[b][e][rr * M + k] = make_float2(v.hi, v.lo);
+                    sP[b][e][rr * M + k] = make_float2(ph[k].hi, ph[k].lo);
+                }
+                const size_t o = (size_t)i * ld + row;
+                sr[b][e][rr] = reinterpret_cast<const float2*>(A.gp_r)[o];
+                se[b][e][rr] = reinterpret_cast<const float2*>(A.gp_e)[o];
+            } else {
+#pragma unroll
+                for (int k = 0; k < M; ++k) {
+                    sU[b][e][rr * M + k] = make_float2(0.f, 0.f);
+                    sV[b][e][rr * M + k] = make_float2(0.f, 0.f);
+                    sP[b][e][rr * M + k] = make_float2(1.f, 0.f);
+                }
+                sr[b][e][rr] = make_float2(0.f, 0.f);
+                se[b][e][rr] = make_float2(1.f, 0.f);
+            }
+        }
+    };
+    if (warp >= 1 && ptid < R) {
+        {
+            const int lane = ptid;
+            const int rowr = row0 + lane;
+            const bool live = rowr < A.nwalk;
+            const int row = live ? rowr : A.nwalk - 1;
+            const double* th;
+            const double lp = gp_row(A, row, &th);
+            GPDim dm[M];
+#pragma unroll
+            for (int k = 0; k < M; ++k) dm[k] = GPDim{0.0, 0.0, 0.0, 0.0, 0, 0};
+            bool finite = true;
+            double asum = 0.0;
+            int fl = 0;
+            if (lp > -INFINITY) {
+                gp_fill(A.md, th, dm);
+#pragma unroll
+                for (int k = 0; k < M; ++k) {
+                    if (!dm[k].sinpart) asum += dm[k].a;
+                    finite = finite && isfinite(dm[k].a) && isfinite(dm[k].b) && isfinite(dm[k].c) &&
+                             isfinite(dm[k].d);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < M; ++k) {
+                s_c[lane][k] = dm[k].c;
+                s_d[lane][k] = dm[k].d;
+                s_a[lane][k] = ff_split_bits(dm[k].a);
+                s_b[lane][k] = ff_split_bits(dm[k].b);
+                fl |= (dm[k].sinpart ? 1 : 0) << k;
+                fl |= (dm[k].live ? 1 : 0) << (8 + k);
+            }
+            if (lp > -INFINITY && finite) fl |= 1 << 30;
+            s_fl[lane] = fl;
+            s_asum[lane] = finite ? asum : NAN;
+        }
+    }
+    __syncthreads();
+    if (warp >= 1) fill(0, 0);
+    __syncthreads();
+
+    // ---- consumer: the recursion on the staged chunks; the sums across a
+    // row's lanes are broadcast from lane 0 so that every lane holds the same
+    // D and z
+    const int k = lane & (M - 1);
+    const int rl = lane / M;
+    const int rowr = row0 + rl;
     const bool live = rowr < A.nwalk;
     const int row = live ? rowr : A.nwalk - 1;
     const emp_model_desc* md = A.md;
-    const double* th;
-    const double lp = gp_row(A, row, &th);
-    const bool valid = live && (lp > -INFINITY);
-    const double asum_d = valid ? A.gp_asum[row] : 0.0;
-    const FF asum = ff_split(isfinite(asum_d) ? asum_d : 0.0);
-    const size_t ld = (size_t)A.nwalk;
-    const int n = A.d.n;
-    const float2* Up = reinterpret_cast<const float2*>(A.gp_u) + (size_t)row * M + k;
-    const float2* Vp = reinterpret_cast<const float2*>(A.gp_v) + (size_t)row * M + k;
-    const float2* Pp = reinterpret_cast<const float2*>(A.gp_ph) + (size_t)row * M + k;
-    const float2* rp = reinterpret_cast<const float2*>(A.gp_r) + row;
-    const float2* ep = reinterpret_cast<const float2*>(A.gp_e) + row;
+    const double* th = nullptr;
+    double lp = -INFINITY;
+    bool valid = false;
+    double asum_d = 0.0;
+    FF asum{0.f, 0.f};
     FF S[M];
 #pragma unroll
     for (int j = 0; j < M; ++j) S[j] = FF{0.f, 0.f};
     FF f{0.f, 0.f}, W{0.f, 0.f}, Dp{0.f, 0.f}, zp{0.f, 0.f}, quad{0.f, 0.f}, prod{1.f, 0.f};
     int pexp = 0;
-    bool bad = !isfinite(asum_d);
-    // one epoch of the recursion (inputs: this lane's U, V, phi and the row's
-    // residual and err2); products stay unnormalised where the next operation
-    // is an addition or another product (|lo| stays within ~2 ulp of hi)
+    bool bad = false;
+    if (warp == 0) {
+        lp = gp_row(A, row, &th);
+        valid = live && (lp > -INFINITY);
+        asum_d = valid ? s_asum[rl] : 0.0;
+        asum = ff_split(isfinite(asum_d) ? asum_d : 0.0);
+        bad = !isfinite(asum_d);
+    }
     auto epoch = [&](int i, FF Uk, FF Vk, FF Pk, FF ri, FF ei) {
         FF Uj[M];
 #pragma unroll
@@ -542,7 +621,6 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
             }
             f = ff_mul(Pk, ff_add(ff_mul(W, zp), f));
         }
-        // (S U)_k as a pairwise sum
         FF t[M];
 #pragma unroll
         for (int j = 0; j < M; ++j) t[j] = ff_mul(S[j], Uj[j]);
@@ -565,7 +643,6 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
         W = ff_mul(ff_add(Vk, ff_neg(su)), iD);
         const FF z = ff_add(ri, ff_neg(p2));
         quad = ff_add(quad, ff_mul(ff_mul(z, z), iD));
-        // prod *= D, then its binary exponent moves into pexp (exact scaling)
         prod = ff_mul(prod, D);
         {
             const int ex = ((__float_as_int(prod.hi) >> 23) & 0xff) - 127;
@@ -576,34 +653,21 @@ __global__ void __launch_bounds__(128) k_gp_ff(KArgs A) {
         }
         Dp = D; zp = z;
     };
-    // the inputs of PF epochs are loaded one block ahead of their use
-    constexpr int PF = 4;
-    const float2 zero2 = make_float2(0.f, 0.f), one2 = make_float2(1.f, 0.f);
-    float2 cU[PF], cV[PF], cP[PF], cr[PF], ce[PF];
-#pragma unroll
-    for (int q = 0; q < PF; ++q) {
-        const bool ok = valid && q < n;
-        const size_t o = (size_t)q * ld;
-        cU[q] = ok ? Up[o * M] : zero2; cV[q] = ok ? Vp[o * M] : zero2; cP[q] = ok ? Pp[o * M] : one2;
-        cr[q] = ok ? rp[o] : zero2; ce[q] = ok ? ep[o] : one2;
-    }
-    for (int i0 = 0; i0 < n; i0 += PF) {
-        float2 nU[PF], nV[PF], nP[PF], nr[PF], ne[PF];
-#pragma unroll
-        for (int q = 0; q < PF; ++q) {
-            const int i = i0 + PF + q;
-            const bool ok = valid && i < n;
-            const size_t o = (size_t)i * ld;
-            nU[q] = ok ? Up[o * M] : zero2; nV[q] = ok ? Vp[o * M] : zero2; nP[q] = ok ? Pp[o * M] : one2;
-            nr[q] = ok ? rp[o] : zero2; ne[q] = ok ? ep[o] : one2;
+    for (int c = 0; c < nch; ++c) {
+        const int b = c & 1;
+        if (warp >= 1) {
+            if (c + 1 < nch) fill(c + 1, b ^ 1);
+        } else {
+            for (int e = 0; e < E; ++e) {
+                const int i = c * E + e;
+                if (i >= n) break;                            // uniform across the warp
+                epoch(i, ff_of(sU[b][e][lane]), ff_of(sV[b][e][lane]), ff_of(sP[b][e][lane]),
+                      ff_of(sr[b][e][rl]), ff_of(se[b][e][rl]));
+            }
         }
-#pragma unroll
-        for (int q = 0; q < PF; ++q)
-            if (i0 + q < n)                                    // uniform across the warp
-                epoch(i0 + q, ff_of(cU[q]), ff_of(cV[q]), ff_of(cP[q]), ff_of(cr[q]), ff_of(ce[q]));
-#pragma unroll
-        for (int q = 0; q < PF; ++q) { cU[q] = nU[q]; cV[q] = nV[q]; cP[q] = nP[q]; cr[q] = nr[q]; ce[q] = ne[q]; }
+        __syncthreads();
     }
+    if (warp != 0) return;
     double ll = -INFINITY;
     if (valid && !bad) {
         const double q = (double)quad.hi + (double)quad.lo;

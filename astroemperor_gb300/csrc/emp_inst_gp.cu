@@ -8,12 +8,13 @@ using KFn = void (*)(KArgs);
 
 template <int M>
 static KFn pick_gp(int prep, int ff) {
-    if (prep) return ff ? k_gp_prep<M, true> : k_gp_prep<M, false>;
-    return ff ? k_gp_ff<M> : k_gp<M>;
+    if (ff) return k_gp_fused<M>;
+    return prep ? k_gp_prep<M> : k_gp<M>;
 }
 
-// the recursion kernel of M state dimensions (ff != 0: float-float, for the
-// mixed precision), or (prep != 0) its parallel preparation kernel
+// FP64: the recursion kernel of M state dimensions, or (prep != 0) its
+// parallel preparation kernel; ff != 0 (mixed precision): the preparation and
+// the float-float recursion in one kernel
 KFn get_kernel_gp(int M, int prep, int ff) {
     switch (M) {
         case 2: return pick_gp<2>(prep, ff);

@@ -1202,7 +1202,7 @@ __global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 
                                 if (Q == 0) A.gp_r[gi] = (double)b;
                                 A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
                             } else {
-                                // float-float pairs for k_gp_ff
+                                // float-float pairs for k_gp_fused
                                 if (Q == 0) reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)b, 0.f);
                                 reinterpret_cast<float2*>(A.gp_e)[gi] =
                                     make_float2((float)(s_s2[ps] + insc[s_in[ps] * INSW + 1]), 0.f);

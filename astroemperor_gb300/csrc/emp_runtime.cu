@@ -561,12 +561,23 @@ void gp_args(const emp_handle* h, KArgs& a) {
     a.gp_asum = h->gp_asum;
 }
 
-// k_gp_prep (every row x epoch, about 16 warps per SM) then the recursion
-// (M lanes per row) for the rows of `a`: FP64 k_gp, or float-float k_gp_ff
-// for the mixed precision
+// The GP likelihood of the rows of `a`: k_gp_prep (every row x epoch, about
+// 16 warps per SM) then the FP64 recursion k_gp (M lanes per row), or for
+// the mixed precision k_gp_fused (both in one kernel, float-float)
 int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec) {
     const int M = h->gp_M;
     const int ff = prec == EMP_PREC_MIXED ? 1 : 0;
+    if (ff) {
+        // preparation and recursion in one kernel: a CTA per 32/M rows (one
+        // warp of the recursion, kGPProducers warps preparing its inputs)
+        KFn fused = get_kernel_gp(M, 0, 1);
+        if (!fused) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", M);
+        const int R = 32 / M;
+        fused<<<(unsigned)((a.nwalk + R - 1) / R), 32 * (1 + kGPProducers), 0, s>>>(a);
+        g_launches.fetch_add(1);
+        CUDA_TRY(cudaGetLastError());
+        return EMP_OK;
+    }
     KFn prep = get_kernel_gp(M, 1, ff), rec = get_kernel_gp(M, 0, ff);
     if (!prep || !rec) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", M);
     const int gx = (a.nwalk + 31) / 32;
@@ -655,7 +666,7 @@ int enqueue_sweep(emp_handle* h, const emp_pt_state* st, const emp_pt_record* re
                 a.a_inv_exact = frexp(st->a, &ex) == 0.5 ? 1.0 / st->a : 0.0;   // a = 2^(ex-1)
             }
             if ((rc = launch_eval(h, st->precision, a, s, batch ? work.ticket + 1 : nullptr, !batch))) return rc;
-            kcount += h->gp_M > 0 ? 3 : (h->md.am_on ? 2 : 1);
+            kcount += h->gp_M > 0 ? (st->precision == EMP_PREC_MIXED ? 2 : 3) : (h->md.am_on ? 2 : 1);
         }
     }
     if (hc) {

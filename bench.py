@@ -47,14 +47,11 @@ WORKLOADS = {
 }
 SEED = 1234
 
-# DRAM bytes (read + write) of the roofline's kernel per launch, from the ncu
-# captures summarised in profiles/ (k_logpost_mixed_c2_halfstep.md,
-# k_logpost_mixed_c3_ragged_stretch.md; for gp the k_gp_prep + k_gp_ff pair of
-# k_gp_celerite_gp_sweep.md); None where no capture was taken
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of each workload's dominant
 # kernel, from the ncu captures summarised under profiles/ (k_logpost_mixed_c2_halfstep.md,
-# k_logpost_mixed_c3_ragged_stretch.md, k_gp_celerite_gp_sweep.md, k_grad_c4_gradient_batch.md)
-NCU_TRAFFIC = {'c2': 623360, 'c3': 581037824, 'gp': 247542784, 'c4grad': 1083646568}
+# k_logpost_mixed_c3_ragged_stretch.md, k_gp_celerite_gp_sweep.md, k_grad_c4_gradient_batch.md);
+# None where no capture was taken
+NCU_TRAFFIC = {'c2': 623360, 'c3': 581037824, 'gp': 21445376, 'c4grad': 1083646568}
 
 
 def parse():
@@ -709,8 +706,8 @@ def main():
                            'has no CUDA-core figure); compute-issue bound, not HBM or tensor',
             'fp64_peak_tflops': f64p.value / 1e12}
     if any(b.type_ == 'Celerite2' for b in model.blocks):
-        # the GP sweep's dominant kernels are k_gp_prep + k_gp_ff (the mixed
-        # celerite recursion, M lanes per walker row): timed alone through
+        # the GP sweep's dominant kernel is k_gp_fused (the mixed celerite
+        # preparation and recursion, M lanes per walker row): timed alone through
         # emp_gp_logl on the half-step's rows and their residuals (with the
         # conversion of those rows to float-float pairs); the mixed k_logpost
         # that writes the residuals in a sweep is reported beside it
@@ -729,7 +726,7 @@ def main():
                 'traffic': NCU_TRAFFIC.get(args.config),
                 'traffic_source': 'ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch',
                 'algorithmic_bytes': B * (16 * n + 8 * D + 8) + 8 * n,
-                'kernel': 'k_gp_prep<4> + k_gp_ff<4> (celerite recursion, float-float, half-step rows)',
+                'kernel': 'k_gp_fused<4> (celerite preparation and float-float recursion, half-step rows)',
                 'kernel_ms': g_ms,
                 'flop_per_row_epoch': Fg,
                 'peak_source': 'FP64 peak measured on this GPU by the library FMA probe (the '
@@ -737,7 +734,7 @@ def main():
                 # the float-float recursion issues FP32 instructions (about 10 per
                 # FP64-equivalent operation): the same work against the FP32 pipe
                 'fp32_pipe': {'peak': peak32, 'frac': ach / peak32},
-                'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp_ff)',
+                'rv_kernel': {'kernel': 'k_logpost<MIXED,Q=0> (residual rows for k_gp_fused)',
                               'kernel_ms_with_gp_kernels': k_ms, 'launch': roof['launch']}}
 
     # ---- end to end through the public sampler with host buffers
