@@ -238,10 +238,11 @@ def hip21850_data(fix):
     return data, am
 
 
-def model_hip21850(fix):
+def model_hip21850(fix, k=1):
     """The notebook's model: one astrometric Keplerian, acceleration, offsets
     and jitters of four instruments, astrometric offsets and jitters, with
-    its conditions and prior arguments."""
+    its conditions and prior arguments.  k=2 adds a second astrometric
+    Keplerian (periods 20-300 d), a case for the per-planet terms."""
     from astroemperor_gb300.model import (AstrometryJitterBlock, AstrometryKeplerianBlock,
                                           AstrometryOffsetBlock)
     data, am = hip21850_data(fix)
@@ -250,6 +251,13 @@ def model_hip21850(fix):
     ss(kb, ecc_prargs=(0, 0.3))
     for j, lim in enumerate(([2000, 3000], [50, 150], [np.pi, 2 * np.pi], [0, 0.5], [0, np.pi])):
         kb[j].limits = list(lim)
+    kbs = [kb]
+    if k == 2:
+        kb2 = AstrometryKeplerianBlock(2)
+        ss(kb2, ecc_prargs=(0, 0.3))
+        for j, lim in enumerate(([20, 300], [1, 30], [0, 2 * np.pi], [0, 0.5], [0, 2 * np.pi])):
+            kb2[j].limits = list(lim)
+        kbs.append(kb2)
     ab = AccelerationBlock(1)
     ss(ab)
     ob = OffsetBlock(4)
@@ -267,10 +275,17 @@ def model_hip21850(fix):
     ss(ajb)
     ajb[0].limits, ajb[0].prior, ajb[0].prargs = [0, 10], 'Normal', [0, 5]
     ajb[1].limits, ajb[1].prior, ajb[1].prargs = [0, 10], 'Normal', [1, 0.1]
-    model = ReddModel([kb, ab, ob, jb, aob, ajb], data, am_data=am)
+    model = ReddModel(kbs + [ab, ob, jb, aob, ajb], data, am_data=am)
     return model, data, am
+
+
+# the second planet's (P, K, phase, e, w, I, Omega) around which the k=2 case draws
+HIP_K2_PLANET = [97.0, 8.0, 2.0, 0.12, 1.3, 0.9, 2.5]
 
 
 def am_case_thetas(model, n_in=24, n_near=8):
     rng = np.random.default_rng(20251204)
-    return draw_thetas(model, rng, n_in=n_in, center=np.array(HIP_MAP), n_near=n_near, spread=0.01)
+    center = np.array(HIP_MAP)
+    if model.ndim__ == len(HIP_MAP) + 7:
+        center = np.concatenate([center[:7], HIP_K2_PLANET, center[7:]])
+    return draw_thetas(model, rng, n_in=n_in, center=center, n_near=n_near, spread=0.01)

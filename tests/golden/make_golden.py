@@ -32,7 +32,8 @@ Writes
                        instrument's time-ordered subsequence
   hip21850.npz      -- the reference's HIP 21850 RV and astrometric data and the
                        Gaia dead-time tables of its support folder, as arrays
-  am_kat.npz        -- loglike_AM of the HIP 21850 model at seeded theta by the
+  am_kat.npz        -- loglike_AM of the HIP 21850 model (and, keys k2__*, of a
+                       two-planet variant) at seeded theta by the
                        reference's own generated astrometry functions
                        (ReddModel._write_model_AM text with constants.scr), and
                        the oracle's (logL, logprior) of the a00.like model, with
@@ -460,12 +461,21 @@ def am_fixture(ref_root):
     support/astrometry/constants.scr) on the data arrays of this package's
     loader; kepler.solve (absent) is the oracle's solver.  Written with the
     oracle's (logL, logprior) of the whole a00.like model:
-    tests/golden/am_kat.npz."""
+    tests/golden/am_kat.npz (the two-planet variant under keys k2__*)."""
+    from tests.golden.cases import model_hip21850
+    fix = np.load(os.path.join(HERE, 'hip21850.npz'))
+    out = {}
+    for k, pre in ((1, ''), (2, 'k2__')):
+        model, data, am = model_hip21850(fix, k)
+        out.update(_am_case(ref_root, model, data, am, pre))
+    np.savez_compressed(os.path.join(HERE, 'am_kat.npz'), **out)
+    print('am_kat:', {k: v.shape for k, v in out.items()})
+
+
+def _am_case(ref_root, model, data, am, pre):
     import types
     from oracle.rv import kepler_solve
-    from tests.golden.cases import am_case_thetas, model_hip21850
-    fix = np.load(os.path.join(HERE, 'hip21850.npz'))
-    model, data, am = model_hip21850(fix)
+    from tests.golden.cases import am_case_thetas
     src_dir = os.path.join(ref_root, 'src', 'astroemperor')
     g = {'np': np, 'kepler': types.SimpleNamespace(solve=kepler_solve)}
     exec(open(os.path.join(src_dir, 'support', 'astrometry', 'constants.scr')).read(), g)
@@ -496,9 +506,9 @@ def am_fixture(ref_root):
     ll = np.array([o.my_likelihood(t) if np.isfinite(p) else -np.inf for t, p in zip(th, lp)])
     o.am_dtype = np.longdouble
     ll_ld = np.array([o.my_likelihood(t) if np.isfinite(p) else -np.inf for t, p in zip(th, lp)])
-    np.savez_compressed(os.path.join(HERE, 'am_kat.npz'), theta=th, loglike_am_ref=ref_am, logl=ll,
-                        logl_ld=ll_ld, logprior=lp)
-    print('am_kat:', len(th), 'points;', int(np.isfinite(lp).sum()), 'inside the prior')
+    print(f'am_kat {pre or "k1"}:', len(th), 'points;', int(np.isfinite(lp).sum()), 'inside the prior')
+    return {pre + 'theta': th, pre + 'loglike_am_ref': ref_am, pre + 'logl': ll, pre + 'logl_ld': ll_ld,
+            pre + 'logprior': lp}
 
 
 if __name__ == '__main__':

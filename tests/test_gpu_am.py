@@ -40,10 +40,20 @@ def hip(lib, cuda):
     return model, data, am, Context(model, 'cuda:0')
 
 
+def _case(planets):
+    """(model, context, fixture arrays) of the one- or two-planet case"""
+    fix = np.load(os.path.join(GOLDEN, 'hip21850.npz'))
+    model, data, am = model_hip21850(fix, planets)
+    pre = '' if planets == 1 else 'k2__'
+    k = {key[len(pre):]: v for key, v in np.load(os.path.join(GOLDEN, 'am_kat.npz')).items()
+         if key.startswith(pre) and (pre or not key.startswith('k2__'))}
+    return model, Context(model, 'cuda:0'), k
+
+
+@pytest.mark.parametrize('planets', [1, 2])
 @pytest.mark.parametrize('prec,tol', [(N.EMP_PREC_FP64, 5e-10), (N.EMP_PREC_MIXED, 1e-6)])
-def test_logpost_matches_the_oracle(hip, prec, tol):
-    model, data, am, ctx = hip
-    k = np.load(os.path.join(GOLDEN, 'am_kat.npz'))
+def test_logpost_matches_the_oracle(lib, cuda, planets, prec, tol):
+    model, ctx, k = _case(planets)
     th = k['theta']
     ll, lp = ctx.logpost(torch.as_tensor(th, device='cuda:0'), precision=prec)
     torch.cuda.synchronize()
