@@ -450,14 +450,16 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
                     gE.add(tE.x + tE.y);
                 }
             }
+            // the tile's five sums accumulate across tiles as float-float pairs
+            // (FP64 instructions only in the chain rule at the end)
             const LaneAcc<EMP_PREC_MIXED>* gv[5] = {&gM, &gMt, &gA, &gB, &gE};
+            FF* ugf = reinterpret_cast<FF*>(ug);
 #pragma unroll
             for (int j = 0; j < 5; ++j) {
-                const double sj = gv[j]->template group_sum<L>(red, r);
-                if (r == 0 && valid) ug[p * 5 + j] += sj;
-                if (L <= 32) __syncwarp();
-                else __syncthreads();
+                const FF sj = gv[j]->template group_sum_ff<L>();
+                if (r == 0 && valid) ugf[p * 5 + j] = ff_add(ugf[p * 5 + j], sj);
             }
+            __syncwarp();
         }
         for (int j = 0; j < acc_order; ++j) {
             LaneAcc<EMP_PREC_MIXED> ga;
@@ -850,8 +852,11 @@ __global__ void __launch_bounds__(NT) k_grad(GArgs A) {
     __syncthreads();
     if (valid)
         for (int p = r; p < n_planets; p += L) {
-            double o[5];
-            grad_planet_chain(md->kep_param[p], full + md->kep_slot[p], ug + p * 5, o);
+            const FF* ugf = reinterpret_cast<const FF*>(ug);
+            double u5[5], o[5];
+#pragma unroll
+            for (int j = 0; j < 5; ++j) u5[j] = (double)ugf[p * 5 + j].hi + (double)ugf[p * 5 + j].lo;
+            grad_planet_chain(md->kep_param[p], full + md->kep_slot[p], u5, o);
 #pragma unroll
             for (int j = 0; j < 5; ++j) ug[p * 5 + j] = o[j];
         }

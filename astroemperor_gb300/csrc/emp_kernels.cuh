@@ -796,6 +796,23 @@ template <> struct LaneAcc<EMP_PREC_MIXED> {
         }
         return (double)h + (double)l;
     }
+    // the group total as a float-float pair (no FP64 instruction), for
+    // groups of at most one warp; every lane holds it
+    template <int L>
+    __device__ __forceinline__ FF group_sum_ff() const {
+        static_assert(L <= 32, "one warp");
+        float h = hi, l = lo;
+#pragma unroll
+        for (int o = L / 2; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, h, o, L);
+            const float ol = __shfl_xor_sync(0xffffffffu, l, o, L);
+            float s, e;
+            two_sum(h, oh, s, e);
+            h = s;
+            l = __fadd_rn(__fadd_rn(l, ol), e);
+        }
+        return FF{h, l};
+    }
 };
 
 // Mixed kernels of 128 threads are held to 5 resident CTAs per SM (at most
