@@ -482,11 +482,13 @@ template <int M>
 __global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
     constexpr int R = 32 / M;                     // rows per CTA (one warp of the recursion)
     constexpr int E = kGPChunk;
+    static_assert(M >= 2 && M <= 32, "the per-dimension bit masks hold 32 dimensions");
     __shared__ float2 sU[2][E][32], sV[2][E][32], sP[2][E][32];
     __shared__ float2 sr[2][E][R], se[2][E][R];
     __shared__ double s_c[R][M], s_d[R][M], s_asum[R];
     __shared__ float2 s_a[R][M], s_b[R][M];
-    __shared__ int s_fl[R];                       // bit k: sine part, bit 8+k: live dim, bit 30: compute
+    __shared__ unsigned s_ps[R], s_pv[R];         // bit k: dimension k is a sine part / is live
+    __shared__ int s_on[R];                       // the row's inputs are computed (else neutral)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ptid = threadIdx.x - 32;            // producer thread index (warps 1..)
     const int row0 = blockIdx.x * R;
@@ -500,15 +502,15 @@ __global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
             const int e = task / R, rr = task - e * R;
             const int i = c * E + e;
             const int row = min(row0 + rr, A.nwalk - 1);
-            const int fl = s_fl[rr];
-            const bool on = i < n && (fl >> 30 & 1);
+            const unsigned fps = s_ps[rr], fpv = s_pv[rr];
+            const bool on = i < n && s_on[rr] != 0;
             if (on) {
                 const double ti = A.d.t[i];
                 const double dt = i > 0 ? ti - A.d.t[i - 1] : 0.0;
                 FF sn[M], cs[M], ph[M];
 #pragma unroll
                 for (int k = 0; k < M; ++k) {
-                    const bool ps = fl >> k & 1, pv = fl >> (8 + k) & 1;
+                    const bool ps = fps >> k & 1u, pv = fpv >> k & 1u;
                     const double pc = s_c[rr][k], pd = s_d[rr][k];
                     if (k > 0 && ps) { sn[k] = sn[k - 1]; cs[k] = cs[k - 1]; ph[k] = ph[k - 1]; }
                     else {
@@ -552,7 +554,7 @@ __global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
             for (int k = 0; k < M; ++k) dm[k] = GPDim{0.0, 0.0, 0.0, 0.0, 0, 0};
             bool finite = true;
             double asum = 0.0;
-            int fl = 0;
+            unsigned fps = 0u, fpv = 0u;
             if (lp > -INFINITY) {
                 gp_fill(A.md, th, dm);
 #pragma unroll
@@ -568,11 +570,12 @@ __global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
                 s_d[lane][k] = dm[k].d;
                 s_a[lane][k] = ff_split_bits(dm[k].a);
                 s_b[lane][k] = ff_split_bits(dm[k].b);
-                fl |= (dm[k].sinpart ? 1 : 0) << k;
-                fl |= (dm[k].live ? 1 : 0) << (8 + k);
+                fps |= (dm[k].sinpart ? 1u : 0u) << k;
+                fpv |= (dm[k].live ? 1u : 0u) << k;
             }
-            if (lp > -INFINITY && finite) fl |= 1 << 30;
-            s_fl[lane] = fl;
+            s_ps[lane] = fps;
+            s_pv[lane] = fpv;
+            s_on[lane] = (lp > -INFINITY && finite) ? 1 : 0;
             s_asum[lane] = finite ? asum : NAN;
         }
     }

@@ -142,6 +142,20 @@ def gp_case_models(arr, n_in=12, n_near=8):
             c[j] = 0.5 * (lim[j, 0] + lim[j, 1])
         th = draw_thetas(m, rng, n_in=n_in, center=c, n_near=n_near)
         out[name] = (m, d, th)
+    # wider state vectors: two rotation terms (8 dimensions), four
+    # GonzRotation terms (16 dimensions)
+    rot = {'sigma': None, 'period': None, 'Q0': None, 'dQ': None, 'f': None}
+    grot = {'rho': None, 'tau': None, 'A1': None, 'A2': None}
+    for name, ker in (('rot_x2', {'terms': ['RotationTerm'] * 2, 'params': [dict(rot), dict(rot)]}),
+                      ('grot_x4', {'terms': ['GonzRotationTerm'] * 4, 'params': [dict(grot) for _ in range(4)]})):
+        m, d = model_51peg(arr, k=1, par=1, gp=ker)
+        free = m.free_parameters()
+        lim = m.limits_free()
+        c = np.array(PEG_MAP_P1 + [0.0] * (len(free) - len(PEG_MAP_P1)))
+        for j in range(len(PEG_MAP_P1), len(free)):
+            c[j] = 0.5 * (lim[j, 0] + lim[j, 1])
+        th = draw_thetas(m, rng, n_in=n_in, center=c, n_near=n_near)
+        out[name] = (m, d, th)
     return out
 
 
