@@ -224,6 +224,12 @@ def kat_case_models(arr):
     # of 2048 on the device)
     m, d, setup, truth = synth.build_model('c5', seed=5)
     add('c5_ma2', m, d, center=truth, spread=1e-4)
+    # MA(3): the largest order the kernels are built for, global and
+    # documented per instrument
+    m, d = model_51peg(arr, k=1, par=1, moav={'order': 3, 'global': True})
+    add('51peg_gma3', m, d, center=PEG_MAP_P1 + [0.2, 8.0, 0.1, 15.0, 0.05, 30.0])
+    m, d = model_51peg(arr, k=1, par=1, moav={'order': 3, 'global': False})
+    add('51peg_ma3_inst', m, d, center=PEG_MAP_P1 + [0.2, 8.0, 0.1, 15.0, 0.05, 30.0])
     return cases
 
 

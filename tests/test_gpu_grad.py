@@ -227,3 +227,14 @@ def test_multistart_map_finds_the_51peg_fit(peg_arr, lib, cuda):
     print('51 Peg multistart MAP: best log posterior', lp.max())
     assert lp.max() >= -881.52 - 0.01
     assert best[0] == pytest.approx(4.2308, abs=5e-4)
+
+
+def test_gradient_refuses_ma3(peg_arr, lib, cuda):
+    """The adjoint kernel is built for MA orders 0-2; an MA(3) model is
+    refused with EMP_E_UNSUPPORTED (its log-posterior runs: 51peg_gma3 is a
+    golden case of the forward kernels)."""
+    m, d, th = kat_case_models(peg_arr)['51peg_gma3']
+    ctx = Context(m, 'cuda:0')
+    with pytest.raises(N.EmpError) as e:
+        ctx.logpost_grad(torch.as_tensor(th[:4], dtype=torch.float64, device='cuda:0'))
+    assert e.value.code == N.EMP_E_UNSUPPORTED
