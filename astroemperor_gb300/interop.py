@@ -12,8 +12,9 @@ from __future__ import annotations
 import numpy as np
 
 from .data import RVData
-from .model import (AccelerationBlock, CeleriteBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock,
-                    MOAVBlock, OffsetBlock, Parameter, ReddModel, SinusoidBlock)
+from .model import (AccelerationBlock, AstrometryJitterBlock, AstrometryKeplerianBlock, AstrometryOffsetBlock,
+                    CeleriteBlock, JitterBlock, KeplerianBlock, MagneticCycleBlock, MOAVBlock, OffsetBlock,
+                    Parameter, ReddModel, SinusoidBlock)
 
 
 def data_from_frame(df, labels=None, common_t=0.0) -> RVData:
@@ -42,16 +43,27 @@ def _copy_params(src_block, dst_block):
     return dst_block
 
 
-def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False, my_kernel=None) -> ReddModel:
+def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False, my_kernel=None,
+                      am_data=None) -> ReddModel:
     """ReddModel from the reference's block list (emp_model.py:32-170 objects).
 
     A 'Celerite2' block needs the Simulation's ``my_kernel`` (the reference's
     block does not keep it; emp.py:1283-1296 builds it from ``self.my_kernel``).
+    A joint RV + astrometry model (Keplerian blocks with ``astrometry_bool``,
+    'AstrometryOffset' and 'AstrometryJitter' blocks) needs the astrometric
+    data: ``astrometry.load_am`` on the same ``datafiles/<star>/AM/`` folder
+    the reference read.
     """
     out = []
     for b in blocks:
         t = b.type_
-        if t == 'Keplerian':
+        if t == 'Keplerian' and getattr(b, 'astrometry_bool', False):
+            nb = AstrometryKeplerianBlock(int(b.number_))
+        elif t == 'AstrometryOffset':
+            nb = AstrometryOffsetBlock()
+        elif t == 'AstrometryJitter':
+            nb = AstrometryJitterBlock()
+        elif t == 'Keplerian':
             nb = KeplerianBlock(int(b.parameterisation), int(b.number_))
             extra = []
             for ap in getattr(b, 'additional_parameters', []):
@@ -92,4 +104,4 @@ def model_from_blocks(blocks, data: RVData, moav_reference_quirk=False, my_kerne
         rest = [b for b in out if b not in cos]
         k = next(i for i, b in enumerate(rest) if b.type_ == 'MOAV')
         out = rest[:k] + cos + rest[k:]
-    return ReddModel(out, data, moav_reference_quirk=moav_reference_quirk)
+    return ReddModel(out, data, moav_reference_quirk=moav_reference_quirk, am_data=am_data)

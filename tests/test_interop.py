@@ -31,6 +31,7 @@ def _ref_like(block, normalise=True):
     b.moav = block.moav
     b.is_global = block.is_global
     b.additional_parameters = extra
+    b.astrometry_bool = getattr(block, 'astrometry_bool', False)
     return b
 
 
@@ -76,3 +77,21 @@ def test_model_with_hill_from_reference_blocks(peg_arr):
     m2 = model_from_blocks([_ref_like(b) for b in m.blocks], d2)
     assert bytes(m.descriptor()) == bytes(m2.descriptor())
     assert m2.descriptor().hill_mask == (1 << 2) | (1 << 3)
+
+
+def test_model_with_astrometry_from_reference_blocks():
+    """The HIP 21850 model (tests/03_hip21850_test.ipynb) from stand-ins of the
+    reference's blocks compiles to the same descriptor and likelihood."""
+    import os
+    from tests.golden.cases import HIP_MAP, model_hip21850
+    fix = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'hip21850.npz'))
+    m, d, am = model_hip21850(fix)
+    frame = {'BJD': d.BJD, 'RV': d.RV, 'eRV': d.eRV, 'Flag': d.Flag}
+    d2 = data_from_frame(frame, labels=d.labels, common_t=d.common_t)
+    m2 = model_from_blocks([_ref_like(b) for b in m.blocks], d2, am_data=am)
+    assert bytes(m.descriptor()) == bytes(m2.descriptor())
+    o1 = OracleRV(m.spec(), dict(d.as_dict(), am=am.as_dict()))
+    o2 = OracleRV(m2.spec(), dict(d2.as_dict(), am=am.as_dict()))
+    x = np.array(HIP_MAP)
+    assert o1.my_likelihood(x) == o2.my_likelihood(x)
+    assert o1.my_prior(x) == o2.my_prior(x)
