@@ -18,6 +18,7 @@ GFn get_kernel_grad(int q, int lidx) {
         case 0: return pick_grad<0>(lidx);
         case 1: return pick_grad<1>(lidx);
         case 2: return pick_grad<2>(lidx);
+        case 3: return pick_grad<3>(lidx);
         default: return nullptr;
     }
 }

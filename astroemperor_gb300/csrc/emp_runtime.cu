@@ -124,6 +124,7 @@ struct emp_handle {
     // adjoint kernel: epoch tile (0: chosen per call) and the residual buffer
     // of MA models whose series spans several tiles (grown on demand)
     int grad_tile = 0;
+    bool grad_attr[4] = {};      // the adjoint kernel's shared-memory limit set, by MA order
     void* grad_buf = nullptr;
     size_t grad_bytes = 0;
     // joint astrometry (md.am_on): the data on the device, and per walker
@@ -1247,7 +1248,7 @@ int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, do
     const emp_model_desc& m = h->md;
     if (m.n_ins > kGradMaxIns)
         return fail(EMP_E_UNSUPPORTED, "gradient: %d instruments (at most %d)", m.n_ins, kGradMaxIns);
-    if (h->q > 2) return fail(EMP_E_UNSUPPORTED, "gradient: MA order %d (at most 2)", h->q);
+    if (h->q > 3) return fail(EMP_E_UNSUPPORTED, "gradient: MA order %d (at most 3)", h->q);
     constexpr int L = 32, NT = 128, G = NT / L;
     const int n = h->n;
     // the epoch tile: the caller's, else the series rounded up to 32 lanes,
@@ -1284,10 +1285,9 @@ int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl, do
     }
     GFn fn = get_kernel_grad(h->q, 0);
     if (!fn) return fail(EMP_E_UNSUPPORTED, "no gradient kernel for q=%d", h->q);
-    static bool attr[3] = {};
-    if (!attr[h->q]) {
+    if (!h->grad_attr[h->q]) {
         CUDA_TRY(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-        attr[h->q] = true;
+        h->grad_attr[h->q] = true;
     }
     GArgs a{};
     a.md = h->md_dev;

@@ -246,7 +246,7 @@ int emp_logpost(emp_handle* h, const double* theta, int B,
    free parameters.  Planet constants in float-float from FP64, FP32
    per-epoch forward and adjoint terms, float-float sums finished in FP64.
    Every Keplerian parameterisation (kep00-kep07.model), sinusoid and
-   magnetic-cycle terms, acceleration, up to 4 instruments, MA order <= 2,
+   magnetic-cycle terms, acceleration, up to 4 instruments, MA order <= 3,
    any number of epochs (streamed in tiles).  With MA and a series longer
    than one tile the handle keeps a residual buffer of B * epochs floats,
    allocated by the first call that needs more (make that call outside any

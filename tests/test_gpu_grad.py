@@ -35,7 +35,8 @@ COND_TOL = 5e-7
 COND_TOL_MA = 5e-6
 CASES = ['51peg_k0', '51peg_k1_p0', '51peg_k1_p1', '51peg_k1_p2', '51peg_k1_p3', '51peg_k1_p4',
          '51peg_k1_p6', '51peg_k1_p7', '51peg_fixed_acc', '51peg_gma2', '51peg_k1_sin',
-         '51peg_k1_cycle_gma1', '51peg_k2_hill', '51peg_ma2_inst', 'c2_ma1', 'c2_ma1_quirk']
+         '51peg_k1_cycle_gma1', '51peg_k2_hill', '51peg_ma2_inst', 'c2_ma1', 'c2_ma1_quirk',
+         '51peg_gma3', '51peg_ma3_inst']
 
 
 def _rel_err(g, ref):
@@ -228,13 +229,3 @@ def test_multistart_map_finds_the_51peg_fit(peg_arr, lib, cuda):
     assert lp.max() >= -881.52 - 0.01
     assert best[0] == pytest.approx(4.2308, abs=5e-4)
 
-
-def test_gradient_refuses_ma3(peg_arr, lib, cuda):
-    """The adjoint kernel is built for MA orders 0-2; an MA(3) model is
-    refused with EMP_E_UNSUPPORTED (its log-posterior runs: 51peg_gma3 is a
-    golden case of the forward kernels)."""
-    m, d, th = kat_case_models(peg_arr)['51peg_gma3']
-    ctx = Context(m, 'cuda:0')
-    with pytest.raises(N.EmpError) as e:
-        ctx.logpost_grad(torch.as_tensor(th[:4], dtype=torch.float64, device='cuda:0'))
-    assert e.value.code == N.EMP_E_UNSUPPORTED
