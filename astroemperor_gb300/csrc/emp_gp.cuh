@@ -483,6 +483,7 @@ __global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
     constexpr int R = 32 / M;                     // rows per CTA (one warp of the recursion)
     constexpr int E = kGPChunk;
     static_assert(M >= 2 && M <= 32, "the per-dimension bit masks hold 32 dimensions");
+    static_assert((M & (M - 1)) == 0, "a row's lanes are lane & (M - 1)");
     __shared__ float2 sU[2][E][32], sV[2][E][32], sP[2][E][32];
     __shared__ float2 sr[2][E][R], se[2][E][R];
     __shared__ double s_c[R][M], s_d[R][M], s_asum[R];
