@@ -131,6 +131,47 @@ __device__ inline double gp_row(const KArgs& A, int row, const double** th) {
     return A.gp_meta[row].lp;
 }
 
+// System s of a batch handle seen as a one-system launch: its model, its
+// series and every row array from that system's first element on (a
+// one-system launch comes back unchanged).  Epoch-major arrays hold all
+// systems' epochs ([epochs][rows]), row arrays [systems][rows].  In stretch
+// mode the proposals carry the batch's own slot numbers, so the slot arrays
+// stay whole and the temperatures and acceptance counts move instead.
+template <int M>
+__device__ __forceinline__ KArgs gp_system(const KArgs& B, int s) {
+    KArgs A = B;
+    if (B.sys_off == nullptr) return A;
+    const int64_t e0 = B.sys_off[s];
+    const size_t rows = (size_t)B.nwalk, ds = (size_t)B.dstride;
+    const size_t ep = (size_t)e0 * rows, so = (size_t)s * rows;
+    A.md = B.md + s;
+    A.d.t = B.d.t + e0;
+    A.d.n = (int)(B.sys_off[s + 1] - e0);
+    A.gp_r = B.gp_r + ep;
+    A.gp_e = B.gp_e + ep;
+    A.gp_u = B.gp_u + ep * M;
+    A.gp_v = B.gp_v + ep * M;
+    A.gp_ph = B.gp_ph + ep * M;
+    A.gp_asum = B.gp_asum + so;
+    A.gp_meta = B.gp_meta + so;
+    A.gp_prop = B.gp_prop + so * ds;
+    if (B.mode == kModeLogpost) {
+        A.theta = B.theta + so * ds;
+        A.logprior = B.logprior + so;
+        A.logl = B.logl + so;
+        if (B.logp != nullptr) A.logp = B.logp + so;
+        if (B.beta != nullptr) A.beta = B.beta + so;
+    } else if (B.mode == kModeSlots) {
+        A.st_theta = B.st_theta + so * ds;
+        A.st_logprior = B.st_logprior + so;
+        A.st_logl = B.st_logl + so;
+    } else if (B.mode == kModeStretch) {
+        A.betas = B.betas + (size_t)s * B.T;
+        A.accepted = B.accepted + (size_t)s * B.T * B.W;
+    }
+    return A;
+}
+
 // x as a float-float pair by bit manipulation (integer and FP32 instructions
 // only; a double-to-float conversion would take the FP64 pipe): hi = x
 // truncated to 24 significant bits, lo = the remaining 29 bits rounded to a
@@ -251,7 +292,8 @@ __device__ __forceinline__ FF ff_exp_neg(double y) {
 // per component).  Thread (row, g): rows across the warp's lanes (coalesced
 // [n][rows][M] writes), epochs g, g + E, ... with E = 8 * gridDim.y.
 template <int M>
-__global__ void __launch_bounds__(256) k_gp_prep(KArgs A) {
+__global__ void __launch_bounds__(256) k_gp_prep(KArgs A0) {
+    const KArgs A = gp_system<M>(A0, blockIdx.z);
     const int row = blockIdx.x * 32 + (threadIdx.x & 31);
     const int E = gridDim.y * 8;
     const int g = blockIdx.y * 8 + (threadIdx.x >> 5);
@@ -356,7 +398,8 @@ __device__ __forceinline__ void gp_finish(const KArgs& A, int row, int k, bool l
 // prior compute on unwritten residuals and are discarded), which keeps the
 // shuffles convergent.
 template <int M>
-__global__ void __launch_bounds__(128) k_gp(KArgs A) {
+__global__ void __launch_bounds__(128) k_gp(KArgs A0) {
+    const KArgs A = gp_system<M>(A0, blockIdx.y);
     const unsigned FULL = 0xffffffffu;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
     const int rowr = gtid / M;
@@ -479,7 +522,8 @@ constexpr int kGPChunk = 16;
 constexpr int kGPProducers = 3;                   // producer warps per CTA
 
 template <int M>
-__global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A) {
+__global__ void __launch_bounds__(32 * (1 + kGPProducers)) k_gp_fused(KArgs A0) {
+    const KArgs A = gp_system<M>(A0, blockIdx.y);
     constexpr int R = 32 / M;                     // rows per CTA (one warp of the recursion)
     constexpr int E = kGPChunk;
     static_assert(M >= 2 && M <= 32, "the per-dimension bit masks hold 32 dimensions");

@@ -1214,7 +1214,7 @@ __global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 
                         if constexpr (GPW) {
                             // GP likelihood: hand the residual and err2 to k_gp
                             // (with MA the residual follows the recurrence, below)
-                            const size_t gi = (size_t)(base + r * C + k0 + e) * A.nwalk + wk;
+                            const size_t gi = (size_t)(e0 + base + r * C + k0 + e) * A.nwalk + wk;
                             if constexpr (PREC == EMP_PREC_FP64) {
                                 if (Q == 0) A.gp_r[gi] = (double)b;
                                 A.gp_e[gi] = (double)(s_s2[ps] + insc[s_in[ps] * INSW + 1]);
@@ -1346,7 +1346,7 @@ __global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 
                     R rr = gmx[ps];
 #pragma unroll
                     for (int q2 = 0; q2 < NQ; ++q2) rr += gmg[q2 * tile + ps] * u[q2];
-                    const size_t gi = (size_t)(base + r * C + k) * A.nwalk + wk;
+                    const size_t gi = (size_t)(e0 + base + r * C + k) * A.nwalk + wk;
                     if constexpr (PREC == EMP_PREC_FP64) A.gp_r[gi] = (double)rr;
                     else reinterpret_cast<float2*>(A.gp_r)[gi] = make_float2((float)rr, 0.f);
                 }
@@ -1372,11 +1372,11 @@ __global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 
                 GPMeta m;
                 m.lp = lp; m.z = z; m.uword = uword; m.slot = slot_j;
                 m.pos = t_idx * A.W + j_idx; m.t = t_idx;
-                A.gp_meta[wk] = m;
+                A.gp_meta[(size_t)sys * A.nwalk + wk] = m;     // rows [S][nwalk]
             }
         }
         if (active && A.mode == kModeStretch) {
-            double* dst = A.gp_prop + (size_t)wk * ds;
+            double* dst = A.gp_prop + ((size_t)sys * A.nwalk + wk) * ds;
             for (int d = r; d < n_free; d += L) dst[d] = thp[d];
         }
     } else if (A.am_rv != nullptr && A.mode == kModeStretch) {

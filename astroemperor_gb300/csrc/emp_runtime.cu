@@ -506,19 +506,21 @@ int am_reserve(emp_handle* h, int64_t rows) {
     return EMP_OK;
 }
 
-// GP row buffers for launches of up to `rows` walker rows; allocated (or
-// grown) outside any stream capture, before the launches that use them.  A
-// captured sweep graph refers to the old buffers, so growing drops it.
+// GP row buffers for launches of up to `rows` walker rows per system;
+// allocated (or grown) outside any stream capture, before the launches that
+// use them.  A captured sweep graph refers to the old buffers, so growing
+// drops it.  Epoch-major arrays are [all systems' epochs][rows] (system s
+// from its first epoch on), row arrays [systems][rows].
 int gp_reserve(emp_handle* h, int64_t rows) {
     if (h->gp_M == 0 || rows <= h->gp_rows) return EMP_OK;
-    const size_t n = (size_t)h->n, D = (size_t)std::max(h->lay[1], 1);
+    const size_t n = (size_t)h->dd.n, D = (size_t)std::max(h->lay[1], 1), S = (size_t)h->n_sys;
     const size_t al = 256;
     auto up = [al](size_t b) { return (b + al - 1) & ~(al - 1); };
     const size_t b_re = up(8 * n * (size_t)rows);
-    const size_t b_prop = up(8 * D * (size_t)rows);
-    const size_t b_meta = up(sizeof(GPMeta) * (size_t)rows);
+    const size_t b_prop = up(8 * D * (size_t)rows * S);
+    const size_t b_meta = up(sizeof(GPMeta) * (size_t)rows * S);
     const size_t b_uvp = up(8 * n * (size_t)rows * (size_t)h->gp_M);
-    const size_t b_asum = up(8 * (size_t)rows);
+    const size_t b_asum = up(8 * (size_t)rows * S);
     const size_t total = 2 * b_re + b_prop + b_meta + 3 * b_uvp + b_asum;
     if (total > ((size_t)64 << 30))
         return fail(EMP_E_SIZE, "GP workspace of %zu B for %lld rows exceeds 64 GiB", total, (long long)rows);
@@ -564,7 +566,8 @@ void gp_args(const emp_handle* h, KArgs& a) {
 
 // The GP likelihood of the rows of `a`: k_gp_prep (every row x epoch, about
 // 16 warps per SM) then the FP64 recursion k_gp (M lanes per row), or for
-// the mixed precision k_gp_fused (both in one kernel, float-float)
+// the mixed precision k_gp_fused (both in one kernel, float-float); the
+// last grid dimension is the system of a batch handle
 int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec) {
     const int M = h->gp_M;
     const int ff = prec == EMP_PREC_MIXED ? 1 : 0;
@@ -574,7 +577,7 @@ int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec) {
         KFn fused = get_kernel_gp(M, 0, 1);
         if (!fused) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", M);
         const int R = 32 / M;
-        fused<<<(unsigned)((a.nwalk + R - 1) / R), 32 * (1 + kGPProducers), 0, s>>>(a);
+        fused<<<dim3((unsigned)((a.nwalk + R - 1) / R), (unsigned)h->n_sys), 32 * (1 + kGPProducers), 0, s>>>(a);
         g_launches.fetch_add(1);
         CUDA_TRY(cudaGetLastError());
         return EMP_OK;
@@ -583,12 +586,13 @@ int launch_gp(emp_handle* h, KArgs& a, cudaStream_t s, int prec) {
     if (!prep || !rec) return fail(EMP_E_UNSUPPORTED, "no GP kernel for %d state dimensions", M);
     const int gx = (a.nwalk + 31) / 32;
     const int want_warps = std::max(1, h->sms) * 16;
-    const int gy = std::max(1, std::min((h->n + 7) / 8, (want_warps + 8 * gx - 1) / (8 * gx)));
-    prep<<<dim3(gx, gy), 256, 0, s>>>(a);
+    const int64_t per_y = 8 * (int64_t)gx * h->n_sys;
+    const int gy = (int)std::max<int64_t>(1, std::min<int64_t>((h->n + 7) / 8, (want_warps + per_y - 1) / per_y));
+    prep<<<dim3(gx, gy, (unsigned)h->n_sys), 256, 0, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
     const int64_t threads = (int64_t)a.nwalk * M;
-    rec<<<(unsigned)((threads + kGPBlock - 1) / kGPBlock), kGPBlock, 0, s>>>(a);
+    rec<<<dim3((unsigned)((threads + kGPBlock - 1) / kGPBlock), (unsigned)h->n_sys), kGPBlock, 0, s>>>(a);
     g_launches.fetch_add(1);
     CUDA_TRY(cudaGetLastError());
     return EMP_OK;
@@ -919,8 +923,6 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
             return fail(EMP_E_UNSUPPORTED, "system %d: MA order %d differs from system 0's %d", s,
                         ma_order_on_device(m), q);
         if ((rc = check_system(m, data, s, &nsys[s]))) return rc;
-        if (S > 1 && m->gp_nterms > 0)
-            return fail(EMP_E_UNSUPPORTED, "system %d: GP likelihoods take a one-system handle", s);
         if (S > 1 && m->am_on)
             return fail(EMP_E_UNSUPPORTED, "system %d: astrometric likelihoods take a one-system handle", s);
         total += nsys[s];
@@ -961,6 +963,26 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
     std::vector<int64_t> sorted_n(nsys);
     std::sort(sorted_n.begin(), sorted_n.end());
 
+    // one GP state dimension for every system of a batch: the largest, as a
+    // power of two (a system's unused dimensions stay zero and add nothing;
+    // a system without GP terms then has the Gaussian likelihood)
+    int gp_M = 0;
+    {
+        int dims = 0;
+        bool any = false;
+        for (int s = 0; s < S; ++s) {
+            int d = 0;
+            for (int j = 0; j < models[s].gp_nterms; ++j) d += gp_term_dims(models[s].gp_kind[j]);
+            dims = std::max(dims, d);
+            any = any || models[s].gp_nterms > 0;
+        }
+        if (any) {
+            gp_M = 2;
+            while (gp_M < dims) gp_M <<= 1;
+            if (S > 65535) return fail(EMP_E_SIZE, "%d systems with GP likelihoods (at most 65535)", S);
+        }
+    }
+
     emp_handle* h = new (std::nothrow) emp_handle();
     if (!h) return fail(EMP_E_INVALID, "out of host memory");
     h->md = models[0];
@@ -969,12 +991,7 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
     h->n_sys = S;
     for (int k = 0; k < 5; ++k) h->lay[k] = lay[k];
     h->q = q;
-    if (models[0].gp_nterms > 0) {
-        int dims = 0;
-        for (int j = 0; j < models[0].gp_nterms; ++j) dims += gp_term_dims(models[0].gp_kind[j]);
-        h->gp_M = 2;
-        while (h->gp_M < dims) h->gp_M <<= 1;
-    }
+    if (gp_M > 0) h->gp_M = gp_M;
 
     // one device allocation for the dataset, descriptors and system tables
     size_t bytes = 0;
@@ -1205,6 +1222,7 @@ int emp_gp_logl(emp_handle* h, const double* theta, int B, const double* resid, 
     if (precision != EMP_PREC_FP64 && precision != EMP_PREC_MIXED)
         return fail(EMP_E_INVALID, "precision %d unknown", precision);
     if (h->gp_M == 0) return fail(EMP_E_UNSUPPORTED, "the handle's model has no GP");
+    if (h->n_sys > 1) return fail(EMP_E_UNSUPPORTED, "emp_gp_logl takes a one-system handle");
     if (B < 0) return fail(EMP_E_INVALID, "B=%d < 0", B);
     if (B == 0) return EMP_OK;
     if (!theta || !resid || !err2 || !logl) return fail(EMP_E_INVALID, "a NULL argument");

@@ -217,7 +217,12 @@ int emp_destroy(emp_handle* h);
    counter), swaps run one CTA per system, and the record keeps each
    system's cold chain (emp_pt_record.chain [rows][S][W][ndim], log_like /
    log_prob [rows][S][W], beta_history [rows][S][T], tsw_history
-   [rows][S][T-1]; smd_history unused). */
+   [rows][S][T-1]; smd_history unused).  Systems may carry Celerite2 GP
+   likelihoods (at most 65535 systems then): the GP kernels run every
+   system with the largest state dimension of the batch, as a power of two
+   (a system's unused dimensions stay zero; a system without GP terms then
+   gets the Gaussian likelihood through the same recursion).  Astrometric
+   models take a one-system handle (EMP_E_UNSUPPORTED). */
 int emp_create_batch(const emp_model_desc* models, const emp_dataset_desc* data,
                      emp_handle** out);
 int emp_num_systems(emp_handle* h);
@@ -277,7 +282,7 @@ int emp_model_eval(emp_handle* h, const double* theta, int B, double* model,
    order); logl [B].  Semiseparable recursion with M lanes per row, in FP64
    (EMP_PREC_FP64) or float-float (EMP_PREC_MIXED, the residuals converted
    first); logl = -inf where the covariance is not positive definite.
-   EMP_E_UNSUPPORTED for a handle without a GP.  Uses (and on first need
+   EMP_E_UNSUPPORTED for a handle without a GP or a batch handle.  Uses (and on first need
    allocates) the handle's GP row workspace, as emp_logpost does.  The
    log-posterior entries compute the residuals themselves; this one serves
    callers with their own mean model. */

@@ -272,9 +272,10 @@ def test_create_rejects_bad_gp_and_hill_fields(lib, peg_arr):
     assert rc == N.EMP_E_UNSUPPORTED and 'Hill' in msg
 
 
-def test_gp_batch_rejected_before_touching_the_gpu(lib, peg_arr):
-    from tests.golden.cases import GP_KERNELS, model_51peg
-    m, d = model_51peg(peg_arr, k=1, par=1, gp=GP_KERNELS['grot'])
+def test_astrometry_batch_rejected_before_touching_the_gpu(lib):
+    from tests.golden.cases import model_hip21850
+    fix = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'hip21850.npz'))
+    m, d, _ = model_hip21850(fix)
     parts = [(d.BJD, d.RV, d.eRV, d.Flag)] * 2
     rc, msg = _batch(lib, [m, m], parts)
     assert rc == N.EMP_E_UNSUPPORTED and 'one-system' in msg

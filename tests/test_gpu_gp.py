@@ -182,9 +182,14 @@ def test_gp_unsupported_paths(peg_arr, lib, cuda):
     r = torch.zeros(2, m0.data.ndata, dtype=torch.float64, device='cuda:0')
     with pytest.raises(N.EmpError, match='no GP'):
         ctx0.gp_logl(t0, r, r + 1.0)
+    # a batch handle takes GP models, but not the residual-row entry
     from astroemperor_gb300.batch import BatchContext
+    bctx = BatchContext([m, m], 'cuda:0')
+    rb = torch.zeros(2, m.data.ndata, dtype=torch.float64, device='cuda:0')
+    out = torch.empty(2, dtype=torch.float64, device='cuda:0')
     with pytest.raises(N.EmpError, match='one-system'):
-        BatchContext([m, m], 'cuda:0')
+        N.call('emp_gp_logl', bctx.h, t.data_ptr(), 2, rb.data_ptr(), (rb + 1.0).data_ptr(), out.data_ptr(),
+               int(N.EMP_PREC_FP64), None)
 
 
 def test_gp_with_quirk_moav_on_device(peg_arr, lib, cuda):
