@@ -188,59 +188,73 @@ __global__ void __launch_bounds__(1024) k_swap(SwapArgs S) {
     }
     __syncthreads();
 
-    for (int i = T - 1; i >= 1; --i) {
-        const uint32_t m = s_perm[i][0];
-        const uint32_t b = s_perm[i][1];
-        const float dbf = s_dbf[i];
+    // one exchange log entry per accepted pair, consecutive slots per warp
+    // (one shared-memory atomic per warp and temperature pair)
+    auto log_pair = [&](int i, bool acc, int sa, int sb) {
+        const unsigned act = __activemask();
+        const unsigned am = __ballot_sync(act, acc);
+        const int lane = tid & 31;
+        const int leader = __ffs(act) - 1;
+        int base = 0;
+        if (lane == leader && am != 0u) base = atomicAdd(&s_cnt[i], __popc(am));
+        base = __shfl_sync(act, base, leader);
+        if (acc && !BATCH) {
+            const int k = base + __popc(am & ((1u << lane) - 1u));
+            wk.pairs[i * W + k] = make_int2(sa, sb);
+        }
+    };
+    if (SMEM) {
+        // Pair i (hottest first) exchanges position (i, x) with (i-1, perm_i(x)),
+        // and pair i-1 then takes (i-1, perm_i(x)) as its upper position: each
+        // thread follows one such chain x -> perm_i(x) from the hottest pair
+        // down.  Every position is the upper (lower) side of exactly one chain
+        // at each pair and no other chain reads it, so the chains need no
+        // barrier and take the decisions of the sequential pair order.
         for (int j = tid; j < W; j += nth) {
-            // W <= 65535, so m * j + b < 2^32
-            const int jp = (int)(((uint32_t)m * (uint32_t)j + b) % (uint32_t)W);
-            const int ia = i * W + j, ib = (i - 1) * W + jp;
-            int sa, sb;
-            bool acc;
-            if (SMEM) {
-                sa = s_mem[ia]; sb = s_mem[ib];
+            int x = j;
+            for (int i = T - 1; i >= 1; --i) {
+                // W <= 65535, so m * x + b < 2^32
+                const int jp = (int)(((uint32_t)s_perm[i][0] * (uint32_t)x + s_perm[i][1]) % (uint32_t)W);
+                const int ia = i * W + x, ib = (i - 1) * W + jp;
+                const int sa = s_mem[ia], sb = s_mem[ib];
                 // log u < dbeta (la - lb), decided in FP32 outside a guard
                 // band that bounds the FP32 errors, else in FP64
+                const float dbf = s_dbf[i];
                 const float lfa = s_lf[ia], lfb = s_lf[ib], lu = s_lu[ia];
                 const float xf = dbf * (lfa - lfb);
                 const float dd = xf - lu;
                 const float guard = 1e-4f * (1.f + fabsf(lu)) +
                                     2.5e-7f * fabsf(dbf) * (fabsf(lfa) + fabsf(lfb)) + 1e-6f * fabsf(xf);
+                bool acc;
                 if (dd > guard) acc = true;
                 else if (dd < -guard) acc = false;
                 else acc = log(u32u(s_u[ia])) < (s_bused[i - 1] - s_bused[i]) * (s_ll[ia] - s_ll[ib]);
-            } else {
-                sa = members[ia]; sb = members[ib];
-                const double paccept = (s_bused[i - 1] - s_bused[i]) * (S.logl[sa] - S.logl[sb]);
-                acc = log_uniform_below(rng_draw(seed, (uint32_t)ia, sweep, kRngSwapAcc).x, paccept);
-            }
-            if (acc) {
-                if (SMEM) {
+                if (acc) {
                     s_mem[ia] = sb; s_mem[ib] = sa;
                     const double la = s_ll[ia];
                     s_ll[ia] = s_ll[ib]; s_ll[ib] = la;
-                    const float lf = s_lf[ia];
-                    s_lf[ia] = s_lf[ib]; s_lf[ib] = lf;
-                } else {
-                    members[ia] = sb; members[ib] = sa;
+                    s_lf[ia] = lfb; s_lf[ib] = lfa;
                 }
-            }
-            // one shared-memory atomic per warp: the warp's accepted
-            // exchanges take consecutive slots of the pair log
-            const unsigned act = __activemask();
-            const unsigned am = __ballot_sync(act, acc);
-            const int lane = tid & 31;
-            const int leader = __ffs(act) - 1;
-            int base = 0;
-            if (lane == leader && am != 0u) base = atomicAdd(&s_cnt[i], __popc(am));
-            base = __shfl_sync(act, base, leader);
-            if (acc && !BATCH) {
-                const int k = base + __popc(am & ((1u << lane) - 1u));
-                wk.pairs[i * W + k] = make_int2(sa, sb);
+                log_pair(i, acc, sa, sb);
+                x = jp;
             }
         }
         __syncthreads();
+    } else {
+        for (int i = T - 1; i >= 1; --i) {
+            const uint32_t m = s_perm[i][0];
+            const uint32_t b = s_perm[i][1];
+            for (int j = tid; j < W; j += nth) {
+                const int jp = (int)(((uint32_t)m * (uint32_t)j + b) % (uint32_t)W);
+                const int ia = i * W + j, ib = (i - 1) * W + jp;
+                const int sa = members[ia], sb = members[ib];
+                const double paccept = (s_bused[i - 1] - s_bused[i]) * (S.logl[sa] - S.logl[sb]);
+                const bool acc = log_uniform_below(rng_draw(seed, (uint32_t)ia, sweep, kRngSwapAcc).x, paccept);
+                if (acc) { members[ia] = sb; members[ib] = sa; }
+                log_pair(i, acc, sa, sb);
+            }
+            __syncthreads();
+        }
     }
     if (SMEM)
         for (int k = tid; k < TW; k += nth) members[k] = s_mem[k];
