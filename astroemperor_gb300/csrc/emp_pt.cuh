@@ -116,7 +116,8 @@ __device__ __forceinline__ bool log_uniform_below(uint32_t word, double x) {
 // One CTA per system.  With SMEM the positions of every temperature (slot,
 // logL) are staged in shared memory and all random words are drawn up front
 // by every thread; the temperature pairs are then visited from the hottest
-// down with one barrier between pairs.  For one system, accepted exchanges
+// down, each thread along one chain of positions (no barrier between pairs;
+// without SMEM, one barrier per pair).  For one system, accepted exchanges
 // are logged for the swap distance (computed across the GPU by the record
 // kernel) and the sweep counters advance here; for a batch (BATCH), system
 // s = blockIdx.x works on its own [T][W] block of every array with key
