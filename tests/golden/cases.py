@@ -230,7 +230,64 @@ def kat_case_models(arr):
     add('51peg_gma3', m, d, center=PEG_MAP_P1 + [0.2, 8.0, 0.1, 15.0, 0.05, 30.0])
     m, d = model_51peg(arr, k=1, par=1, moav={'order': 3, 'global': False})
     add('51peg_ma3_inst', m, d, center=PEG_MAP_P1 + [0.2, 8.0, 0.1, 15.0, 0.05, 30.0])
+    # real multi-instrument cadence: GJ 876 (eight instruments), two
+    # Keplerians; plain, the documented per-instrument MA(1) and the
+    # reference's per-instrument MA (a no-op there)
+    for name, moav, quirk in (('gj876_k2', None, False),
+                              ('gj876_k2_ma1_inst', {'order': 1, 'global': False}, False),
+                              ('gj876_k2_ma1_quirk', {'order': 1, 'global': False}, True)):
+        m, d = model_gj876(moav=moav, quirk=quirk)
+        add(name, m, d, center=gj876_centre(m))
     return cases
+
+
+def gj876_data():
+    """RVData of the GJ 876 fixture (tests/golden/gj876_rv.npz)."""
+    import os
+    fix = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'gj876_rv.npz'))
+    names = [str(n) for n in fix['names']]
+    return preprocess_instruments([fix[f'ins_{k}'] for k in range(len(names))], names)
+
+
+def model_gj876(moav=None, quirk=False):
+    """Two parameterisation-1 Keplerians (periods 55-65 d and 28-32 d), an
+    offset and a jitter per instrument, optionally per-instrument MA(1)."""
+    data = gj876_data()
+    ss = SmartSetter(data)
+    blocks = []
+    for number, plim, klim in ((1, [55.0, 65.0], [150.0, 260.0]), (2, [28.0, 32.0], [40.0, 120.0])):
+        kb = _kep(ss, 1, number)
+        kb[0].limits = plim
+        kb[1].limits = klim
+        blocks.append(kb)
+    ob = OffsetBlock(data.nins)
+    ss(ob)
+    blocks.append(ob)
+    jb = JitterBlock(data.nins)
+    ss(jb, jit_prargs=(5, 5))
+    blocks.append(jb)
+    if moav:
+        mb = MOAVBlock(data.nins, moav)
+        ss(mb)
+        blocks.append(mb)
+    return ReddModel(blocks, data, moav_reference_quirk=quirk), data
+
+
+# a two-Keplerian maximum of the log posterior of model_gj876() (no MA),
+# found with the oracle by Nelder-Mead from a phase grid: P, K, phase,
+# sqrt(e) sin w, sqrt(e) cos w of each planet, then the eight offsets and
+# the eight jitters (the two inner planets are not modelled, hence ~15 m/s)
+GJ876_FIT = [61.0337, 211.906, 6.20890, -3.59882e-04, 9.51621e-04,
+             30.2266, 86.9011, 6.28312, 0.0838683, -0.162759,
+             -35.6556, 15.2604, 10.6571, 12.8218, 15.8653, 17.5366, 19.7600, -19.8340,
+             0.0590557, 14.7155, 14.8289, 15.0750, 15.9099, 15.8155, 13.8305, 14.6368]
+
+
+def gj876_centre(m):
+    """GJ876_FIT, with MA coefficients 0.1 and timescales 5 d, clipped to the limits."""
+    lim = m.limits_free()
+    c = np.array(GJ876_FIT + [0.1, 5.0] * ((len(lim) - len(GJ876_FIT)) // 2))
+    return np.clip(c, lim[:, 0], lim[:, 1])
 
 
 # ---------------------------------------------------------------------------

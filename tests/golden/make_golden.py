@@ -30,6 +30,9 @@ Writes
                        own per-instrument template does not compute) is pinned
                        to its live global template moav01.model run on each
                        instrument's time-ordered subsequence
+  gj876_rv.npz      -- the reference's tests/datafiles/GJ876/RV/*.vels (eight
+                       instruments; BJD, RV, eRV columns of each, the files in
+                       the sorted order the reference reads them)
   hip21850.npz      -- the reference's HIP 21850 RV and astrometric data and the
                        Gaia dead-time tables of its support folder, as arrays
   am_kat.npz        -- loglike_AM of the HIP 21850 model (and, keys k2__*, of a
@@ -62,6 +65,7 @@ def main(ref_root):
     vels = os.path.join(ref_root, 'tests', 'datafiles', '51Peg', 'RV', '51peg.vels')
     arr = np.loadtxt(vels)
     np.savez_compressed(os.path.join(HERE, '51peg_rv.npz'), data=arr)
+    gj876_fixture(ref_root)
     out = {}
     specs = {}
     for name, (spec, data, thetas) in kat_cases(arr).items():
@@ -81,6 +85,17 @@ def main(ref_root):
     smartsetter_fixture(ref_root, arr)
     hip21850_fixture(ref_root)
     am_fixture(ref_root)
+
+
+def gj876_fixture(ref_root):
+    """The GJ 876 RV files as the reference's DataWrapper lists them (sorted)."""
+    folder = os.path.join(ref_root, 'tests', 'datafiles', 'GJ876', 'RV')
+    names = [fn for fn in sorted(os.listdir(folder)) if fn != '.DS_Store']
+    out = {'names': np.array(names)}
+    for k, fn in enumerate(names):
+        out[f'ins_{k}'] = np.loadtxt(os.path.join(folder, fn), ndmin=2)[:, :3]
+    np.savez_compressed(os.path.join(HERE, 'gj876_rv.npz'), **out)
+    print('gj876_rv:', names)
 
 
 class _Col:
