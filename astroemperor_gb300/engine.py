@@ -466,9 +466,13 @@ class PTSampler:
         CUDA graph (``emp_pt_run_host``); returns after the copy back."""
         if not self._initialised:
             raise RuntimeError('run_mcmc or set_positions first')
-        if not h_state.is_pinned() or h_state.numel() != self._state.numel() or \
-                h_state.dtype != torch.float64:
+        if h_state.numel() != self._state.numel() or h_state.dtype != torch.float64:
             raise ValueError('h_state must be the pinned float64 buffer of host_state()')
+        # the pinned-memory query once per buffer (it costs a driver call)
+        if getattr(self, '_pinned_ptr', None) != h_state.data_ptr():
+            if not h_state.is_pinned():
+                raise ValueError('h_state must be the pinned float64 buffer of host_state()')
+            self._pinned_ptr = h_state.data_ptr()
         if self.cap == 0:
             self._grow(1)
         st = self._state_struct(1)
