@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import _native as N
-from .engine import PRECISIONS, default_betas, perm_units
+from .engine import PRECISIONS, am_descriptor, default_betas, perm_units
 from .model import ReddModel
 
 GOLDEN = 0x9E3779B97F4A7C15
@@ -83,6 +83,16 @@ class BatchContext:
         self.h = h
         if self.lib.emp_num_systems(self.h) != S:
             raise RuntimeError('native handle reports a different system count')
+        if getattr(models[0], 'am_data', None) is not None:
+            # joint RV + astrometry: one descriptor per system, in order
+            ams = (N.EmpAmDesc * S)()
+            keep = []
+            for s, m in enumerate(models):
+                if getattr(m, 'am_data', None) is None:
+                    raise ValueError(f'system {s}: astrometric and RV-only systems in one batch')
+                ams[s], arrs = am_descriptor(m.am_data)
+                keep.append(arrs)
+            N.call('emp_set_astrometry', self.h, ams)
 
     def close(self):
         if getattr(self, 'h', None):

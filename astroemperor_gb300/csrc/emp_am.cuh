@@ -106,14 +106,17 @@ __device__ inline void am_planet(const double* v, double plx, double* pc) {
     pc[9] = -beta * H * plx / 206265e3;
 }
 
-__global__ void __launch_bounds__(kAmThreads) k_am(KArgs A) {
+__global__ void __launch_bounds__(kAmThreads) k_am(KArgs A0) {
+    // system blockIdx.y of a batch handle as a one-system launch
+    KArgs A = sys_rows(A0, blockIdx.y);
+    if (A0.sys_off != nullptr && A0.am_rv != nullptr) A.am_rv = A0.am_rv + (size_t)blockIdx.y * A0.nwalk;
     __shared__ AmSmem sm[kAmThreads / 32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rowr = blockIdx.x * (kAmThreads / 32) + warp;
     const bool live = rowr < A.nwalk;
     const int row = live ? rowr : A.nwalk - 1;
     const emp_model_desc* md = A.md;
-    const AmDev& d = A.am;
+    const AmDev d = A0.am_sys != nullptr ? A0.am_sys[blockIdx.y] : A0.am;
     AmSmem& S = sm[warp];
     const double* th;
     const double lp = gp_row(A, row, &th);

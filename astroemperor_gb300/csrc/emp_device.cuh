@@ -181,6 +181,7 @@ struct KArgs {
     // adds the astrometric term and finishes every mode
     double* am_rv;             // [nwalk] (stretch)
     AmDev am;
+    const AmDev* am_sys;       // [S] one per system of a batch handle (null: am)
 };
 
 

@@ -137,24 +137,17 @@ __device__ inline double gp_row(const KArgs& A, int row, const double** th) {
 // systems' epochs ([epochs][rows]), row arrays [systems][rows].  In stretch
 // mode the proposals carry the batch's own slot numbers, so the slot arrays
 // stay whole and the temperatures and acceptance counts move instead.
-template <int M>
-__device__ __forceinline__ KArgs gp_system(const KArgs& B, int s) {
+__device__ __forceinline__ KArgs sys_rows(const KArgs& B, int s) {
     KArgs A = B;
     if (B.sys_off == nullptr) return A;
     const int64_t e0 = B.sys_off[s];
     const size_t rows = (size_t)B.nwalk, ds = (size_t)B.dstride;
-    const size_t ep = (size_t)e0 * rows, so = (size_t)s * rows;
+    const size_t so = (size_t)s * rows;
     A.md = B.md + s;
     A.d.t = B.d.t + e0;
     A.d.n = (int)(B.sys_off[s + 1] - e0);
-    A.gp_r = B.gp_r + ep;
-    A.gp_e = B.gp_e + ep;
-    A.gp_u = B.gp_u + ep * M;
-    A.gp_v = B.gp_v + ep * M;
-    A.gp_ph = B.gp_ph + ep * M;
-    A.gp_asum = B.gp_asum + so;
-    A.gp_meta = B.gp_meta + so;
-    A.gp_prop = B.gp_prop + so * ds;
+    if (B.gp_meta != nullptr) A.gp_meta = B.gp_meta + so;
+    if (B.gp_prop != nullptr) A.gp_prop = B.gp_prop + so * ds;
     if (B.mode == kModeLogpost) {
         A.theta = B.theta + so * ds;
         A.logprior = B.logprior + so;
@@ -169,6 +162,23 @@ __device__ __forceinline__ KArgs gp_system(const KArgs& B, int s) {
         A.betas = B.betas + (size_t)s * B.T;
         A.accepted = B.accepted + (size_t)s * B.T * B.W;
     }
+    return A;
+}
+
+// the GP kernels' view: the rows above and the GP row buffers
+template <int M>
+__device__ __forceinline__ KArgs gp_system(const KArgs& B, int s) {
+    KArgs A = sys_rows(B, s);
+    if (B.sys_off == nullptr) return A;
+    const size_t ep = (size_t)B.sys_off[s] * (size_t)B.nwalk, so = (size_t)s * (size_t)B.nwalk;
+    A.gp_r = B.gp_r + ep;
+    A.gp_e = B.gp_e + ep;
+    if (B.gp_u != nullptr) {
+        A.gp_u = B.gp_u + ep * M;
+        A.gp_v = B.gp_v + ep * M;
+        A.gp_ph = B.gp_ph + ep * M;
+    }
+    A.gp_asum = B.gp_asum + so;
     return A;
 }
 

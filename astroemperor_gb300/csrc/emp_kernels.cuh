@@ -1386,11 +1386,11 @@ __global__ void __launch_bounds__(NT, (PREC == EMP_PREC_MIXED && NT == 128) ? 5 
             GPMeta m;
             m.lp = lp; m.z = z; m.uword = uword; m.slot = slot_j;
             m.pos = t_idx * A.W + j_idx; m.t = t_idx;
-            A.gp_meta[wk] = m;
-            A.am_rv[wk] = logl;
+            A.gp_meta[(size_t)sys * A.nwalk + wk] = m;       // rows [S][nwalk]
+            A.am_rv[(size_t)sys * A.nwalk + wk] = logl;
         }
         if (active) {
-            double* dst = A.gp_prop + (size_t)wk * ds;
+            double* dst = A.gp_prop + ((size_t)sys * A.nwalk + wk) * ds;
             for (int d = r; d < n_free; d += L) dst[d] = thp[d];
         }
     } else if (A.mode == kModeLogpost) {

@@ -131,6 +131,7 @@ struct emp_handle {
     // row of a stretch half-step the proposal, its meta and its RV logL
     bool am_set = false;
     AmDev am{};
+    const AmDev* am_sys = nullptr;   // [S] on the device, a batch handle's per-system data
     void* am_buf = nullptr;
     void* am_rows_buf = nullptr;
     int64_t am_rows = 0;
@@ -446,6 +447,7 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     if (am) {
         if (!h->am_set) return fail(EMP_E_INVALID, "the model has astrometry but emp_set_astrometry was not called");
         a.am = h->am;
+        a.am_sys = h->am_sys;
         if (a.mode == kModeStretch) {
             if (a.nwalk > h->am_rows)
                 return fail(EMP_E_INVALID, "astrometry rows hold %lld walkers, launch has %d", (long long)h->am_rows,
@@ -472,22 +474,23 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     if (gp) return launch_gp(h, a, s, prec);
     if (am) {
         const int rows_per_cta = kAmThreads / 32;
-        get_kernel_am()<<<(a.nwalk + rows_per_cta - 1) / rows_per_cta, kAmThreads, 0, s>>>(a);
+        get_kernel_am()<<<dim3((unsigned)((a.nwalk + rows_per_cta - 1) / rows_per_cta), (unsigned)h->n_sys),
+                          kAmThreads, 0, s>>>(a);
         g_launches.fetch_add(1);
         CUDA_TRY(cudaGetLastError());
     }
     return EMP_OK;
 }
 
-// Stretch buffers of the astrometric term for up to `rows` walker rows
-// (proposal, meta, RV logL); allocated outside any capture, growing drops
-// the captured sweep graphs.
+// Stretch buffers of the astrometric term for up to `rows` walker rows per
+// system (proposal, meta, RV logL; [systems][rows]); allocated outside any
+// capture, growing drops the captured sweep graphs.
 int am_reserve(emp_handle* h, int64_t rows) {
     if (!h->md.am_on || rows <= h->am_rows) return EMP_OK;
-    const size_t D = (size_t)std::max(h->lay[1], 1);
+    const size_t D = (size_t)std::max(h->lay[1], 1), R = (size_t)rows * (size_t)h->n_sys;
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t b_prop = up(8 * D * (size_t)rows), b_meta = up(sizeof(GPMeta) * (size_t)rows);
-    const size_t b_rv = up(8 * (size_t)rows);
+    const size_t b_prop = up(8 * D * R), b_meta = up(sizeof(GPMeta) * R);
+    const size_t b_rv = up(8 * R);
     h->gc.reset();
     h->gch.reset();
     if (h->am_rows_buf) {
@@ -923,8 +926,8 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
             return fail(EMP_E_UNSUPPORTED, "system %d: MA order %d differs from system 0's %d", s,
                         ma_order_on_device(m), q);
         if ((rc = check_system(m, data, s, &nsys[s]))) return rc;
-        if (S > 1 && m->am_on)
-            return fail(EMP_E_UNSUPPORTED, "system %d: astrometric likelihoods take a one-system handle", s);
+        if ((m->am_on != 0) != (models[0].am_on != 0))
+            return fail(EMP_E_UNSUPPORTED, "system %d: astrometric and RV-only systems in one batch", s);
         total += nsys[s];
         lay[0] = std::max(lay[0], m->n_full);
         lay[1] = std::max(lay[1], m->n_free);
@@ -982,6 +985,7 @@ int create_impl(const emp_model_desc* models, int S, const emp_dataset_desc* dat
             if (S > 65535) return fail(EMP_E_SIZE, "%d systems with GP likelihoods (at most 65535)", S);
         }
     }
+    if (models[0].am_on && S > 65535) return fail(EMP_E_SIZE, "%d systems with astrometry (at most 65535)", S);
 
     emp_handle* h = new (std::nothrow) emp_handle();
     if (!h) return fail(EMP_E_INVALID, "out of host memory");
@@ -1152,41 +1156,64 @@ int emp_set_astrometry(emp_handle* h, const emp_am_desc* am) {
     if (!h) return fail(EMP_E_INVALID, "handle is NULL");
     if (!am) return fail(EMP_E_INVALID, "astrometry descriptor is NULL");
     if (!h->md.am_on) return fail(EMP_E_INVALID, "the handle's model has no astrometry");
-    if (am->n_hipp < 1 || am->n_gost < 5)
-        return fail(EMP_E_INVALID, "astrometry needs Hipparcos abscissae and at least 5 Gaia epochs");
-    if (!am->catalogs || !am->inv_cov || !am->log_det_cov || !am->astro_gost || !am->hipp || !am->gost || !am->gsv)
-        return fail(EMP_E_INVALID, "an astrometry array is NULL");
-    const size_t nh = (size_t)am->n_hipp, ng = (size_t)am->n_gost;
-    const size_t counts[7] = {21, 75, 3, 10, 7 * nh, 4 * ng, 10 * ng};
-    const double* srcs[7] = {am->catalogs, am->inv_cov, am->log_det_cov, am->astro_gost, am->hipp, am->gost,
-                             am->gsv};
-    size_t total = 0, offs[7];
-    for (int k = 0; k < 7; ++k) {
-        offs[k] = total;
-        total += (8 * counts[k] + 255) & ~(size_t)255;
-        for (size_t i = 0; i < counts[k]; ++i)
-            if (!isfinite(srcs[k][i])) return fail(EMP_E_INVALID, "astrometry array %d holds a non-finite value", k);
+    // one descriptor per system (a batch handle's systems in order); every
+    // array is checked before anything reaches the device
+    const int S = h->n_sys;
+    std::vector<size_t> offs((size_t)S * 7);
+    size_t total = 0;
+    for (int sy = 0; sy < S; ++sy) {
+        const emp_am_desc* a = am + sy;
+        if (a->n_hipp < 1 || a->n_gost < 5)
+            return fail(EMP_E_INVALID, "system %d: astrometry needs Hipparcos abscissae and at least 5 Gaia epochs",
+                        sy);
+        if (!a->catalogs || !a->inv_cov || !a->log_det_cov || !a->astro_gost || !a->hipp || !a->gost || !a->gsv)
+            return fail(EMP_E_INVALID, "system %d: an astrometry array is NULL", sy);
+        const size_t nh = (size_t)a->n_hipp, ng = (size_t)a->n_gost;
+        const size_t counts[7] = {21, 75, 3, 10, 7 * nh, 4 * ng, 10 * ng};
+        const double* srcs[7] = {a->catalogs, a->inv_cov, a->log_det_cov, a->astro_gost, a->hipp, a->gost, a->gsv};
+        for (int k = 0; k < 7; ++k) {
+            offs[(size_t)sy * 7 + k] = total;
+            total += (8 * counts[k] + 255) & ~(size_t)255;
+            for (size_t i = 0; i < counts[k]; ++i)
+                if (!isfinite(srcs[k][i]))
+                    return fail(EMP_E_INVALID, "system %d: astrometry array %d holds a non-finite value", sy, k);
+        }
     }
+    const size_t o_dev = total;
+    if (S > 1) total += sizeof(AmDev) * (size_t)S;
     if (h->am_buf) {
         cudaFree(h->am_buf);
         h->am_buf = nullptr;
+        h->am_sys = nullptr;
         h->am_set = false;
     }
     CUDA_TRY(cudaMalloc(&h->am_buf, total));
     char* b = (char*)h->am_buf;
-    for (int k = 0; k < 7; ++k) CUDA_TRY(cudaMemcpy(b + offs[k], srcs[k], 8 * counts[k], cudaMemcpyHostToDevice));
-    AmDev d{};
-    d.n_hipp = am->n_hipp;
-    d.n_gost = am->n_gost;
-    d.catalogs = (const double*)(b + offs[0]);
-    d.inv_cov = (const double*)(b + offs[1]);
-    d.log_det_cov = (const double*)(b + offs[2]);
-    d.astro_gost = (const double*)(b + offs[3]);
-    d.hipp = (const double*)(b + offs[4]);
-    d.gost = (const double*)(b + offs[5]);
-    d.gsv = (const double*)(b + offs[6]);
-    d.common_t = am->common_t;
-    h->am = d;
+    std::vector<AmDev> devs((size_t)S);
+    for (int sy = 0; sy < S; ++sy) {
+        const emp_am_desc* a = am + sy;
+        const size_t nh = (size_t)a->n_hipp, ng = (size_t)a->n_gost;
+        const size_t counts[7] = {21, 75, 3, 10, 7 * nh, 4 * ng, 10 * ng};
+        const double* srcs[7] = {a->catalogs, a->inv_cov, a->log_det_cov, a->astro_gost, a->hipp, a->gost, a->gsv};
+        const size_t* o = &offs[(size_t)sy * 7];
+        for (int k = 0; k < 7; ++k) CUDA_TRY(cudaMemcpy(b + o[k], srcs[k], 8 * counts[k], cudaMemcpyHostToDevice));
+        AmDev& d = devs[(size_t)sy];
+        d.n_hipp = a->n_hipp;
+        d.n_gost = a->n_gost;
+        d.catalogs = (const double*)(b + o[0]);
+        d.inv_cov = (const double*)(b + o[1]);
+        d.log_det_cov = (const double*)(b + o[2]);
+        d.astro_gost = (const double*)(b + o[3]);
+        d.hipp = (const double*)(b + o[4]);
+        d.gost = (const double*)(b + o[5]);
+        d.gsv = (const double*)(b + o[6]);
+        d.common_t = a->common_t;
+    }
+    if (S > 1) {
+        CUDA_TRY(cudaMemcpy(b + o_dev, devs.data(), sizeof(AmDev) * (size_t)S, cudaMemcpyHostToDevice));
+        h->am_sys = (const AmDev*)(b + o_dev);
+    }
+    h->am = devs[0];
     h->am_set = true;
     h->gc.reset();
     h->gch.reset();

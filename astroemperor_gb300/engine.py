@@ -51,6 +51,28 @@ def perm_units(W: int) -> np.ndarray:
     return np.array([m for m in range(1, max(W, 2)) if math.gcd(m, W) == 1] or [1], dtype=np.int32)
 
 
+def am_descriptor(am):
+    """(emp_am_desc, arrays it points into) of the astrometric data of a
+    joint fit; the arrays must outlive the emp_set_astrometry call."""
+    f64 = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+    ng = am.n_gost
+    gsv = np.zeros((2, 5, ng))
+    for c, cat in enumerate(('GDR2', 'GDR3')):
+        gsv[c][:, am.masks[cat]] = am.gsv[cat]
+    arrs = {
+        'catalogs': f64(am.catalogs), 'inv_cov': f64(am.inv_cov), 'log_det_cov': f64(am.log_det_cov),
+        'astro_gost': f64(am.astro_gost),
+        'hipp': f64(np.stack([am.hipp[k] for k in ('BJD', 'EPOCH', 'PARF', 'CPSI', 'SPSI', 'RES', 'SRES')])),
+        'gost': f64(np.stack([am.gost[k] for k in ('BJD', 'CPSI', 'SPSI', 'parf')])),
+        'gsv': f64(gsv)}
+    d = N.EmpAmDesc()
+    d.n_hipp, d.n_gost = am.n_hipp, ng
+    for k, v in arrs.items():
+        setattr(d, k, v.ctypes.data)
+    d.common_t = float(am.common_t)
+    return d, arrs
+
+
 class Context:
     """Native handle: compiled model + dataset resident on one GPU."""
 
@@ -84,22 +106,7 @@ class Context:
 
     def _set_astrometry(self, am):
         """Upload the astrometric data of a joint fit (emp_set_astrometry)."""
-        f64 = lambda x: np.ascontiguousarray(x, dtype=np.float64)
-        ng = am.n_gost
-        gsv = np.zeros((2, 5, ng))
-        for c, cat in enumerate(('GDR2', 'GDR3')):
-            gsv[c][:, am.masks[cat]] = am.gsv[cat]
-        arrs = {
-            'catalogs': f64(am.catalogs), 'inv_cov': f64(am.inv_cov), 'log_det_cov': f64(am.log_det_cov),
-            'astro_gost': f64(am.astro_gost),
-            'hipp': f64(np.stack([am.hipp[k] for k in ('BJD', 'EPOCH', 'PARF', 'CPSI', 'SPSI', 'RES', 'SRES')])),
-            'gost': f64(np.stack([am.gost[k] for k in ('BJD', 'CPSI', 'SPSI', 'parf')])),
-            'gsv': f64(gsv)}
-        d = N.EmpAmDesc()
-        d.n_hipp, d.n_gost = am.n_hipp, ng
-        for k, v in arrs.items():
-            setattr(d, k, v.ctypes.data)
-        d.common_t = float(am.common_t)
+        d, keep = am_descriptor(am)
         N.call('emp_set_astrometry', self.h, C.byref(d))
 
     def close(self):

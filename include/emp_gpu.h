@@ -221,8 +221,10 @@ int emp_destroy(emp_handle* h);
    likelihoods (at most 65535 systems then): the GP kernels run every
    system with the largest state dimension of the batch, as a power of two
    (a system's unused dimensions stay zero; a system without GP terms then
-   gets the Gaussian likelihood through the same recursion).  Astrometric
-   models take a one-system handle (EMP_E_UNSUPPORTED). */
+   gets the Gaussian likelihood through the same recursion).  Joint RV +
+   astrometry models: every system or none (EMP_E_UNSUPPORTED otherwise),
+   with one emp_set_astrometry descriptor per system, at most 65535
+   systems. */
 int emp_create_batch(const emp_model_desc* models, const emp_dataset_desc* data,
                      emp_handle** out);
 int emp_num_systems(emp_handle* h);
@@ -263,8 +265,10 @@ int emp_logpost_grad(emp_handle* h, const double* theta, int B, double* logl,
 
 /* Replaces: the astrometric data prologue of the generated script
    (emp_model.py:609-706) for a handle whose model has am_on: copies the
-   arrays to the device.  Call once after emp_create, outside any stream
-   capture.  One-system handles only. */
+   arrays to the device.  Call once after emp_create (or emp_create_batch),
+   outside any stream capture.  For a batch handle `am` points to one
+   descriptor per system, in system order; every descriptor is checked
+   before anything is copied. */
 int emp_set_astrometry(emp_handle* h, const emp_am_desc* am);
 
 /* Replaces: my_model(theta) -> (model0, err20) (emp_model.py:706-781) for a

@@ -272,10 +272,11 @@ def test_create_rejects_bad_gp_and_hill_fields(lib, peg_arr):
     assert rc == N.EMP_E_UNSUPPORTED and 'Hill' in msg
 
 
-def test_astrometry_batch_rejected_before_touching_the_gpu(lib):
-    from tests.golden.cases import model_hip21850
+def test_mixed_astrometry_batch_rejected_before_touching_the_gpu(lib, peg_arr):
+    from tests.golden.cases import model_51peg, model_hip21850
     fix = np.load(os.path.join(os.path.dirname(__file__), 'golden', 'hip21850.npz'))
     m, d, _ = model_hip21850(fix)
-    parts = [(d.BJD, d.RV, d.eRV, d.Flag)] * 2
-    rc, msg = _batch(lib, [m, m], parts)
-    assert rc == N.EMP_E_UNSUPPORTED and 'one-system' in msg
+    m2, d2 = model_51peg(peg_arr, k=1, par=1)
+    parts = [(d.BJD, d.RV, d.eRV, d.Flag), (d2.BJD, d2.RV, d2.eRV, d2.Flag)]
+    rc, msg = _batch(lib, [m, m2], parts)
+    assert rc == N.EMP_E_UNSUPPORTED and 'astrometric and RV-only' in msg
