@@ -135,8 +135,9 @@ typedef struct emp_model_desc {
     /* Gaussian-process likelihood (support/likelihoods/02.like): with
        gp_nterms > 0 the log-likelihood is the celerite GP log-likelihood of the
        residuals with diagonal err2 instead of the independent Gaussian sum;
-       not combined with an MA that runs on the device (a per-instrument MA
-       under ma_quirk, the reference's no-op, is accepted) */
+       with an MA that runs on the device (global, or per instrument without
+       ma_quirk) the residuals are those after the MA recurrence, as 02.like's
+       gp_.mean = model gives them; not combined with am_on */
     int32_t gp_nterms;
     int32_t _pad2;
     int32_t gp_kind[EMP_MAX_GP_TERMS];
