@@ -12,6 +12,9 @@ System s uses the Philox key ``seed + s * 0x9E3779B97F4A7C15`` (mod 2^64),
 so its chain equals a one-system :class:`~astroemperor_gb300.engine.PTSampler`
 run with that seed and the same launch shape.  Arrays hold the systems
 back to back; parameter rows are padded to the largest free dimension.
+Systems may carry celerite GP blocks (with or without: the batch runs the
+largest GP state dimension) or, all of them, joint RV + astrometry data
+(one astrometry descriptor per system).
 """
 from __future__ import annotations
 
