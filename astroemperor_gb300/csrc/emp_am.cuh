@@ -106,6 +106,13 @@ __device__ inline void am_planet(const double* v, double plx, double* pc) {
     pc[9] = -beta * H * plx / 206265e3;
 }
 
+// PREC = EMP_PREC_MIXED solves Kepler's equation of each planet-epoch in
+// FP32 (kepler_f32_n: Halley iterations on the special function unit's
+// sin/cos, then one Newton step with an accurate sin/cos and the low parts
+// of the FP64-reduced mean anomaly and of e, E to ~1e-11); the
+// orbit enters the abscissae through amplitudes of a few mas, so its error
+// there stays below 1e-7 mas.  Everything else is FP64 in both precisions.
+template <int PREC>
 __global__ void __launch_bounds__(kAmThreads) k_am(KArgs A0) {
     // system blockIdx.y of a batch handle as a one-system launch
     KArgs A = sys_rows(A0, blockIdx.y);
@@ -169,7 +176,16 @@ __global__ void __launch_bounds__(kAmThreads) k_am(KArgs A0) {
                 if (Mr < 0.0) Mr += kTwoPi;
                 Mr -= kPi;
                 double sE, cE;
-                kepler_f64(Mr, pc[2], sE, cE);
+                if constexpr (PREC == EMP_PREC_MIXED) {
+                    const float mh = (float)Mr, eh = (float)pc[2];
+                    const float M1[1] = {mh}, L1[1] = {(float)(Mr - (double)mh)};
+                    float s1[1], c1[1];
+                    kepler_f32_n<1>(M1, L1, eh, (float)(pc[2] - (double)eh), s1, c1);
+                    sE = s1[0];
+                    cE = c1[0];
+                } else {
+                    kepler_f64(Mr, pc[2], sE, cE);
+                }
                 const double X = cE - pc[2], Y = pc[3] * sE;
                 c0 += pc[4] * X + pc[5] * Y;
                 c1 += pc[6] * X + pc[7] * Y;

@@ -6,6 +6,7 @@ namespace emp {
 
 using KFn = void (*)(KArgs);
 
-KFn get_kernel_am() { return k_am; }
+// the astrometric kernel of a precision (EMP_PREC_FP64 or EMP_PREC_MIXED)
+KFn get_kernel_am(int prec) { return prec == EMP_PREC_MIXED ? k_am<EMP_PREC_MIXED> : k_am<EMP_PREC_FP64>; }
 
 }  // namespace emp

@@ -28,7 +28,7 @@ KFn get_kernel_mixed(int q, int lidx);
 using GFn = void (*)(GArgs);
 GFn get_kernel_grad(int q, int lidx);
 KFn get_kernel_gp(int M, int prep, int ff);
-KFn get_kernel_am();
+KFn get_kernel_am(int prec);
 }  // namespace emp
 
 using namespace emp;
@@ -474,7 +474,7 @@ int launch_eval(emp_handle* h, int prec, KArgs& a, cudaStream_t s, unsigned* cou
     if (gp) return launch_gp(h, a, s, prec);
     if (am) {
         const int rows_per_cta = kAmThreads / 32;
-        get_kernel_am()<<<dim3((unsigned)((a.nwalk + rows_per_cta - 1) / rows_per_cta), (unsigned)h->n_sys),
+        get_kernel_am(prec)<<<dim3((unsigned)((a.nwalk + rows_per_cta - 1) / rows_per_cta), (unsigned)h->n_sys),
                           kAmThreads, 0, s>>>(a);
         g_launches.fetch_add(1);
         CUDA_TRY(cudaGetLastError());

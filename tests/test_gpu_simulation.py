@@ -14,7 +14,9 @@ Reference values recorded by that notebook (10 temperatures x 500 walkers x
   jitter 2.961 with the printed (-, +) ranges (01_51peg_basic.ipynb:548-562, 617)
 
 BIC is held to +-0.2 (the likelihood at the maximum-posterior sample to
-+-0.1).  The fit is held to twice the printed range of each parameter
++-0.1), chi2 (268.680, 01_51peg_basic.ipynb:622) to +-12 (it follows the
+jitter of the maximum-posterior sample, which the sampler draws anew on
+every launch shape the autotuner picks).  The fit is held to twice the printed range of each parameter
 (3 decimals printed, so at least 1e-3); phase and omega are individually
 weakly constrained at e ~ 0.01, so the mean longitude phase + omega, which
 the data fix to ~0.01 rad, is held to 0.05 rad.
@@ -61,7 +63,10 @@ def test_autorun_51peg_reproduces_the_reference_notebook(peg_arr, lib, cuda, tmp
     assert [x['k'] for x in h] == [0, 1]
     assert h[0]['BIC'] == pytest.approx(2628.678, abs=0.2)
     assert h[1]['BIC'] == pytest.approx(1777.801, abs=0.2)
-    assert sim.chi2 == pytest.approx(268.680, abs=1.0)
+    # chi2 = sum r^2 / (sigma^2 + jitter^2) at the maximum-posterior sample
+    # moves by ~40 per m/s of that sample's jitter (the printed jitter range
+    # is -0.144 / +0.571 m/s), so it is held to +-12, twice the lower range
+    assert sim.chi2 == pytest.approx(268.680, abs=12.0)
 
     # the k = 1 model: Keplerian (param. 1), offset, jitter; the jitter limit
     # was narrowed between the runs, the Keplerian started in its k = 0 ranges
