@@ -9,7 +9,8 @@ rounding (2.5e-8 mas per ulp of 60 degrees) moves the Gaia term by up to
 the reference's own functions to 1e-12, against the same formulas with the
 propagation in long double).  The device forms the scan positions as offsets
 from the DR3 position and is compared with the long-double value:
-FP64 logL relative 5e-10 (the astrometric term is FP64 in both precisions;
+FP64 logL relative 5e-10 (the astrometric term is FP64; the mixed precision
+solves its Kepler equations in FP32 with a float-float correction, E to ~1e-11;
 what remains is the Hipparcos-epoch barycentre, propagated through absolute
 angles as the reference does, where one ulp moves the Hipparcos term by up
 to 5.4e-11 of the total; measured 1.1e-10), mixed 1e-6, logprior 1e-13 (the
