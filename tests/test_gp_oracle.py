@@ -57,6 +57,20 @@ def test_sum_of_terms_equals_dense():
     assert abs(a - b) <= RTOL * abs(b)
 
 
+def test_zero_amplitude_terms_give_the_gaussian_likelihood():
+    """A state dimension whose U is zero adds nothing to D_n or z_n, so the
+    recursion of a system without GP terms (all dimensions padding, as a
+    batch handle runs it beside GP systems) is the independent Gaussian
+    log-likelihood -0.5 sum(r^2 / err2 + log err2) - 0.5 N log 2 pi."""
+    rng = np.random.default_rng(11)
+    t, r, diag = _series(rng, 150)
+    gauss = -0.5 * np.sum(r * r / diag + np.log(diag)) - 0.5 * len(t) * np.log(2 * np.pi)
+    for terms in ([(gp.GP_REAL, [0.0, 0.3])], [(gp.GP_SHO, [0.0, 0.9, 3.0])],
+                  [(gp.GP_ROTATION, [0.0, 12.0, 0.8, 1.5, 0.4])]):
+        co = gp.coefficients(terms)
+        assert gp.semisep_loglike(t, r, diag, co) == pytest.approx(gauss, rel=1e-14)
+
+
 def test_sho_parameterisations_agree():
     # (sigma, rho, tau) and the equivalent (S0, w0, Q) give one kernel
     sigma, rho, tau = 2.0, 7.0, 15.0
